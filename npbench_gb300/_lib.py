@@ -1,0 +1,75 @@
+"""ctypes binding of libnpbgb.so (the C ABI declared in include/npbgb.h).
+
+The library is loaded from this package directory.  There is no fallback: if
+it is missing or fails to load, every entry point raises ``RuntimeError``
+telling how to build it (``python -m npbench_gb300.build``).
+"""
+import ctypes
+import os
+import threading
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libnpbgb.so")
+
+NPBGB_OK = 0
+NPBGB_ERR_ARG = 1
+NPBGB_ERR_DTYPE = 2
+NPBGB_ERR_CUDA = 3
+NPBGB_ERR_TIMEOUT = 4
+NPBGB_ERR_NOMEM = 5
+NPBGB_ERR_STATE = 6
+NPBGB_F64 = 0
+NPBGB_F32 = 1
+
+# Every symbol include/npbgb.h declares, with its ctypes signature.
+_i32, _i64, _vp, _cp = ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p, ctypes.c_char_p
+SIGNATURES = {
+    "npbgb_version": (_cp, []),
+    "npbgb_last_error": (_cp, []),
+    "npbgb_status_string": (_cp, [_i32]),
+    "npbgb_jacobi2d": (_i32, [_vp, _vp, _i64, _i64, _i32, _i32, _vp]),
+    "npbgb_heat3d": (_i32, [_vp, _vp, _i64, _i64, _i64, _i32, _i32, _vp]),
+    "npbgb_hdiff": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i32, _vp]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+class NpbgbError(RuntimeError):
+    """A libnpbgb entry point returned a non-OK status."""
+
+    def __init__(self, status, where, message):
+        super().__init__(f"{where}: {message} (status {status})")
+        self.status = status
+
+
+def load():
+    """Load and bind libnpbgb.so (once per process)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(
+                    f"{LIB_PATH} is not built; run `python -m npbench_gb300.build` "
+                    "(or __graft_entry__.build()) -- there is no CPU fallback")
+            lib = ctypes.CDLL(LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = lib
+    return _lib
+
+
+def check(status, where):
+    """Raise NpbgbError for a non-OK status, with the library's message."""
+    if status != NPBGB_OK:
+        lib = load()
+        msg = lib.npbgb_last_error().decode(errors="replace")
+        if not msg:
+            msg = lib.npbgb_status_string(status).decode()
+        raise NpbgbError(status, where, msg)
+
+
+def version():
+    return load().npbgb_version().decode()

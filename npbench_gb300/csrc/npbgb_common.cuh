@@ -1,0 +1,51 @@
+// Shared definitions for the libnpbgb CUDA sources (sm_103a only).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+
+#include "../../include/npbgb.h"
+
+namespace npbgb {
+
+// Records a message for npbgb_last_error() and returns `code`.
+int32_t set_error(int32_t code, const char* fmt, ...);
+
+// Maps a CUDA error to a status, recording the CUDA message.
+inline int32_t cuda_status(cudaError_t e, const char* where) {
+  if (e == cudaSuccess) return NPBGB_OK;
+  return set_error(NPBGB_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+#define NPBGB_CHECK_LAUNCH(where)                                      \
+  do {                                                                 \
+    cudaError_t _e = cudaGetLastError();                               \
+    if (_e != cudaSuccess) return ::npbgb::cuda_status(_e, where);     \
+  } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 152;
+  }
+  return n;
+}
+
+inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Correctly rounded IEEE operations with no contraction into FMA, so that each
+// result is rounded exactly once per source operator, as NumPy's ufuncs do.
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+
+}  // namespace npbgb

@@ -1,0 +1,170 @@
+"""NPBench-signature stencil kernels running on libnpbgb's sm_103a CUDA code.
+
+These are drop-ins for the reference NumPy kernels:
+
+* ``jacobi_2d_kernel(TSTEPS, A, B)``   -- polybench/jacobi_2d/jacobi_2d_numpy.py:4
+* ``heat_3d_kernel(TSTEPS, A, B)``     -- polybench/heat_3d/heat_3d_numpy.py:4
+* ``hdiff(in_field, out_field, coeff)`` -- weather_stencils/hdiff/hdiff_numpy.py:5
+
+Arguments are updated in place and nothing is returned, as in the reference.
+They may be
+
+* ``torch.Tensor`` on a CUDA device (the framework plugin's path): the kernels
+  run on the tensors' current stream and return without synchronising;
+* ``numpy.ndarray`` (host): the arrays are copied to the current CUDA device,
+  updated there and copied back into the same NumPy arrays before returning.
+
+Results are bit-identical to the reference NumPy kernels for float64 and
+float32 (hdiff: float64 only).  Errors raise ``TypeError`` (dtype),
+``ValueError`` (shape, device, aliasing) or ``npbench_gb300.NpbgbError``
+(a status from the library).  There is no CPU fallback: without a CUDA device
+or without libnpbgb.so these functions raise.
+"""
+import numpy as np
+
+from . import _lib
+
+__all__ = ["jacobi_2d_kernel", "heat_3d_kernel", "hdiff"]
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _dtype_code(dtype, allowed=(np.float64, np.float32)):
+    torch = _torch()
+    table = {torch.float64: _lib.NPBGB_F64, torch.float32: _lib.NPBGB_F32,
+             np.dtype(np.float64): _lib.NPBGB_F64, np.dtype(np.float32): _lib.NPBGB_F32}
+    allowed_codes = {_lib.NPBGB_F64 if a == np.float64 else _lib.NPBGB_F32 for a in allowed}
+    code = table.get(dtype)
+    if code is None or code not in allowed_codes:
+        raise TypeError(f"unsupported dtype {dtype}; expected one of "
+                        f"{[np.dtype(a).name for a in allowed]}")
+    return code
+
+
+class _DeviceView:
+    """Contiguous CUDA tensors standing for the caller's arrays during one call.
+
+    For CUDA tensors that are already contiguous the tensors themselves are
+    used (no copy).  Otherwise a contiguous device copy is made and written
+    back on ``finish()`` into the caller's object, which keeps its identity.
+    """
+
+    def __init__(self, arrays, writable):
+        torch = _torch()
+        self.orig = arrays
+        self.writable = writable
+        self.dev = []
+        first = arrays[0]
+        if isinstance(first, torch.Tensor):
+            if not all(isinstance(a, torch.Tensor) for a in arrays):
+                raise TypeError("mix of torch tensors and other arrays")
+            device = first.device
+            if device.type != "cuda":
+                raise ValueError(f"tensors must be on a CUDA device, got {device}")
+            for a in arrays:
+                if a.device != device:
+                    raise ValueError("all tensors must be on the same device")
+                self.dev.append(a if a.is_contiguous() else a.contiguous())
+            self.device = device
+            self.host = False
+        else:
+            if not torch.cuda.is_available():
+                raise RuntimeError("no CUDA device available (no CPU fallback)")
+            self.device = torch.device("cuda", torch.cuda.current_device())
+            for o, w in zip(arrays, writable):
+                if w and not isinstance(o, np.ndarray):
+                    raise TypeError("output arguments must be numpy arrays or CUDA tensors")
+            arrs = [np.asarray(a) for a in arrays]
+            self.dev = [torch.from_numpy(np.ascontiguousarray(a)).to(self.device) for a in arrs]
+            self.host = True
+
+    @property
+    def stream(self):
+        return _torch().cuda.current_stream(self.device).cuda_stream
+
+    def ptr(self, i):
+        return self.dev[i].data_ptr()
+
+    def finish(self):
+        for i, (o, d) in enumerate(zip(self.orig, self.dev)):
+            if not self.writable[i]:
+                continue
+            if self.host:
+                np.copyto(o, d.cpu().numpy())
+            elif d is not o:
+                o.copy_(d)
+
+
+def _check_same(arrays, names):
+    a0 = arrays[0]
+    for a, n in zip(arrays[1:], names[1:]):
+        if tuple(a.shape) != tuple(a0.shape):
+            raise ValueError(f"{n} has shape {tuple(a.shape)}, {names[0]} has {tuple(a0.shape)}")
+        if a.dtype != a0.dtype:
+            raise TypeError(f"{n} has dtype {a.dtype}, {names[0]} has {a0.dtype}")
+
+
+def _shares_memory(x, y):
+    torch = _torch()
+    if isinstance(x, torch.Tensor):
+        if x.numel() == 0 or y.numel() == 0:
+            return False
+        xs, xe = x.data_ptr(), x.data_ptr() + x.numel() * x.element_size()
+        ys, ye = y.data_ptr(), y.data_ptr() + y.numel() * y.element_size()
+        return xs < ye and ys < xe
+    return np.shares_memory(x, y)
+
+
+def _pingpong(name, entry, ndim, TSTEPS, A, B):
+    _check_same((A, B), ("A", "B"))
+    if len(A.shape) != ndim:
+        raise ValueError(f"{name}: expected {ndim}-D arrays, got shape {tuple(A.shape)}")
+    code = _dtype_code(A.dtype)
+    T = int(TSTEPS)
+    if not (-2**31 <= T < 2**31):
+        raise ValueError(f"{name}: TSTEPS out of int32 range")
+    if _shares_memory(A, B):
+        raise ValueError(f"{name}: A and B share memory")
+    lib = _lib.load()
+    torch = _torch()
+    view = _DeviceView((A, B), (True, True))
+    with torch.cuda.device(view.device):
+        st = entry(lib)(view.ptr(0), view.ptr(1), *[int(s) for s in A.shape], T, code, view.stream)
+        _lib.check(st, name)
+        view.finish()
+
+
+def jacobi_2d_kernel(TSTEPS, A, B):
+    """``kernel(TSTEPS, A, B)`` of polybench/jacobi_2d/jacobi_2d_numpy.py:4-10, on the GPU."""
+    _pingpong("jacobi_2d", lambda lib: lib.npbgb_jacobi2d, 2, TSTEPS, A, B)
+
+
+def heat_3d_kernel(TSTEPS, A, B):
+    """``kernel(TSTEPS, A, B)`` of polybench/heat_3d/heat_3d_numpy.py:4-20, on the GPU."""
+    _pingpong("heat_3d", lambda lib: lib.npbgb_heat3d, 3, TSTEPS, A, B)
+
+
+def hdiff(in_field, out_field, coeff):
+    """``hdiff(in_field, out_field, coeff)`` of weather_stencils/hdiff/hdiff_numpy.py:5-29."""
+    I, J, K = (int(s) for s in out_field.shape)
+    if tuple(in_field.shape) != (I + 4, J + 4, K):
+        raise ValueError(f"hdiff: in_field shape {tuple(in_field.shape)}, expected "
+                         f"{(I + 4, J + 4, K)}")
+    if tuple(coeff.shape) != (I, J, K):
+        raise ValueError(f"hdiff: coeff shape {tuple(coeff.shape)}, expected {(I, J, K)}")
+    for n, a in (("in_field", in_field), ("coeff", coeff)):
+        if a.dtype != out_field.dtype:
+            raise TypeError(f"hdiff: {n} dtype {a.dtype} differs from out_field {out_field.dtype}")
+        if _shares_memory(a, out_field):
+            raise ValueError(f"hdiff: {n} shares memory with out_field")
+    code = _dtype_code(out_field.dtype, allowed=(np.float64,))
+    lib = _lib.load()
+    torch = _torch()
+    view = _DeviceView((in_field, out_field, coeff), (False, True, False))
+    with torch.cuda.device(view.device):
+        st = lib.npbgb_hdiff(view.ptr(0), view.ptr(1), view.ptr(2), I, J, K, code, view.stream)
+        _lib.check(st, "hdiff")
+        view.finish()

@@ -1,0 +1,92 @@
+"""ctypes binding of the C oracle (oracle/stencils.c) -- TEST INFRASTRUCTURE ONLY.
+
+``load()`` builds ``oracle/_build/liboracle.so`` with ``make`` when it is
+missing and returns wrappers that take NumPy arrays and mutate them in place,
+with the same call shapes as the reference kernels:
+
+* ``jacobi_2d_kernel(TSTEPS, A, B)``   -- polybench/jacobi_2d/jacobi_2d_numpy.py:4
+* ``heat_3d_kernel(TSTEPS, A, B)``     -- polybench/heat_3d/heat_3d_numpy.py:4
+* ``hdiff(in_field, out_field, coeff)`` -- weather_stencils/hdiff/hdiff_numpy.py:5
+"""
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force=False):
+    """Compile the C oracle with its Makefile; returns the .so path."""
+    if force or not os.path.exists(_LIB_PATH):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def _bind(lib):
+    i64, i32, vp = ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p
+    for sfx in ("f64", "f32"):
+        getattr(lib, "oracle_jacobi2d_" + sfx).argtypes = [vp, vp, i64, i64, i32]
+        getattr(lib, "oracle_jacobi2d_half_" + sfx).argtypes = [vp, vp, i64, i64]
+        getattr(lib, "oracle_heat3d_" + sfx).argtypes = [vp, vp, i64, i64, i64, i32]
+        getattr(lib, "oracle_heat3d_half_" + sfx).argtypes = [vp, vp, i64, i64, i64]
+    lib.oracle_hdiff_f64.argtypes = [vp, vp, vp, i64, i64, i64]
+    return lib
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            _lib = _bind(ctypes.CDLL(build()))
+    return _lib
+
+
+def _sfx(*arrays):
+    dt = arrays[0].dtype
+    for a in arrays:
+        if a.dtype != dt or not a.flags.c_contiguous:
+            raise ValueError("oracle wants C-contiguous arrays of one dtype")
+    if dt == np.float64:
+        return "f64"
+    if dt == np.float32:
+        return "f32"
+    raise TypeError(f"unsupported dtype {dt}")
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def jacobi_2d_kernel(TSTEPS, A, B):
+    sfx = _sfx(A, B)
+    getattr(lib(), "oracle_jacobi2d_" + sfx)(_p(A), _p(B), A.shape[0], A.shape[1], int(TSTEPS))
+
+
+def heat_3d_kernel(TSTEPS, A, B):
+    sfx = _sfx(A, B)
+    getattr(lib(), "oracle_heat3d_" + sfx)(_p(A), _p(B), *A.shape, int(TSTEPS))
+
+
+def jacobi_2d_half_sweep(src, dst):
+    sfx = _sfx(src, dst)
+    getattr(lib(), "oracle_jacobi2d_half_" + sfx)(_p(src), _p(dst), *src.shape)
+
+
+def heat_3d_half_sweep(src, dst):
+    sfx = _sfx(src, dst)
+    getattr(lib(), "oracle_heat3d_half_" + sfx)(_p(src), _p(dst), *src.shape)
+
+
+def hdiff(in_field, out_field, coeff):
+    if _sfx(in_field, out_field, coeff) != "f64":
+        raise TypeError("hdiff oracle is float64 only")
+    I, J, K = out_field.shape
+    if in_field.shape != (I + 4, J + 4, K) or coeff.shape != (I, J, K):
+        raise ValueError("hdiff shapes: in (I+4, J+4, K), out/coeff (I, J, K)")
+    lib().oracle_hdiff_f64(_p(in_field), _p(out_field), _p(coeff), I, J, K)

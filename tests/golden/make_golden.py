@@ -1,0 +1,147 @@
+"""Generate the golden vectors for the stencil path from the reference itself.
+
+Run in a checkout that has the NPBench sources (default ``/root/reference``):
+
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--ref DIR]
+
+It imports the reference's own NumPy kernels
+
+* ``npbench.benchmarks.polybench.jacobi_2d.jacobi_2d_numpy.kernel``
+* ``npbench.benchmarks.polybench.heat_3d.heat_3d_numpy.kernel``
+* ``npbench.benchmarks.weather_stencils.hdiff.hdiff_numpy.hdiff``
+
+and their ``initialize`` functions, runs them on seeded inputs, and writes
+
+* ``cases.npz``     -- inputs and outputs of the small cases (exact arrays);
+* ``manifest.json`` -- every case with its parameters, and for the larger
+  preset cases SHA-256 digests of the inputs and outputs instead of arrays.
+
+The tests under ``tests/`` compare the oracle and the CUDA kernels with these
+files; none of them reads the reference at run time.
+"""
+import argparse
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def sha(a):
+    a = np.ascontiguousarray(a)
+    return hashlib.sha256(a.tobytes()).hexdigest()
+
+
+def special_values(rng, shape, dtype):
+    """U[0,1) sprinkled with signed zeros, negatives, tiny, huge, inf and nan."""
+    a = rng.random(shape).astype(dtype)
+    flat = a.reshape(-1)
+    info = np.finfo(dtype)
+    pool = np.array([0.0, -0.0, -0.75, 1.5, info.tiny, info.tiny * 2 ** -3, -info.tiny / 4,
+                     info.max / 1.5, -info.max / 3, np.inf, -np.inf, np.nan, 1e-3, 3.0],
+                    dtype=dtype)
+    idx = rng.choice(flat.size, size=max(1, flat.size // 6), replace=False)
+    flat[idx] = pool[rng.integers(0, pool.size, size=idx.size)]
+    return a
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    sys.dont_write_bytecode = True
+    sys.path.insert(0, args.ref)
+    from npbench.benchmarks.polybench.jacobi_2d import jacobi_2d_numpy, jacobi_2d
+    from npbench.benchmarks.polybench.heat_3d import heat_3d_numpy, heat_3d
+    from npbench.benchmarks.weather_stencils.hdiff import hdiff_numpy, hdiff
+
+    arrays, cases = {}, []
+    rng = np.random.default_rng(20211)
+
+    def add_tsteps_case(bench, kern, name, tsteps, A, B, store=True, **meta):
+        a, b = A.copy(), B.copy()
+        kern(tsteps, a, b)
+        case = dict(name=name, bench=bench, tsteps=int(tsteps), dtype=A.dtype.name,
+                    shape=list(A.shape), **meta)
+        if store:
+            for k, v in (("A_in", A), ("B_in", B), ("A_out", a), ("B_out", b)):
+                arrays[f"{name}/{k}"] = v
+        else:
+            case.update(sha_A_in=sha(A), sha_B_in=sha(B), sha_A_out=sha(a), sha_B_out=sha(b))
+        cases.append(case)
+
+    # Jacobi-2D: empty/ragged interiors, non-square, step counts 0..17, both dtypes.
+    for dt in (np.float64, np.float32):
+        for shape in [(2, 2), (2, 6), (3, 3), (4, 4), (5, 7), (9, 4), (33, 47), (64, 65)]:
+            for T in ((0, 1, 2, 3, 17) if shape[0] * shape[1] < 100 else (2, 17)):
+                A = rng.random(shape).astype(dt)
+                B = rng.random(shape).astype(dt)
+                add_tsteps_case("jacobi_2d", jacobi_2d_numpy.kernel,
+                                f"jacobi_2d/{dt.__name__}/{shape[0]}x{shape[1]}/T{T}", T, A, B)
+        A = special_values(rng, (23, 29), dt)
+        B = special_values(rng, (23, 29), dt)
+        add_tsteps_case("jacobi_2d", jacobi_2d_numpy.kernel,
+                        f"jacobi_2d/{dt.__name__}/special/T4", 4, A, B, special=True)
+        # The reference's own initializer at preset S (N=150, TSTEPS=50).
+        A, B = jacobi_2d.initialize(150, dt)
+        add_tsteps_case("jacobi_2d", jacobi_2d_numpy.kernel,
+                        f"jacobi_2d/{dt.__name__}/presetS", 50, A, B, store=False,
+                        init="reference", N=150)
+
+    # Heat-3D.
+    for dt in (np.float64, np.float32):
+        for shape in [(2, 4, 4), (3, 3, 3), (4, 5, 6), (5, 3, 7), (9, 17, 33), (12, 12, 12)]:
+            for T in ((0, 1, 2, 3, 17) if np.prod(shape) < 200 else (2, 17)):
+                A = rng.random(shape).astype(dt)
+                B = A.copy()
+                add_tsteps_case("heat_3d", heat_3d_numpy.kernel,
+                                f"heat_3d/{dt.__name__}/{'x'.join(map(str, shape))}/T{T}", T, A, B)
+        A = special_values(rng, (7, 9, 11), dt)
+        B = special_values(rng, (7, 9, 11), dt)
+        add_tsteps_case("heat_3d", heat_3d_numpy.kernel,
+                        f"heat_3d/{dt.__name__}/special/T3", 3, A, B, special=True)
+        A, B = heat_3d.initialize(25, dt)
+        add_tsteps_case("heat_3d", heat_3d_numpy.kernel,
+                        f"heat_3d/{dt.__name__}/presetS", 25, A, B, store=False,
+                        init="reference", N=25)
+
+    # hdiff (float64 only).
+    for (I, J, K) in [(1, 1, 1), (1, 3, 2), (4, 5, 3), (13, 7, 1), (8, 8, 5), (16, 9, 17)]:
+        inf = rng.random((I + 4, J + 4, K))
+        coeff = rng.random((I, J, K))
+        out0 = rng.random((I, J, K))
+        out = out0.copy()
+        hdiff_numpy.hdiff(inf, out, coeff)
+        name = f"hdiff/float64/{I}x{J}x{K}"
+        arrays.update({f"{name}/in": inf, f"{name}/coeff": coeff, f"{name}/out_in": out0,
+                       f"{name}/out": out})
+        cases.append(dict(name=name, bench="hdiff", dtype="float64", shape=[I, J, K]))
+    inf = special_values(rng, (10, 11, 6), np.float64)
+    coeff = special_values(rng, (6, 7, 6), np.float64)
+    out = np.zeros((6, 7, 6))
+    with np.errstate(all="ignore"):
+        hdiff_numpy.hdiff(inf, out, coeff)
+    name = "hdiff/float64/special"
+    arrays.update({f"{name}/in": inf, f"{name}/coeff": coeff, f"{name}/out_in": np.zeros_like(out),
+                   f"{name}/out": out})
+    cases.append(dict(name=name, bench="hdiff", dtype="float64", shape=[6, 7, 6], special=True))
+    # Preset S with the reference initializer (default_rng(42)).
+    inf, out, coeff = hdiff.initialize(64, 64, 60)
+    o = out.copy()
+    hdiff_numpy.hdiff(inf, o, coeff)
+    cases.append(dict(name="hdiff/float64/presetS", bench="hdiff", dtype="float64",
+                      shape=[64, 64, 60], init="reference", sha_in=sha(inf), sha_coeff=sha(coeff),
+                      sha_out=sha(o)))
+
+    np.savez_compressed(os.path.join(HERE, "cases.npz"), **arrays)
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump({"numpy": np.__version__, "seed": 20211, "cases": cases}, f, indent=1)
+    print(f"{len(cases)} cases, {len(arrays)} arrays")
+
+
+if __name__ == "__main__":
+    with np.errstate(all="ignore"):
+        main()

@@ -1,0 +1,96 @@
+"""The C-ABI library loads, exports every declared symbol, and validates arguments on the host.
+
+No test here launches a kernel: argument errors and no-op sizes return before
+any CUDA call, so these run on machines without a GPU.
+"""
+import ctypes
+import os
+import re
+
+import pytest
+
+from npbench_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for fn in os.listdir(inc):
+        if fn.endswith(".h"):
+            with open(os.path.join(inc, fn)) as f:
+                names |= set(re.findall(r"NPBGB_API\s+[\w\s\*]+?\b(npbgb_\w+)\s*\(", f.read()))
+    return names
+
+
+def test_header_declares_the_bound_symbols():
+    declared = _declared_symbols()
+    assert declared, "no NPBGB_API declarations found"
+    assert declared == set(_lib.SIGNATURES), (declared ^ set(_lib.SIGNATURES))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(_lib.LIB_PATH)
+    for name in _declared_symbols():
+        assert hasattr(lib, name), name
+
+
+def test_version_and_status_strings():
+    lib = _lib.load()
+    assert lib.npbgb_version().decode().startswith("npbgb ")
+    assert "sm_103a" in lib.npbgb_version().decode()
+    assert lib.npbgb_status_string(_lib.NPBGB_OK) == b"ok"
+    assert lib.npbgb_status_string(_lib.NPBGB_ERR_TIMEOUT) == b"device wait timed out"
+    assert lib.npbgb_status_string(12345) == b"unknown status"
+
+
+def test_argument_errors_are_status_codes_not_crashes():
+    lib = _lib.load()
+    assert lib.npbgb_jacobi2d(None, None, -1, 4, 5, _lib.NPBGB_F64, None) == _lib.NPBGB_ERR_ARG
+    assert b"negative" in lib.npbgb_last_error()
+    assert lib.npbgb_heat3d(None, None, 4, -4, 4, 5, _lib.NPBGB_F32, None) == _lib.NPBGB_ERR_ARG
+    assert lib.npbgb_hdiff(None, None, None, 4, 4, 4, _lib.NPBGB_F32, None) == _lib.NPBGB_ERR_DTYPE
+    assert lib.npbgb_hdiff(None, None, None, 4, 4, 4, _lib.NPBGB_F64, None) == _lib.NPBGB_ERR_ARG
+    assert lib.npbgb_jacobi2d(None, None, 8, 8, 3, _lib.NPBGB_F64, None) == _lib.NPBGB_ERR_ARG
+    assert b"null" in lib.npbgb_last_error()
+    assert lib.npbgb_jacobi2d(ctypes.c_void_p(4096), ctypes.c_void_p(4096), 8, 8, 3,
+                              _lib.NPBGB_F64, None) == _lib.NPBGB_ERR_ARG
+    assert b"alias" in lib.npbgb_last_error()
+    assert lib.npbgb_heat3d(ctypes.c_void_p(4096), ctypes.c_void_p(8192), 8, 8, 8, 3, 7,
+                            None) == _lib.NPBGB_ERR_DTYPE
+
+
+def test_noop_sizes_return_ok_without_touching_memory():
+    lib = _lib.load()
+    # tsteps <= 1 and empty interiors are no-ops, exactly as the reference's loops are.
+    assert lib.npbgb_jacobi2d(None, None, 100, 100, 1, _lib.NPBGB_F64, None) == _lib.NPBGB_OK
+    assert lib.npbgb_jacobi2d(None, None, 2, 100, 50, _lib.NPBGB_F32, None) == _lib.NPBGB_OK
+    assert lib.npbgb_heat3d(None, None, 100, 2, 100, 50, _lib.NPBGB_F64, None) == _lib.NPBGB_OK
+    assert lib.npbgb_hdiff(None, None, None, 0, 5, 5, _lib.NPBGB_F64, None) == _lib.NPBGB_OK
+
+
+def test_python_errors_mirror_reference_behaviour():
+    import numpy as np
+    from npbench_gb300 import stencils
+    with pytest.raises(ValueError):
+        stencils.jacobi_2d_kernel(3, np.zeros((4, 4)), np.zeros((4, 5)))
+    with pytest.raises(TypeError):
+        stencils.jacobi_2d_kernel(3, np.zeros((4, 4), np.int64), np.zeros((4, 4), np.int64))
+    with pytest.raises(TypeError):
+        stencils.hdiff(np.zeros((8, 8, 2), np.float32), np.zeros((4, 4, 2), np.float32),
+                       np.zeros((4, 4, 2), np.float32))
+    with pytest.raises(ValueError):
+        stencils.hdiff(np.zeros((8, 9, 2)), np.zeros((4, 4, 2)), np.zeros((4, 4, 2)))
+    a = np.zeros((6, 6))
+    with pytest.raises(ValueError):
+        stencils.jacobi_2d_kernel(3, a, a)
+    with pytest.raises(ValueError):
+        stencils.heat_3d_kernel(3, np.zeros((4, 4)), np.zeros((4, 4)))
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "libnpbgb.so"))
+    monkeypatch.setattr(_lib, "_lib", None)
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        _lib.load()

@@ -1,0 +1,202 @@
+"""Parity of the CUDA stencils with the reference, on the GPU.
+
+* every stored golden case (reference NumPy outputs) -- bit for bit;
+* preset S with the reference initializers -- SHA-256 of the outputs;
+* seeded U[0,1) grids at the full benchmark sizes (Jacobi-2D 1000^2 x 100
+  steps, Heat-3D 256^3 x 100 steps in float64 and float32, hdiff
+  256x256x160) against the C oracle -- bit for bit;
+* host NumPy arrays through the same entry points (copy in, copy back).
+
+Bit-exact means identical bit patterns, except that any NaN matches any NaN.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import bits_equal, first_diff
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+from npbench_gb300 import stencils, workloads  # noqa: E402
+from oracle import cref  # noqa: E402
+
+DEV = torch.device("cuda", 0)
+
+
+def _dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(DEV)
+
+
+def _host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def _sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+KERNELS = {"jacobi_2d": stencils.jacobi_2d_kernel, "heat_3d": stencils.heat_3d_kernel}
+
+
+@pytest.mark.parametrize("bench", ["jacobi_2d", "heat_3d"])
+def test_golden_pingpong_bit_exact(golden, bench):
+    manifest, arrays = golden
+    n = 0
+    for c in manifest["cases"]:
+        if c["bench"] != bench or "init" in c:
+            continue
+        name = c["name"]
+        A, B = _dev(arrays[f"{name}/A_in"]), _dev(arrays[f"{name}/B_in"])
+        KERNELS[bench](c["tsteps"], A, B)
+        a, b = _host(A), _host(B)
+        assert bits_equal(a, arrays[f"{name}/A_out"]), (name, first_diff(a, arrays[f"{name}/A_out"]))
+        assert bits_equal(b, arrays[f"{name}/B_out"]), (name, first_diff(b, arrays[f"{name}/B_out"]))
+        n += 1
+    assert n >= 20
+
+
+def test_golden_hdiff_bit_exact(golden):
+    manifest, arrays = golden
+    n = 0
+    for c in manifest["cases"]:
+        if c["bench"] != "hdiff" or "init" in c:
+            continue
+        name = c["name"]
+        out = _dev(arrays[f"{name}/out_in"])
+        stencils.hdiff(_dev(arrays[f"{name}/in"]), out, _dev(arrays[f"{name}/coeff"]))
+        o = _host(out)
+        assert bits_equal(o, arrays[f"{name}/out"]), (name, first_diff(o, arrays[f"{name}/out"]))
+        n += 1
+    assert n >= 6
+
+
+def test_reference_initializer_presets(golden):
+    seen = 0
+    for c in golden[0]["cases"]:
+        if c.get("init") != "reference":
+            continue
+        if c["bench"] == "hdiff":
+            inf, out, coeff = workloads.init_hdiff(*c["shape"])
+            o = _dev(out)
+            stencils.hdiff(_dev(inf), o, _dev(coeff))
+            assert _sha(_host(o)) == c["sha_out"], c["name"]
+        else:
+            init = workloads.init_jacobi_2d if c["bench"] == "jacobi_2d" else workloads.init_heat_3d
+            A, B = init(c["N"], np.dtype(c["dtype"]).type)
+            dA, dB = _dev(A), _dev(B)
+            KERNELS[c["bench"]](c["tsteps"], dA, dB)
+            assert _sha(_host(dA)) == c["sha_A_out"], c["name"]
+            assert _sha(_host(dB)) == c["sha_B_out"], c["name"]
+        seen += 1
+    assert seen == 5
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_jacobi_full_size_vs_oracle(dtype):
+    A, B = workloads.uniform_pair((1000, 1000), dtype, seed=11)
+    dA, dB = _dev(A), _dev(B)
+    stencils.jacobi_2d_kernel(100, dA, dB)
+    cref.jacobi_2d_kernel(100, A, B)
+    assert bits_equal(_host(dA), A), first_diff(_host(dA), A)
+    assert bits_equal(_host(dB), B)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_heat_full_size_vs_oracle(dtype):
+    A, B = workloads.uniform_heat((256, 256, 256), dtype, seed=12)
+    dA, dB = _dev(A), _dev(B)
+    stencils.heat_3d_kernel(100, dA, dB)
+    cref.heat_3d_kernel(100, A, B)
+    assert bits_equal(_host(dA), A), first_diff(_host(dA), A)
+    assert bits_equal(_host(dB), B)
+
+
+def test_hdiff_full_size_vs_oracle():
+    inf, out, coeff = workloads.uniform_hdiff(256, 256, 160, seed=13)
+    d = _dev(out)
+    stencils.hdiff(_dev(inf), d, _dev(coeff))
+    cref.hdiff(inf, out, coeff)
+    assert bits_equal(_host(d), out), first_diff(_host(d), out)
+
+
+@pytest.mark.parametrize("shape", [(3, 3), (7, 300), (300, 7), (129, 257), (1000, 33)])
+def test_jacobi_ragged_shapes(shape):
+    for dtype in (np.float64, np.float32):
+        A, B = workloads.uniform_pair(shape, dtype, seed=shape[0])
+        dA, dB = _dev(A), _dev(B)
+        stencils.jacobi_2d_kernel(7, dA, dB)
+        cref.jacobi_2d_kernel(7, A, B)
+        assert bits_equal(_host(dA), A) and bits_equal(_host(dB), B), (shape, dtype)
+
+
+@pytest.mark.parametrize("shape", [(3, 3, 3), (3, 40, 70), (70, 3, 40), (33, 65, 3), (37, 45, 131)])
+def test_heat_ragged_shapes(shape):
+    for dtype in (np.float64, np.float32):
+        A, B = workloads.uniform_heat(shape, dtype, seed=sum(shape))
+        dA, dB = _dev(A), _dev(B)
+        stencils.heat_3d_kernel(5, dA, dB)
+        cref.heat_3d_kernel(5, A, B)
+        assert bits_equal(_host(dA), A) and bits_equal(_host(dB), B), (shape, dtype)
+
+
+@pytest.mark.parametrize("IJK", [(1, 1, 1), (3, 17, 2), (17, 3, 33), (9, 9, 64), (64, 64, 160),
+                                 (130, 70, 31)])
+def test_hdiff_ragged_shapes(IJK):
+    inf, out, coeff = workloads.uniform_hdiff(*IJK, seed=sum(IJK))
+    d = _dev(out)
+    stencils.hdiff(_dev(inf), d, _dev(coeff))
+    cref.hdiff(inf, out, coeff)
+    assert bits_equal(_host(d), out), (IJK, first_diff(_host(d), out))
+
+
+def test_host_numpy_arrays_are_updated_in_place(golden):
+    _, arrays = golden
+    name = "jacobi_2d/float64/33x47/T17"
+    a, b = arrays[f"{name}/A_in"].copy(), arrays[f"{name}/B_in"].copy()
+    a_id, b_id = id(a), id(b)
+    stencils.jacobi_2d_kernel(17, a, b)
+    assert id(a) == a_id and id(b) == b_id
+    assert bits_equal(a, arrays[f"{name}/A_out"]) and bits_equal(b, arrays[f"{name}/B_out"])
+    # non-contiguous host views are handled like NumPy does
+    big = np.zeros((12, 12, 12))
+    big[::2, ::2, ::2] = np.random.default_rng(1).random((6, 6, 6))
+    ref = big[::2, ::2, ::2].copy(), big[::2, ::2, ::2].copy()
+    va = big[::2, ::2, ::2]
+    vb = va.copy()
+    stencils.heat_3d_kernel(4, va, vb)
+    cref.heat_3d_kernel(4, *ref)
+    assert bits_equal(big[::2, ::2, ::2], ref[0]) and bits_equal(vb, ref[1])
+
+
+def test_noncontiguous_tensor_keeps_identity():
+    A, B = workloads.uniform_pair((40, 60), np.float64, seed=2)
+    big = torch.zeros((40, 120), dtype=torch.float64, device=DEV)
+    big[:, ::2] = _dev(A)
+    view = big[:, ::2]
+    dB = _dev(B)
+    stencils.jacobi_2d_kernel(6, view, dB)
+    cref.jacobi_2d_kernel(6, A, B)
+    assert bits_equal(_host(big[:, ::2]), A) and bits_equal(_host(dB), B)
+    assert bits_equal(_host(big[:, 1::2]), np.zeros((40, 60)))
+
+
+def test_cpu_tensor_is_rejected():
+    with pytest.raises(ValueError):
+        stencils.jacobi_2d_kernel(3, torch.zeros(5, 5, dtype=torch.float64),
+                                  torch.zeros(5, 5, dtype=torch.float64))
+
+
+def test_determinism_across_runs():
+    A, B = workloads.uniform_heat((96, 80, 72), np.float64, seed=5)
+    outs = []
+    for _ in range(2):
+        dA, dB = _dev(A), _dev(B)
+        stencils.heat_3d_kernel(9, dA, dB)
+        outs.append((_host(dA), _host(dB)))
+    assert bits_equal(outs[0][0], outs[1][0]) and bits_equal(outs[0][1], outs[1][1])

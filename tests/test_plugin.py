@@ -1,0 +1,98 @@
+"""The gb300 framework plugin inside NPBench's own harness.
+
+* CPU: the plugin installs into an NPBench tree, ``generate_framework("gb300")``
+  returns ``GB300Framework`` and every stencil benchmark resolves to the
+  npbench_gb300 kernels with the reference's argument strings plus a device
+  synchronisation (framework.py:140-162, cupy_framework.py:32-58).
+* GPU: the harness's ``Test.run`` executes each stencil benchmark at preset S
+  through the plugin, validates it against the harness's own NumPy run
+  (test.py:103-126) and reports SUCCESS.  It uses the NPBench tree that
+  ``__graft_entry__.build()`` installs into baseline/_ref/npbench, and is
+  skipped where that tree was never built.
+"""
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+STUBS = os.path.join(ROOT, "tests", "stubs")
+BUILT_TREE = os.path.join(ROOT, "baseline", "_ref", "npbench")
+
+
+def _npbench_source():
+    src = os.environ.get("NPBENCH_SRC", os.path.join(os.sep, "root", "reference"))
+    if not os.path.isdir(os.path.join(src, "npbench", "infrastructure")):
+        return None
+    return src
+
+
+def _run(tree, code, timeout=600):
+    env = dict(os.environ)
+    env["PYTHONPATH"] = os.pathsep.join([tree, ROOT, STUBS, env.get("PYTHONPATH", "")])
+    env["PYTHONDONTWRITEBYTECODE"] = "1"
+    return subprocess.run([sys.executable, "-c", code], cwd=tree, env=env, capture_output=True,
+                          text=True, timeout=timeout)
+
+
+def test_plugin_resolves_in_harness(tmp_path):
+    src = _npbench_source()
+    if src is None:
+        pytest.skip("no NPBench source tree available")
+    from npbench_gb300.plugin import install
+    tree = str(tmp_path / "npbench")
+    install.install(tree, copy_from=src)
+    code = r"""
+from npbench.infrastructure import Benchmark, generate_framework
+f = generate_framework("gb300")
+assert type(f).__name__ == "GB300Framework"
+assert f.version().startswith("npbgb ")
+for name, fn, mod in [("jacobi_2d", "kernel", "npbench.benchmarks.polybench.jacobi_2d.jacobi_2d_gb300"),
+                      ("heat_3d", "kernel", "npbench.benchmarks.polybench.heat_3d.heat_3d_gb300"),
+                      ("hdiff", "hdiff", "npbench.benchmarks.weather_stencils.hdiff.hdiff_gb300")]:
+    b = Benchmark(name)
+    impl, label = f.implementations(b)[0]
+    assert impl.__module__ == mod and impl.__name__ == fn and label == "default", impl
+    assert f.exec_str(b).endswith("; torch.cuda.synchronize()"), f.exec_str(b)
+    assert f.setup_str(b).endswith("; torch.cuda.synchronize()"), f.setup_str(b)
+    assert "__npb_gb_" in f.exec_str(b)
+print("OK")
+"""
+    r = _run(tree, code)
+    assert r.returncode == 0 and "OK" in r.stdout, r.stdout + r.stderr
+
+
+def test_install_is_idempotent(tmp_path):
+    src = _npbench_source()
+    if src is None:
+        pytest.skip("no NPBench source tree available")
+    from npbench_gb300.plugin import install
+    tree = str(tmp_path / "npbench")
+    install.install(tree, copy_from=src)
+    install.install(tree)
+    with open(os.path.join(tree, "npbench", "infrastructure", "__init__.py")) as f:
+        assert f.read().count("gb300_framework") == 1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bench", ["jacobi_2d", "heat_3d", "hdiff"])
+def test_harness_runs_and_validates_plugin(tmp_path, bench):
+    if not os.path.isdir(os.path.join(BUILT_TREE, "npbench", "infrastructure")):
+        pytest.skip("baseline/_ref/npbench was not built")
+    import shutil
+    tree = str(tmp_path / "npbench")
+    shutil.copytree(BUILT_TREE, tree)
+    code = f"""
+from npbench.infrastructure import Benchmark, generate_framework, Test
+bench = Benchmark("{bench}")
+frmwrk = generate_framework("gb300")
+numpy = generate_framework("numpy")
+Test(bench, frmwrk, numpy).run("S", True, 2, 300.0, False)
+print("HARNESS-DONE")
+"""
+    r = _run(tree, code)
+    out = r.stdout + r.stderr
+    assert r.returncode == 0 and "HARNESS-DONE" in r.stdout, out
+    assert "validation: SUCCESS" in r.stdout, out
+    assert "did not validate" not in out, out
