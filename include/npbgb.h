@@ -42,6 +42,18 @@ extern "C" {
 #define NPBGB_F64 0
 #define NPBGB_F32 1
 
+/* Configuration keys for npbgb_set_config / npbgb_get_config.  Settings are
+ * process-wide and read when an entry point launches its kernels. */
+#define NPBGB_CFG_F64_EMULATION 1 /* 1 (default): binary64 additions run exactly in
+                                     fixed point on the integer pipe where every
+                                     operand allows it, else hardware binary64;
+                                     0: hardware binary64 only.  Results are
+                                     identical either way. */
+#define NPBGB_CFG_HEAT_CHUNK 2    /* axis-0 planes per CTA in heat3d; 0 = automatic */
+#define NPBGB_CFG_HEAT_TMA 3      /* 1 (default): heat3d stages planes with TMA when the
+                                     arrays allow it; 0: plain loads only */
+#define NPBGB_CFG_JACOBI_CHUNK 4  /* rows per warp in jacobi2d; 0 = automatic */
+
 /* Library identification: "npbgb <version> sm_103a". */
 NPBGB_API const char* npbgb_version(void);
 
@@ -50,6 +62,25 @@ NPBGB_API const char* npbgb_last_error(void);
 
 /* Text for a status code. */
 NPBGB_API const char* npbgb_status_string(int32_t status);
+
+/* Sets / reads a configuration value (NPBGB_CFG_*).  NPBGB_ERR_ARG for an
+ * unknown key or an out-of-range value.  No counterpart in the reference,
+ * whose NumPy kernels have no tuning knobs. */
+NPBGB_API int32_t npbgb_set_config(int32_t key, int64_t value);
+NPBGB_API int32_t npbgb_get_config(int32_t key, int64_t* value);
+
+/* Synchronises `stream` (NULL: the whole device), then reads and clears the
+ * library's device error words.  NPBGB_ERR_TIMEOUT if a kernel gave up a
+ * bounded wait (for example on a TMA copy that never completed) since the
+ * last call.  Counterpart of the harness's per-run timeout,
+ * npbench/infrastructure/timeout_decorator.py:46-72, on the device side. */
+NPBGB_API int32_t npbgb_device_status(void* stream);
+
+/* Launches one CTA that waits on an mbarrier nothing completes, with a limit
+ * of limit_ns (1 .. 2e9).  The wait gives up and records the error that
+ * npbgb_device_status then reports: a check of the timeout path that needs
+ * no fault.  No counterpart in the reference. */
+NPBGB_API int32_t npbgb_selftest_wait_timeout(int64_t limit_ns, void* stream);
 
 /* 2D 5-point Jacobi, the whole time loop of
  *   kernel(TSTEPS, A, B)   polybench/jacobi_2d/jacobi_2d_numpy.py:4-10

@@ -19,6 +19,10 @@ NPBGB_ERR_NOMEM = 5
 NPBGB_ERR_STATE = 6
 NPBGB_F64 = 0
 NPBGB_F32 = 1
+NPBGB_CFG_F64_EMULATION = 1
+NPBGB_CFG_HEAT_CHUNK = 2
+NPBGB_CFG_HEAT_TMA = 3
+NPBGB_CFG_JACOBI_CHUNK = 4
 
 # Every symbol include/npbgb.h declares, with its ctypes signature.
 _i32, _i64, _vp, _cp = ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p, ctypes.c_char_p
@@ -26,6 +30,10 @@ SIGNATURES = {
     "npbgb_version": (_cp, []),
     "npbgb_last_error": (_cp, []),
     "npbgb_status_string": (_cp, [_i32]),
+    "npbgb_set_config": (_i32, [_i32, _i64]),
+    "npbgb_get_config": (_i32, [_i32, ctypes.POINTER(_i64)]),
+    "npbgb_device_status": (_i32, [_vp]),
+    "npbgb_selftest_wait_timeout": (_i32, [_i64, _vp]),
     "npbgb_jacobi2d": (_i32, [_vp, _vp, _i64, _i64, _i32, _i32, _vp]),
     "npbgb_heat3d": (_i32, [_vp, _vp, _i64, _i64, _i64, _i32, _i32, _vp]),
     "npbgb_hdiff": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i32, _vp]),
@@ -69,6 +77,24 @@ def check(status, where):
         if not msg:
             msg = lib.npbgb_status_string(status).decode()
         raise NpbgbError(status, where, msg)
+
+
+def set_config(key, value):
+    """Set a library knob (NPBGB_CFG_*); returns the previous value."""
+    old = get_config(key)
+    check(load().npbgb_set_config(key, int(value)), "npbgb_set_config")
+    return old
+
+
+def get_config(key):
+    v = _i64(0)
+    check(load().npbgb_get_config(key, ctypes.byref(v)), "npbgb_get_config")
+    return v.value
+
+
+def device_status(stream=None):
+    """Synchronise and raise NpbgbError if a kernel gave up a bounded device wait."""
+    check(load().npbgb_device_status(stream), "device_status")
 
 
 def version():

@@ -2,11 +2,22 @@
 #include <cstdarg>
 #include <cstdio>
 
+#include <mutex>
+
 #include "npbgb_common.cuh"
+#include "tma.cuh"
 
 namespace npbgb {
 
 static thread_local char g_last_error[512] = "";
+
+int64_t g_cfg_f64_emulation = 1;
+int64_t g_cfg_heat_chunk = 0;
+int64_t g_cfg_heat_tma = 1;
+int64_t g_cfg_jacobi_chunk = 0;
+
+uint32_t take_heat_device_error();
+int32_t launch_wait_timeout_selftest(uint64_t limit_ns, cudaStream_t st);
 
 int32_t set_error(int32_t code, const char* fmt, ...) {
   va_list ap;
@@ -15,6 +26,46 @@ int32_t set_error(int32_t code, const char* fmt, ...) {
   va_end(ap);
   return code;
 }
+
+namespace tma {
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+cudaError_t encode_3d(CUtensorMap* map, int esize, const void* base, const uint64_t dims[3],
+                      const uint32_t box[3]) {
+  if ((esize != 4 && esize != 8) || !base) return cudaErrorInvalidValue;
+  if (reinterpret_cast<uintptr_t>(base) % 16 != 0) return cudaErrorInvalidValue;
+  const uint64_t strides[2] = {dims[0] * esize, dims[0] * dims[1] * esize};
+  if (strides[0] % 16 != 0 || strides[1] % 16 != 0) return cudaErrorInvalidValue;
+  if ((box[0] * esize) % 16 != 0) return cudaErrorInvalidValue;
+  for (int d = 0; d < 3; ++d) {
+    if (box[d] == 0 || box[d] > 256) return cudaErrorInvalidValue;
+    if (dims[d] == 0 || dims[d] > (uint64_t(1) << 32)) return cudaErrorInvalidValue;
+  }
+  if (strides[1] >= (uint64_t(1) << 40)) return cudaErrorInvalidValue;
+  auto fn = encode_fn();
+  if (!fn) return cudaErrorNotSupported;
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = fn(map, esize == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                        3, const_cast<void*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+}  // namespace tma
 
 }  // namespace npbgb
 
@@ -35,6 +86,58 @@ const char* npbgb_status_string(int32_t status) {
     case NPBGB_ERR_STATE: return "invalid state";
     default: return "unknown status";
   }
+}
+
+int32_t npbgb_set_config(int32_t key, int64_t value) {
+  using namespace npbgb;
+  switch (key) {
+    case NPBGB_CFG_F64_EMULATION:
+      if (value != 0 && value != 1) return set_error(NPBGB_ERR_ARG, "f64 emulation: 0 or 1");
+      g_cfg_f64_emulation = value;
+      return NPBGB_OK;
+    case NPBGB_CFG_HEAT_CHUNK:
+      if (value < 0 || value > (1 << 20)) return set_error(NPBGB_ERR_ARG, "heat chunk out of range");
+      g_cfg_heat_chunk = value;
+      return NPBGB_OK;
+    case NPBGB_CFG_HEAT_TMA:
+      if (value != 0 && value != 1) return set_error(NPBGB_ERR_ARG, "heat tma: 0 or 1");
+      g_cfg_heat_tma = value;
+      return NPBGB_OK;
+    case NPBGB_CFG_JACOBI_CHUNK:
+      if (value < 0 || value > (1 << 20)) return set_error(NPBGB_ERR_ARG, "jacobi chunk out of range");
+      g_cfg_jacobi_chunk = value;
+      return NPBGB_OK;
+    default:
+      return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
+  }
+}
+
+int32_t npbgb_get_config(int32_t key, int64_t* value) {
+  using namespace npbgb;
+  if (!value) return set_error(NPBGB_ERR_ARG, "null output");
+  switch (key) {
+    case NPBGB_CFG_F64_EMULATION: *value = g_cfg_f64_emulation; return NPBGB_OK;
+    case NPBGB_CFG_HEAT_CHUNK: *value = g_cfg_heat_chunk; return NPBGB_OK;
+    case NPBGB_CFG_HEAT_TMA: *value = g_cfg_heat_tma; return NPBGB_OK;
+    case NPBGB_CFG_JACOBI_CHUNK: *value = g_cfg_jacobi_chunk; return NPBGB_OK;
+    default: return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
+  }
+}
+
+int32_t npbgb_device_status(void* stream) {
+  using namespace npbgb;
+  cudaError_t e = stream ? cudaStreamSynchronize(as_stream(stream)) : cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_status(e, "device status");
+  const uint32_t h = take_heat_device_error();
+  if (h == 0xffffffffu) return set_error(NPBGB_ERR_CUDA, "reading the device error word");
+  if (h) return set_error(NPBGB_ERR_TIMEOUT, "a bounded device wait gave up (heat3d)");
+  return NPBGB_OK;
+}
+
+int32_t npbgb_selftest_wait_timeout(int64_t limit_ns, void* stream) {
+  using namespace npbgb;
+  if (limit_ns <= 0 || limit_ns > 2000000000) return set_error(NPBGB_ERR_ARG, "limit out of range");
+  return launch_wait_timeout_selftest(uint64_t(limit_ns), as_stream(stream));
 }
 
 }  // extern "C"

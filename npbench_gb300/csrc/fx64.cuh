@@ -1,0 +1,140 @@
+// Exact binary64 addition on the integer pipe, in fixed point.
+//
+// GB300's binary64 pipe retires about 1.6 operations per SM per clock (about
+// 0.5 Tflop/s for the whole GPU), against 128 binary32 lanes, so a stencil
+// written with hardware binary64 adds is bound by that pipe, not by HBM.
+// These helpers reproduce IEEE round-to-nearest-even binary64 addition
+// exactly with 32-bit integer instructions for operands held in a fixed-point
+// frame:
+//
+//   a frame F represents the value v by the int64 X with v = X * 2^-F.
+//
+// A double x is representable in frame F when its unit in the last place is at
+// least 2^-F.  If x and y are representable in F and |X + Y| < 2^62, then
+//   fl(x + y) = round53(X + Y) * 2^-F
+// where round53 rounds the exact integer sum to 53 significant bits with ties
+// to even.  If |X + Y| < 2^53 the exact sum has at most 53 significant bits
+// and is a normal double (F is far below 1022), so IEEE returns it unchanged;
+// otherwise IEEE rounds at integer bit p - 52 (p the leading-bit position of
+// |X + Y|), which is exactly what round53 does.  Zero results are +0, as IEEE
+// gives for x + (-x) under round-to-nearest, so -0.0 inputs must be excluded
+// by the caller.
+//
+// Multiplying by a power of two is a change of frame (exact, no instruction):
+// 0.125 * v in frame F is the same integer read in frame F + 3.
+//
+// The header compiles for the device (nvcc) and for the host (any C++17
+// compiler), so the host build can be checked against the CPU's IEEE doubles.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+
+#if defined(__CUDACC__)
+#define NPBGB_FX_FN __host__ __device__ __forceinline__
+#else
+#define NPBGB_FX_FN inline
+#endif
+
+namespace npbgb {
+namespace fx {
+
+NPBGB_FX_FN int clz32(uint32_t v) {
+#if defined(__CUDA_ARCH__)
+  return __clz(static_cast<int>(v));
+#else
+  return v ? __builtin_clz(v) : 32;
+#endif
+}
+
+NPBGB_FX_FN int clz64(uint64_t v) {
+#if defined(__CUDA_ARCH__)
+  return __clzll(static_cast<long long>(v));
+#else
+  return v ? __builtin_clzll(v) : 64;
+#endif
+}
+
+NPBGB_FX_FN uint64_t bits_of(double x) {
+#if defined(__CUDA_ARCH__)
+  return static_cast<uint64_t>(__double_as_longlong(x));
+#else
+  uint64_t b;
+  std::memcpy(&b, &x, 8);
+  return b;
+#endif
+}
+
+NPBGB_FX_FN double double_of(uint64_t b) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double(static_cast<long long>(b));
+#else
+  double x;
+  std::memcpy(&x, &b, 8);
+  return x;
+#endif
+}
+
+// Rounds the exact integer x (|x| < 2^63 - 2^11) to 53 significant bits,
+// ties to even.  Works on two's complement directly: for negative x the
+// leading bit of ~x = |x| - 1 is that of |x| unless |x| is a power of two, and
+// then x has no bits below the rounding point anyway.
+NPBGB_FX_FN int64_t round53(int64_t x) {
+  const int32_t hi = static_cast<int32_t>(x >> 32);
+  const uint32_t h = static_cast<uint32_t>(hi ^ (hi >> 31));
+  int sh = (31 - clz32(h)) - 20;  // bits below the 53-bit window
+  sh = sh < 0 ? 0 : sh;           // 0..11, all within the low word
+  const uint32_t mask = (1u << sh) - 1u;
+  const uint32_t lo = static_cast<uint32_t>(x);
+  // floor((x + half - 1 + lsb) / 2^sh) * 2^sh is round-half-even on two's complement
+  const uint32_t add = ((mask >> 1) + ((lo >> sh) & 1u)) & mask;
+  return static_cast<int64_t>((static_cast<uint64_t>(x) + add) & ~static_cast<uint64_t>(mask));
+}
+
+// x -> frame-59 integer for x == +0.0 or x in [2^-7, 1).  Sets ok = false for
+// anything else (negative, -0.0, >= 1, < 2^-7, subnormal, inf, nan); the
+// returned value is then meaningless.
+NPBGB_FX_FN int64_t from_f64_f59(double x, bool& ok) {
+  const uint64_t b = bits_of(x);
+  const uint32_t hi = static_cast<uint32_t>(b >> 32);
+  const uint32_t lo = static_cast<uint32_t>(b);
+  const uint32_t sh = (hi >> 20) - 1016u;  // sign bit set -> huge -> rejected
+  const bool zero = b == 0;
+  ok = (sh <= 6u) || zero;
+  const uint32_t s = sh & 7u;
+  const uint32_t mh = (hi & 0xfffffu) | 0x100000u;
+  const uint32_t xh = s ? ((mh << s) | (lo >> (32u - s))) : mh;
+  const uint32_t xl = lo << s;
+  const int64_t X = static_cast<int64_t>((static_cast<uint64_t>(xh) << 32) | xl);
+  return zero ? 0 : X;
+}
+
+// Poison mark for values the fixed-point path refuses.  Accepted frame-59
+// values lie in [0, 2^59), so bit 30 of their high word is never set; OR-ing
+// the high words of a point's inputs and testing this bit finds any refused
+// input in one step.
+constexpr uint32_t kPoisonHi = 0x40000000u;
+
+NPBGB_FX_FN int64_t from_f64_f59_or_poison(double x) {
+  bool ok;
+  const int64_t v = from_f64_f59(x, ok);
+  return ok ? v : static_cast<int64_t>(static_cast<uint64_t>(kPoisonHi) << 32);
+}
+
+NPBGB_FX_FN uint32_t hi32(int64_t x) { return static_cast<uint32_t>(static_cast<uint64_t>(x) >> 32); }
+
+// Frame-F integer (already rounded to 53 significant bits, |w| < 2^63) -> double.
+template <int F>
+NPBGB_FX_FN double to_f64(int64_t w) {
+  const uint64_t sign = static_cast<uint64_t>(w) & 0x8000000000000000ull;
+  const uint64_t m = w < 0 ? static_cast<uint64_t>(0) - static_cast<uint64_t>(w)
+                           : static_cast<uint64_t>(w);
+  const int lz = clz64(m);
+  const uint64_t norm = m << (lz & 63);
+  // exponent field = 1086 - F - lz; the implicit bit of norm >> 11 adds one.
+  const uint64_t bits = (norm >> 11) + (static_cast<uint64_t>(1085 - F - lz) << 52);
+  return m == 0 ? 0.0 : double_of(bits | sign);
+}
+
+}  // namespace fx
+}  // namespace npbgb

@@ -1,76 +1,356 @@
 // 3D 7-point heat time loop (polybench/heat_3d/heat_3d_numpy.py:4-20).
 //
-// One launch per half-sweep.  Threads cover the (axis-1, axis-2) interior
-// plane, axis 2 contiguous across the warp, and stream along axis 0 with a
-// register queue (prev, centre, next).  Per point:
-//   tx  = 0.125 * ((next_x - 2*c) + prev_x)      for x = 0, 1, 2
+// Per interior point, in the reference's order:
+//   tx  = 0.125 * ((next_x - 2*c) + prev_x)      x = axis 0, 1, 2
 //   dst = ((t0 + t1) + t2) + c
-// 2*c is exact and identical for the three axes, so it is formed once.
+//
+// One launch per half-sweep.  A CTA owns a TJ x 32 tile of the
+// (axis 1, axis 2) plane -- axis 2 contiguous, one element per lane -- and
+// streams along axis 0 over a chunk of planes.
+//
+// heat3d_tma (used when the arrays meet the TMA alignment rules): each
+//   halo'd plane tile arrives by one cp.async.bulk.tensor copy into an
+//   NSTAGE-deep ring of shared-memory buffers, completion tracked by one
+//   mbarrier per buffer, so several planes per CTA are in flight while the
+//   current one is computed.  Planes i-1, i, i+1 are read from shared memory.
+// heat3d_ldg (any layout): each plane tile is staged by plain loads into
+//   three rotating shared buffers; axis-0 neighbours stay in registers.
+//
+// binary32 uses IEEE float operations.  binary64 runs in fixed point on the
+// integer pipe (fx64.cuh): staged values are converted once to frame-59
+// integers, values outside [2^-7, 1) (other than +0) are marked with a poison
+// bit, and a point whose seven inputs are all clean is evaluated with exact
+// integer adds and round53; any other point is evaluated with hardware
+// binary64 from global memory.  Both give the IEEE result bit for bit.
+#include <type_traits>
+
+#include "fx64.cuh"
 #include "npbgb_common.cuh"
+#include "tma.cuh"
 
 namespace npbgb {
+
+extern int64_t g_cfg_f64_emulation;
+extern int64_t g_cfg_heat_chunk;
+extern int64_t g_cfg_heat_tma;
+
 namespace {
 
-constexpr int kBX = 32, kBY = 8, kChunk0 = 32;
+__device__ unsigned int g_heat_error;  // bit 0: an mbarrier wait timed out
+
+constexpr int kTK = 32;   // tile extent along axis 2 (one warp)
+constexpr int kTJ = 8;    // tile extent along axis 1 (warps per CTA)
+constexpr int kThreads = kTK * kTJ;
+using fx::hi32;
+using fx::kPoisonHi;
 
 template <typename T>
-__global__ void __launch_bounds__(kBX * kBY)
-heat3d_half(const T* __restrict__ src, T* __restrict__ dst, int64_t n0, int64_t n1, int64_t n2) {
+__device__ __forceinline__ T heat_point(T c, T ip, T im, T jp, T jm, T kp, T km) {
   const T two = T(2.0), eighth = T(0.125);
-  const int64_t k = 1 + int64_t(blockIdx.x) * kBX + threadIdx.x;
-  const int64_t j = 1 + int64_t(blockIdx.y) * kBY + threadIdx.y;
-  if (k >= n2 - 1 || j >= n1 - 1) return;
-  const int64_t s0 = n1 * n2, s1 = n2;
-  const int64_t i_begin = 1 + int64_t(blockIdx.z) * kChunk0;
-  const int64_t i_end = (i_begin + kChunk0 < n0 - 1) ? i_begin + kChunk0 : n0 - 1;
-  const T* p = src + j * s1 + k;
-  T prev = p[(i_begin - 1) * s0];
-  T cur = p[i_begin * s0];
-  for (int64_t i = i_begin; i < i_end; ++i) {
-    const T* q = p + i * s0;
-    const T next = q[s0];
-    const T c2 = mul_rn(two, cur);
-    const T t0 = mul_rn(eighth, add_rn(sub_rn(next, c2), prev));
-    const T t1 = mul_rn(eighth, add_rn(sub_rn(q[s1], c2), q[-s1]));
-    const T t2 = mul_rn(eighth, add_rn(sub_rn(q[1], c2), q[-1]));
-    dst[i * s0 + j * s1 + k] = add_rn(add_rn(add_rn(t0, t1), t2), cur);
-    prev = cur;
-    cur = next;
+  const T c2 = mul_rn(two, c);
+  const T t0 = mul_rn(eighth, add_rn(sub_rn(ip, c2), im));
+  const T t1 = mul_rn(eighth, add_rn(sub_rn(jp, c2), jm));
+  const T t2 = mul_rn(eighth, add_rn(sub_rn(kp, c2), km));
+  return add_rn(add_rn(add_rn(t0, t1), t2), c);
+}
+
+// Fixed-point form of heat_point; inputs in frame 59, result as a double.
+__device__ __forceinline__ double heat_point_fx(int64_t c, int64_t ip, int64_t im, int64_t jp,
+                                                int64_t jm, int64_t kp, int64_t km) {
+  using fx::round53;
+  const int64_t c2 = c * 2;
+  const int64_t s0 = round53(round53(ip - c2) + im);  // 8 * t0 in frame 59 == t0 in frame 62
+  const int64_t s1 = round53(round53(jp - c2) + jm);
+  const int64_t s2 = round53(round53(kp - c2) + km);
+  const int64_t w = round53(round53(round53(s0 + s1) + s2) + c * 8);
+  return fx::to_f64<62>(w);
+}
+
+__device__ __forceinline__ int64_t to_fx(double v) { return fx::from_f64_f59_or_poison(v); }
+
+// Evaluates one point from staged values (T for the plain path, frame-59
+// integers with poison marks for binary64), falling back to hardware binary64
+// from global memory `q` (pointer to the centre) when an input is poisoned.
+template <typename T, bool FX, typename S>
+__device__ __forceinline__ T eval_point(S c, S ip, S im, S jp, S jm, S kp, S km, const T* q,
+                                        int64_t s0, int64_t s1) {
+  if constexpr (FX) {
+    const uint32_t tag = hi32(c) | hi32(ip) | hi32(im) | hi32(jp) | hi32(jm) | hi32(kp) | hi32(km);
+    if (!(tag & kPoisonHi)) return heat_point_fx(c, ip, im, jp, jm, kp, km);
+    return heat_point<T>(q[0], q[s0], q[-s0], q[s1], q[-s1], q[1], q[-1]);
+  } else {
+    return heat_point<T>(c, ip, im, jp, jm, kp, km);
   }
 }
 
+// ---------------------------------------------------------------------------
+// TMA pipeline
+// ---------------------------------------------------------------------------
 template <typename T>
+struct TmaGeom {
+  static constexpr int BX = sizeof(T) == 8 ? 34 : 36;  // rows of a 16-byte multiple
+  static constexpr int BY = kTJ + 2;
+  static constexpr int kElems = BX * BY;
+  static constexpr int kBytes = kElems * int(sizeof(T));
+  static constexpr int kStride = (kBytes + 127) / 128 * 128;  // stage pitch, 128-byte aligned
+};
+
+constexpr int kStages = 8;
+
+template <typename T, bool FX>
+__global__ void __launch_bounds__(kThreads)
+heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ src,
+           T* __restrict__ dst, int64_t n0, int64_t n1, int64_t n2, int chunk) {
+  using G = TmaGeom<T>;
+  using S = typename std::conditional<FX, int64_t, T>::type;
+  static_assert(sizeof(S) == sizeof(T) || FX, "in-place conversion keeps the element size");
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kStages * G::kStride);
+
+  const int tid = threadIdx.x;
+  const int tx = tid & 31, ty = tid >> 5;
+  const int64_t k0 = 1 + int64_t(blockIdx.x) * kTK, j0 = 1 + int64_t(blockIdx.y) * kTJ;
+  const int64_t k = k0 + tx, j = j0 + ty;
+  const bool active = k < n2 - 1 && j < n1 - 1;
+  const int64_t s0 = n1 * n2, s1 = n2;
+  const int64_t ib = 1 + int64_t(blockIdx.z) * chunk;
+  const int64_t ie = (ib + chunk < n0 - 1) ? ib + chunk : n0 - 1;
+  const int M = int(ie - ib);     // output planes
+  const int Q = M + 2;            // staged planes ib-1 .. ie
+  // Tile origin: x = k0 - 1 = 32 * blockIdx.x, a multiple of 4 elements (16 bytes).
+  const int x0 = int(k0 - 1), y0 = int(j0 - 1);
+
+  auto stage_ptr = [&](int q) -> S* {
+    return reinterpret_cast<S*>(smem + (q % kStages) * G::kStride);
+  };
+  auto issue = [&](int q) {
+    uint64_t* bar = &bars[q % kStages];
+    tma::mbar_arrive_expect_tx(bar, G::kBytes);
+    tma::load_3d(smem + (q % kStages) * G::kStride, &src_map, x0, y0, int(ib - 1 + q), bar);
+  };
+  auto wait = [&](int q) -> bool {
+    return tma::mbar_wait(&bars[q % kStages], uint32_t((q / kStages) & 1));
+  };
+  auto convert = [&](int q) {
+    if constexpr (FX) {
+      unsigned char* base = smem + (q % kStages) * G::kStride;
+      for (int e = tid; e < G::kElems; e += kThreads) {
+        const double v = reinterpret_cast<const double*>(base)[e];
+        reinterpret_cast<int64_t*>(base)[e] = to_fx(v);
+      }
+    }
+  };
+
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) tma::mbar_init(&bars[s], 1);
+    tma::fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const int n_first = Q < kStages - 1 ? Q : kStages - 1;
+    for (int q = 0; q < n_first; ++q) issue(q);
+  }
+  bool ok = wait(0);
+  if (ok) convert(0);
+  ok = ok && wait(1);
+  if (ok) convert(1);
+
+  const int off = (ty + 1) * G::BX + (tx + 1);
+  for (int m = 0; m < M; ++m) {
+    ok = ok && wait(m + 2);
+    if (ok) convert(m + 2);
+    tma::fence_proxy_async();  // order this thread's generic smem accesses before later bulk writes
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicOr(&g_heat_error, 1u);
+      return;
+    }
+    if (tid == 0 && m - 1 + kStages < Q) issue(m - 1 + kStages);  // refills the buffer of plane m-1
+    if (active) {
+      const S* pm = stage_ptr(m) + off;
+      const S* pc = stage_ptr(m + 1) + off;
+      const S* pp = stage_ptr(m + 2) + off;
+      const int64_t i = ib + m;
+      const T* q = src + i * s0 + j * s1 + k;
+      dst[i * s0 + j * s1 + k] = eval_point<T, FX>(pc[0], pp[0], pm[0], pc[G::BX], pc[-G::BX],
+                                                   pc[1], pc[-1], q, s0, s1);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Plain-load pipeline (any alignment)
+// ---------------------------------------------------------------------------
+template <typename T, bool FX>
+__global__ void __launch_bounds__(kThreads)
+heat3d_ldg(const T* __restrict__ src, T* __restrict__ dst, int64_t n0, int64_t n1, int64_t n2,
+           int chunk) {
+  using S = typename std::conditional<FX, int64_t, T>::type;
+  __shared__ S plane[3][kTJ + 2][kTK + 2];
+
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int64_t k0 = 1 + int64_t(blockIdx.x) * kTK, j0 = 1 + int64_t(blockIdx.y) * kTJ;
+  const int64_t k = k0 + tx, j = j0 + ty;
+  const bool active = k < n2 - 1 && j < n1 - 1;
+  const bool own_inb = k < n2 && j < n1;
+  const int64_t s0 = n1 * n2, s1 = n2;
+  const int64_t ib = 1 + int64_t(blockIdx.z) * chunk;
+  const int64_t ie = (ib + chunk < n0 - 1) ? ib + chunk : n0 - 1;
+
+  // Halo roles: warp 0 the row before the tile, warp 1 the row after, warps
+  // 2 and 3 (first kTJ lanes) the columns before and after.  No corners: the
+  // stencil has no diagonal neighbours.
+  int er = -1, ec = -1;
+  int64_t ej = 0, ek = 0;
+  if (ty == 0) { ej = j0 - 1; ek = k; er = 0; ec = tx + 1; }
+  else if (ty == 1) { ej = j0 + kTJ; ek = k; er = kTJ + 1; ec = tx + 1; }
+  else if (ty == 2 && tx < kTJ) { ej = j0 + tx; ek = k0 - 1; er = tx + 1; ec = 0; }
+  else if (ty == 3 && tx < kTJ) { ej = j0 + tx; ek = k0 + kTK; er = tx + 1; ec = kTK + 1; }
+  const bool has_extra = er >= 0 && ej < n1 && ek < n2;
+  const T* own_p = src + j * s1 + k;
+  const T* extra_p = src + ej * s1 + ek;
+
+  auto stage = [&](int64_t i, int b, S& own) {
+    if (own_inb) {
+      const T v = own_p[i * s0];
+      if constexpr (FX) own = to_fx(v); else own = v;
+      plane[b][ty + 1][tx + 1] = own;
+    }
+    if (has_extra) {
+      const T v = extra_p[i * s0];
+      if constexpr (FX) plane[b][er][ec] = to_fx(v); else plane[b][er][ec] = v;
+    }
+  };
+
+  S xp = S(0), xc = S(0), xn = S(0);
+  int bc = 1, bn = 2;
+  stage(ib - 1, 0, xp);
+  stage(ib, bc, xc);
+  for (int64_t i = ib; i < ie; ++i) {
+    stage(i + 1, bn, xn);
+    __syncthreads();
+    if (active) {
+      const S* P = &plane[bc][ty + 1][tx + 1];
+      dst[i * s0 + j * s1 + k] = eval_point<T, FX>(xc, xn, xp, P[kTK + 2], P[-(kTK + 2)], P[1],
+                                                   P[-1], own_p + i * s0, s0, s1);
+    }
+    const int t = (bn + 1) % 3;  // buffer of plane i-1, free after this barrier round
+    bc = bn;
+    bn = t;
+    xp = xc;
+    xc = xn;
+  }
+}
+
+struct Plan {
+  bool tma = false;
+  int chunk = 0;
+  dim3 grid, block;
+  size_t smem = 0;
+};
+
+int auto_chunk(int64_t n0, int64_t tiles, int ctas_per_sm) {
+  // Smallest number of axis-0 chunks that fills about two waves of CTAs.
+  const int64_t slots = int64_t(sm_count()) * (ctas_per_sm > 0 ? ctas_per_sm : 1);
+  int64_t chunks = cdiv(2 * slots, tiles > 0 ? tiles : 1);
+  if (chunks < 1) chunks = 1;
+  int64_t c = cdiv(n0 - 2, chunks);
+  if (c < 4) c = 4;
+  if (c > n0 - 2) c = n0 - 2;
+  return int(c);
+}
+
+template <typename T, bool FX>
 int32_t run(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps, cudaStream_t st) {
   if (tsteps <= 1 || n0 < 3 || n1 < 3 || n2 < 3) return NPBGB_OK;
-  dim3 block(kBX, kBY);
-  dim3 grid(unsigned(cdiv(n2 - 2, kBX)), unsigned(cdiv(n1 - 2, kBY)),
-            unsigned(cdiv(n0 - 2, kChunk0)));
-  for (int32_t t = 1; t < tsteps; ++t) {
-    heat3d_half<T><<<grid, block, 0, st>>>(a, b, n0, n1, n2);
-    heat3d_half<T><<<grid, block, 0, st>>>(b, a, n0, n1, n2);
+  const int64_t gx = cdiv(n2 - 2, kTK), gy = cdiv(n1 - 2, kTJ);
+  using G = TmaGeom<T>;
+  const size_t smem = size_t(kStages) * G::kStride + kStages * sizeof(uint64_t);
+  CUtensorMap map_a, map_b;
+  bool use_tma = g_cfg_heat_tma != 0;
+  if (use_tma) {
+    const uint64_t dims[3] = {uint64_t(n2), uint64_t(n1), uint64_t(n0)};
+    const uint32_t box[3] = {uint32_t(G::BX), uint32_t(G::BY), 1u};
+    use_tma = tma::encode_3d(&map_a, sizeof(T), a, dims, box) == cudaSuccess &&
+              tma::encode_3d(&map_b, sizeof(T), b, dims, box) == cudaSuccess;
   }
-  NPBGB_CHECK_LAUNCH("heat3d_half");
+  int per_sm = 0;
+  if (use_tma) {
+    static bool attr_done[2][2] = {};
+    if (!attr_done[sizeof(T) == 8][FX]) {
+      cudaError_t e = cudaFuncSetAttribute(heat3d_tma<T, FX>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+      if (e != cudaSuccess) return cuda_status(e, "heat3d: smem attribute");
+      attr_done[sizeof(T) == 8][FX] = true;
+    }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heat3d_tma<T, FX>, kThreads, smem);
+  } else {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heat3d_ldg<T, FX>, kThreads, 0);
+  }
+  const int chunk = g_cfg_heat_chunk > 0 ? int(g_cfg_heat_chunk) : auto_chunk(n0, gx * gy, per_sm);
+  const int64_t gz = cdiv(n0 - 2, chunk);
+  if (gy > 65535 || gz > 65535 || gx > 0x7fffffff)
+    return set_error(NPBGB_ERR_ARG, "heat3d: extent too large");
+  const dim3 grid{unsigned(gx), unsigned(gy), unsigned(gz)};
+  for (int32_t t = 1; t < tsteps; ++t) {
+    if (use_tma) {
+      heat3d_tma<T, FX><<<grid, kThreads, smem, st>>>(map_a, a, b, n0, n1, n2, chunk);
+      heat3d_tma<T, FX><<<grid, kThreads, smem, st>>>(map_b, b, a, n0, n1, n2, chunk);
+    } else {
+      heat3d_ldg<T, FX><<<grid, kThreads, 0, st>>>(a, b, n0, n1, n2, chunk);
+      heat3d_ldg<T, FX><<<grid, kThreads, 0, st>>>(b, a, n0, n1, n2, chunk);
+    }
+  }
+  NPBGB_CHECK_LAUNCH("heat3d");
   return NPBGB_OK;
 }
 
+// One CTA waits, with a short limit, on an mbarrier that nothing completes;
+// the timeout path records the error word exactly as a lost copy would.
+__global__ void wait_timeout_selftest(uint64_t limit_ns) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    tma::mbar_init(&bar, 1);
+    tma::fence_mbar_init();
+  }
+  __syncthreads();
+  const bool ok = tma::mbar_wait_for(&bar, 0, limit_ns);
+  if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicOr(&g_heat_error, 1u);
+}
+
 }  // namespace
+
+int32_t launch_wait_timeout_selftest(uint64_t limit_ns, cudaStream_t st) {
+  wait_timeout_selftest<<<1, 64, 0, st>>>(limit_ns);
+  NPBGB_CHECK_LAUNCH("wait_timeout_selftest");
+  return NPBGB_OK;
+}
+
+// Reads and clears this file's device error word (host; synchronises with the device).
+uint32_t take_heat_device_error() {
+  unsigned int v = 0, zero = 0;
+  if (cudaMemcpyFromSymbol(&v, g_heat_error, sizeof(v)) != cudaSuccess) return 0xffffffffu;
+  if (v) cudaMemcpyToSymbol(g_heat_error, &zero, sizeof(zero));
+  return v;
+}
+
 }  // namespace npbgb
 
 extern "C" int32_t npbgb_heat3d(void* A, void* B, int64_t n0, int64_t n1, int64_t n2,
                                 int32_t tsteps, int32_t dtype, void* stream) {
   using namespace npbgb;
   if (n0 < 0 || n1 < 0 || n2 < 0) return set_error(NPBGB_ERR_ARG, "heat3d: negative extent");
-  if (cdiv(n2, kBX) > 0x7fffffff || cdiv(n1, kBY) > 65535 || cdiv(n0, kChunk0) > 65535)
-    return set_error(NPBGB_ERR_ARG, "heat3d: extent too large");
   if (tsteps > 1 && n0 >= 3 && n1 >= 3 && n2 >= 3) {
     if (!A || !B) return set_error(NPBGB_ERR_ARG, "heat3d: null array");
     if (A == B) return set_error(NPBGB_ERR_ARG, "heat3d: A and B alias");
   }
-  if (dtype == NPBGB_F64)
-    return run<double>(static_cast<double*>(A), static_cast<double*>(B), n0, n1, n2, tsteps,
-                       as_stream(stream));
+  cudaStream_t st = as_stream(stream);
+  if (dtype == NPBGB_F64) {
+    double* a = static_cast<double*>(A);
+    double* b = static_cast<double*>(B);
+    return g_cfg_f64_emulation ? run<double, true>(a, b, n0, n1, n2, tsteps, st)
+                               : run<double, false>(a, b, n0, n1, n2, tsteps, st);
+  }
   if (dtype == NPBGB_F32)
-    return run<float>(static_cast<float*>(A), static_cast<float*>(B), n0, n1, n2, tsteps,
-                      as_stream(stream));
+    return run<float, false>(static_cast<float*>(A), static_cast<float*>(B), n0, n1, n2, tsteps, st);
   return set_error(NPBGB_ERR_DTYPE, "heat3d: dtype %d", dtype);
 }

@@ -1,43 +1,135 @@
 // 2D 5-point Jacobi time loop (polybench/jacobi_2d/jacobi_2d_numpy.py:4-10).
 //
-// One launch per half-sweep.  Each thread owns one interior point and
-// evaluates dst = 0.2 * ((((c + w) + e) + s) + n) with separately rounded IEEE
-// operations, the reference's operator order.
+// Per interior point, in the reference's order:
+//   dst = 0.2 * ((((c + w) + e) + s) + n)
+// with w/e the column neighbours j-1/j+1 and s/n the row neighbours i+1/i-1.
+//
+// Kernel layout (one launch per half-sweep): every warp owns a strip of 32
+// columns (one per lane, the contiguous axis) and streams down a chunk of
+// rows, keeping rows i-1, i, i+1 of its own column in registers and taking
+// the w/e neighbours from the adjacent lanes with shuffles (lanes 0 and 31
+// also load the strip's halo columns).  Warps never wait on each other.
+//
+// binary32 uses IEEE float operations.  binary64 runs its four additions
+// exactly in fixed point on the integer pipe (fx64.cuh) for every point whose
+// five inputs lie in [2^-7, 1) or are +0 (refused values carry a poison bit),
+// and uses hardware binary64 for any other point; the final product by 0.2 is
+// a hardware binary64 multiply.  Both paths give the IEEE result bit for bit.
+#include <type_traits>
+
+#include "fx64.cuh"
 #include "npbgb_common.cuh"
 
 namespace npbgb {
+
+extern int64_t g_cfg_f64_emulation;
+extern int64_t g_cfg_jacobi_chunk;
+
 namespace {
 
-constexpr int kBX = 32, kBY = 8;
+constexpr int kWarps = 8;
 
-template <typename T>
-__global__ void __launch_bounds__(kBX * kBY)
-jacobi2d_half(const T* __restrict__ src, T* __restrict__ dst, int64_t ny, int64_t nx) {
+template <typename S>
+__device__ __forceinline__ S shfl_up1(S v) { return __shfl_up_sync(0xffffffffu, v, 1); }
+template <typename S>
+__device__ __forceinline__ S shfl_down1(S v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+
+template <typename T, bool FX>
+__global__ void __launch_bounds__(32 * kWarps)
+jacobi2d_strip(const T* __restrict__ src, T* __restrict__ dst, int64_t ny, int64_t nx, int chunk) {
+  using S = typename std::conditional<FX, int64_t, T>::type;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t k0 = 1 + (int64_t(blockIdx.x) * kWarps + warp) * 32;
+  if (k0 >= nx - 1) return;  // whole strip outside the interior (warp-uniform)
+  const int64_t j = k0 + lane;
+  const bool active_col = j < nx - 1;
+  const bool own_inb = j < nx;
+  const int64_t ib = 1 + int64_t(blockIdx.y) * chunk;
+  const int64_t ie = (ib + chunk < ny - 1) ? ib + chunk : ny - 1;
+  // Halo column: lane 0 reads k0-1, lane 31 reads k0+32 (when inside the array).
+  const int64_t hj = lane == 0 ? k0 - 1 : k0 + 32;
+  const bool has_halo = (lane == 0) || (lane == 31 && hj < nx);
+
+  auto load = [&](int64_t i, S& own, S& halo) {
+    const T* row = src + i * nx;
+    if (own_inb) {
+      const T v = row[j];
+      if constexpr (FX) own = fx::from_f64_f59_or_poison(v); else own = v;
+    }
+    if (has_halo) {
+      const T v = row[hj];
+      if constexpr (FX) halo = fx::from_f64_f59_or_poison(v); else halo = v;
+    }
+  };
+
+  S xp = S(0), xc = S(0), xn = S(0), hc = S(0), hn = S(0), hdummy = S(0);
+  load(ib - 1, xp, hdummy);
+  load(ib, xc, hc);
   const T k02 = T(0.2);
-  const int64_t j = 1 + int64_t(blockIdx.x) * kBX + threadIdx.x;
-  if (j >= nx - 1) return;
-  for (int64_t i = 1 + int64_t(blockIdx.y) * kBY + threadIdx.y; i < ny - 1;
-       i += int64_t(gridDim.y) * kBY) {
-    const T* r = src + i * nx + j;
-    T acc = add_rn(r[0], r[-1]);
-    acc = add_rn(acc, r[1]);
-    acc = add_rn(acc, r[nx]);
-    acc = add_rn(acc, r[-nx]);
-    dst[i * nx + j] = mul_rn(k02, acc);
+  for (int64_t i = ib; i < ie; ++i) {
+    load(i + 1, xn, hn);
+    // w/e of row i from the neighbouring lanes; the strip ends use the halo.
+    S w = shfl_up1(xc), e = shfl_down1(xc);
+    if (lane == 0) w = hc;
+    if (lane == 31) e = hc;
+    T out;
+    if constexpr (FX) {
+      using fx::hi32;
+      const uint32_t tag = hi32(xc) | hi32(w) | hi32(e) | hi32(xn) | hi32(xp);
+      if (!(tag & fx::kPoisonHi)) {
+        using fx::round53;
+        int64_t acc = round53(xc + w);
+        acc = round53(acc + e);
+        acc = round53(acc + xn);
+        acc = round53(acc + xp);
+        out = mul_rn(k02, fx::to_f64<59>(acc));
+      } else {
+        out = T(0);
+        if (active_col) {
+          const T* r = src + i * nx + j;
+          T acc = add_rn(r[0], r[-1]);
+          acc = add_rn(acc, r[1]);
+          acc = add_rn(acc, r[nx]);
+          acc = add_rn(acc, r[-nx]);
+          out = mul_rn(k02, acc);
+        }
+      }
+    } else {
+      T acc = add_rn(xc, w);
+      acc = add_rn(acc, e);
+      acc = add_rn(acc, xn);
+      acc = add_rn(acc, xp);
+      out = mul_rn(k02, acc);
+    }
+    if (active_col) dst[i * nx + j] = out;
+    xp = xc; xc = xn; hc = hn;
   }
 }
 
-template <typename T>
+int pick_chunk(int64_t ny, int64_t col_blocks) {
+  if (g_cfg_jacobi_chunk > 0) return int(g_cfg_jacobi_chunk);
+  // About 16 warps per SM over 152 SMs, rows per warp at least 8.
+  const int64_t target_blocks = int64_t(sm_count()) * 16 / kWarps * 4;
+  int64_t chunks = cdiv(target_blocks, col_blocks > 0 ? col_blocks : 1);
+  int64_t c = cdiv(ny - 2, chunks > 0 ? chunks : 1);
+  if (c < 8) c = 8;
+  if (c > ny - 2) c = ny - 2;
+  return int(c);
+}
+
+template <typename T, bool FX>
 int32_t run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st) {
   if (tsteps <= 1 || ny < 3 || nx < 3) return NPBGB_OK;
-  dim3 block(kBX, kBY);
-  int64_t gy = cdiv(ny - 2, kBY);
-  dim3 grid(unsigned(cdiv(nx - 2, kBX)), unsigned(gy > 65535 ? 65535 : gy));
+  const int64_t gx = cdiv(nx - 2, 32 * kWarps);
+  const int chunk = pick_chunk(ny, gx);
+  const int64_t gy = cdiv(ny - 2, chunk);
+  if (gx > 0x7fffffff || gy > 65535) return set_error(NPBGB_ERR_ARG, "jacobi2d: extent too large");
+  const dim3 grid{unsigned(gx), unsigned(gy)};
   for (int32_t t = 1; t < tsteps; ++t) {
-    jacobi2d_half<T><<<grid, block, 0, st>>>(a, b, ny, nx);
-    jacobi2d_half<T><<<grid, block, 0, st>>>(b, a, ny, nx);
+    jacobi2d_strip<T, FX><<<grid, 32 * kWarps, 0, st>>>(a, b, ny, nx, chunk);
+    jacobi2d_strip<T, FX><<<grid, 32 * kWarps, 0, st>>>(b, a, ny, nx, chunk);
   }
-  NPBGB_CHECK_LAUNCH("jacobi2d_half");
+  NPBGB_CHECK_LAUNCH("jacobi2d_strip");
   return NPBGB_OK;
 }
 
@@ -48,16 +140,18 @@ extern "C" int32_t npbgb_jacobi2d(void* A, void* B, int64_t ny, int64_t nx, int3
                                   int32_t dtype, void* stream) {
   using namespace npbgb;
   if (ny < 0 || nx < 0) return set_error(NPBGB_ERR_ARG, "jacobi2d: negative extent");
-  if (nx > (int64_t(1) << 31) * kBX) return set_error(NPBGB_ERR_ARG, "jacobi2d: nx too large");
   if (tsteps > 1 && ny >= 3 && nx >= 3) {
     if (!A || !B) return set_error(NPBGB_ERR_ARG, "jacobi2d: null array");
     if (A == B) return set_error(NPBGB_ERR_ARG, "jacobi2d: A and B alias");
   }
-  if (dtype == NPBGB_F64)
-    return run<double>(static_cast<double*>(A), static_cast<double*>(B), ny, nx, tsteps,
-                       as_stream(stream));
+  cudaStream_t st = as_stream(stream);
+  if (dtype == NPBGB_F64) {
+    double* a = static_cast<double*>(A);
+    double* b = static_cast<double*>(B);
+    return g_cfg_f64_emulation ? run<double, true>(a, b, ny, nx, tsteps, st)
+                               : run<double, false>(a, b, ny, nx, tsteps, st);
+  }
   if (dtype == NPBGB_F32)
-    return run<float>(static_cast<float*>(A), static_cast<float*>(B), ny, nx, tsteps,
-                      as_stream(stream));
+    return run<float, false>(static_cast<float*>(A), static_cast<float*>(B), ny, nx, tsteps, st);
   return set_error(NPBGB_ERR_DTYPE, "jacobi2d: dtype %d", dtype);
 }

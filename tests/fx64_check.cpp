@@ -1,0 +1,109 @@
+// Host check of npbench_gb300/csrc/fx64.cuh against the CPU's IEEE binary64.
+//
+// Built by tests/test_fx64.py with -ffp-contract=off.  For random and
+// adversarial operands it checks, bit for bit, that the fixed-point
+// emulation reproduces:
+//   * single additions and subtractions, including ties to even;
+//   * the Heat-3D update ((t0 + t1) + t2) + c, tx = 0.125 * ((nx - 2c) + px);
+//   * the Jacobi-2D sum (((c + w) + e) + s) + n.
+// Prints "OK <count>" and exits 0, or prints the first mismatch and exits 1.
+#include <cinttypes>
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+
+#include "../npbench_gb300/csrc/fx64.cuh"
+
+using namespace npbgb::fx;
+
+static std::mt19937_64 rng(12345);
+
+static uint64_t bits(double x) { return bits_of(x); }
+
+// Doubles in [2^-7, 1) or +0, with a bias towards patterns that make ties.
+static double draw() {
+  const int kind = static_cast<int>(rng() % 8);
+  if (kind == 0) return 0.0;
+  const uint64_t e = 1016 + rng() % 7;  // exponent field for [2^-7, 1)
+  uint64_t m = rng() & ((1ull << 52) - 1);
+  if (kind == 1) m &= ~((1ull << (rng() % 52)) - 1);  // trailing zeros
+  if (kind == 2) m |= (1ull << (rng() % 52)) - 1;     // trailing ones
+  if (kind == 3) m = 0;                                // powers of two
+  if (kind == 4) m = (1ull << 52) - 1;
+  return double_of((e << 52) | m);
+}
+
+static int fail(const char* what, double a, double b, double want, double got) {
+  std::printf("MISMATCH %s: a=%a b=%a want=%a (%016" PRIx64 ") got=%a (%016" PRIx64 ")\n", what,
+              a, b, want, bits(want), got, bits(got));
+  return 1;
+}
+
+int main(int argc, char** argv) {
+  const long n = argc > 1 ? std::atol(argv[1]) : 2000000;
+  long checks = 0;
+  for (long it = 0; it < n; ++it) {
+    const double a = draw(), b = draw();
+    bool oka, okb;
+    const int64_t A = from_f64_f59(a, oka), B = from_f64_f59(b, okb);
+    if (!oka || !okb) return fail("conversion rejected an in-range value", a, b, 0, 0);
+    if (to_f64<59>(A) != a || bits(to_f64<59>(A)) != bits(a)) return fail("roundtrip", a, b, a, to_f64<59>(A));
+    volatile double s = a + b, d = a - b, d2 = a - 2.0 * b;
+    if (bits(to_f64<59>(round53(A + B))) != bits(s)) return fail("add", a, b, s, to_f64<59>(round53(A + B)));
+    if (bits(to_f64<59>(round53(A - B))) != bits(d)) return fail("sub", a, b, d, to_f64<59>(round53(A - B)));
+    if (bits(to_f64<59>(round53(A - 2 * B))) != bits(d2))
+      return fail("sub2", a, b, d2, to_f64<59>(round53(A - 2 * B)));
+    // frame change: 0.125 * x is the same integer in frame 62
+    volatile double e = 0.125 * d2;
+    if (bits(to_f64<62>(round53(A - 2 * B))) != bits(e)) return fail("scale", a, b, e, to_f64<62>(round53(A - 2 * B)));
+    checks += 5;
+  }
+  // Heat-3D update.
+  for (long it = 0; it < n / 2; ++it) {
+    double v[7];
+    int64_t X[7];
+    for (int q = 0; q < 7; ++q) {
+      bool ok;
+      v[q] = draw();
+      X[q] = from_f64_f59(v[q], ok);
+    }
+    const double c = v[0];
+    volatile double t0 = 0.125 * ((v[1] - 2.0 * c) + v[2]);
+    volatile double t1 = 0.125 * ((v[3] - 2.0 * c) + v[4]);
+    volatile double t2 = 0.125 * ((v[5] - 2.0 * c) + v[6]);
+    volatile double want = ((t0 + t1) + t2) + c;
+    const int64_t C2 = X[0] * 2;
+    const int64_t S0 = round53(round53(X[1] - C2) + X[2]);
+    const int64_t S1 = round53(round53(X[3] - C2) + X[4]);
+    const int64_t S2 = round53(round53(X[5] - C2) + X[6]);
+    const int64_t W = round53(round53(round53(S0 + S1) + S2) + X[0] * 8);
+    const double got = to_f64<62>(W);
+    if (bits(got) != bits(want)) return fail("heat", v[0], v[1], want, got);
+    ++checks;
+  }
+  // Jacobi-2D sum (the 0.2 product stays a hardware multiply).
+  for (long it = 0; it < n / 2; ++it) {
+    double v[5];
+    int64_t X[5];
+    for (int q = 0; q < 5; ++q) {
+      bool ok;
+      v[q] = draw();
+      X[q] = from_f64_f59(v[q], ok);
+    }
+    volatile double want = (((v[0] + v[1]) + v[2]) + v[3]) + v[4];
+    const int64_t S = round53(round53(round53(round53(X[0] + X[1]) + X[2]) + X[3]) + X[4]);
+    const double got = to_f64<59>(S);
+    if (bits(got) != bits(want)) return fail("jacobi", v[0], v[1], want, got);
+    ++checks;
+  }
+  // Values the fast path must refuse.
+  const double refuse[] = {-0.0, -0.5, 1.0, 1.5, 0x1p-8, 0x1p-1030, 1e300, __builtin_inf(),
+                           __builtin_nan("")};
+  for (double r : refuse) {
+    bool ok;
+    from_f64_f59(r, ok);
+    if (ok) return fail("refuse", r, 0, 0, 0);
+  }
+  std::printf("OK %ld\n", checks);
+  return 0;
+}

@@ -200,3 +200,137 @@ def test_determinism_across_runs():
         stencils.heat_3d_kernel(9, dA, dB)
         outs.append((_host(dA), _host(dB)))
     assert bits_equal(outs[0][0], outs[1][0]) and bits_equal(outs[0][1], outs[1][1])
+
+
+def _mixed_range_field(shape, seed):
+    """U[0,1) with patches outside the fixed-point range: negatives, tiny, >= 1, -0.0."""
+    rng = np.random.default_rng(seed)
+    a = rng.random(shape)
+    flat = a.reshape(-1)
+    idx = rng.choice(flat.size, size=flat.size // 50, replace=False)
+    pool = np.array([-0.3, 1e-5, 2.5, -0.0, 0.0, 1.0, 3e-300, 0.999999999])
+    flat[idx] = pool[rng.integers(0, pool.size, idx.size)]
+    return a
+
+
+@pytest.mark.parametrize("field", ["uniform", "mixed", "scaled"])
+def test_heat_f64_integer_and_hardware_paths_agree(field):
+    """The fixed-point binary64 path and the hardware path give the oracle's bits."""
+    from npbench_gb300 import _lib
+    shape = (70, 90, 100)
+    if field == "uniform":
+        A = workloads.uniform_heat(shape, np.float64, seed=21)[0]
+    elif field == "mixed":
+        A = _mixed_range_field(shape, 22)
+    else:
+        A = 3.0 * workloads.uniform_heat(shape, np.float64, seed=23)[0] - 1.0
+    ref_a, ref_b = A.copy(), A.copy()
+    cref.heat_3d_kernel(6, ref_a, ref_b)
+    for emul in (1, 0):
+        old = _lib.set_config(_lib.NPBGB_CFG_F64_EMULATION, emul)
+        try:
+            dA, dB = _dev(A), _dev(A)
+            stencils.heat_3d_kernel(6, dA, dB)
+            assert bits_equal(_host(dA), ref_a), (field, emul, first_diff(_host(dA), ref_a))
+            assert bits_equal(_host(dB), ref_b), (field, emul)
+        finally:
+            _lib.set_config(_lib.NPBGB_CFG_F64_EMULATION, old)
+
+
+@pytest.mark.parametrize("chunk", [1, 3, 8, 33, 500])
+def test_heat_chunking_does_not_change_bits(chunk):
+    from npbench_gb300 import _lib
+    A = workloads.uniform_heat((41, 37, 70), np.float64, seed=chunk)[0]
+    ref_a, ref_b = A.copy(), A.copy()
+    cref.heat_3d_kernel(4, ref_a, ref_b)
+    old = _lib.set_config(_lib.NPBGB_CFG_HEAT_CHUNK, chunk)
+    try:
+        for dt in (np.float64, np.float32):
+            a = A.astype(dt)
+            ra, rb = a.copy(), a.copy()
+            cref.heat_3d_kernel(4, ra, rb)
+            dA, dB = _dev(a), _dev(a)
+            stencils.heat_3d_kernel(4, dA, dB)
+            assert bits_equal(_host(dA), ra) and bits_equal(_host(dB), rb), (chunk, dt)
+    finally:
+        _lib.set_config(_lib.NPBGB_CFG_HEAT_CHUNK, old)
+
+
+@pytest.mark.parametrize("tma", [1, 0])
+@pytest.mark.parametrize("shape", [(256, 256, 256), (66, 130, 200), (9, 40, 34), (5, 37, 46)])
+def test_heat_tma_and_plain_staging(tma, shape):
+    """TMA staging (16-byte-aligned rows) and plain staging give the oracle's bits."""
+    from npbench_gb300 import _lib
+    old = _lib.set_config(_lib.NPBGB_CFG_HEAT_TMA, tma)
+    try:
+        for dtype in (np.float64, np.float32):
+            A = _mixed_range_field(shape, 31).astype(dtype) if shape[0] < 100 else \
+                workloads.uniform_heat(shape, dtype, seed=30)[0]
+            ra, rb = A.copy(), A.copy()
+            T = 3 if shape[0] == 256 else 7
+            cref.heat_3d_kernel(T, ra, rb)
+            dA, dB = _dev(A), _dev(A)
+            stencils.heat_3d_kernel(T, dA, dB)
+            _lib.device_status()
+            assert bits_equal(_host(dA), ra), (tma, shape, dtype, first_diff(_host(dA), ra))
+            assert bits_equal(_host(dB), rb), (tma, shape, dtype)
+    finally:
+        _lib.set_config(_lib.NPBGB_CFG_HEAT_TMA, old)
+
+
+@pytest.mark.parametrize("field", ["uniform", "mixed", "scaled"])
+def test_jacobi_f64_integer_and_hardware_paths_agree(field):
+    from npbench_gb300 import _lib
+    shape = (300, 517)
+    if field == "uniform":
+        A, B = workloads.uniform_pair(shape, np.float64, seed=41)
+    elif field == "mixed":
+        A, B = _mixed_range_field(shape, 42), _mixed_range_field(shape, 43)
+    else:
+        A, B = (4.0 * x - 2.0 for x in workloads.uniform_pair(shape, np.float64, seed=44))
+    ra, rb = A.copy(), B.copy()
+    cref.jacobi_2d_kernel(9, ra, rb)
+    for emul in (1, 0):
+        old = _lib.set_config(_lib.NPBGB_CFG_F64_EMULATION, emul)
+        try:
+            dA, dB = _dev(A), _dev(B)
+            stencils.jacobi_2d_kernel(9, dA, dB)
+            assert bits_equal(_host(dA), ra), (field, emul, first_diff(_host(dA), ra))
+            assert bits_equal(_host(dB), rb), (field, emul)
+        finally:
+            _lib.set_config(_lib.NPBGB_CFG_F64_EMULATION, old)
+
+
+@pytest.mark.parametrize("chunk", [1, 5, 64, 4000])
+def test_jacobi_chunking_does_not_change_bits(chunk):
+    from npbench_gb300 import _lib
+    old = _lib.set_config(_lib.NPBGB_CFG_JACOBI_CHUNK, chunk)
+    try:
+        for dt in (np.float64, np.float32):
+            A, B = workloads.uniform_pair((123, 301), dt, seed=chunk)
+            ra, rb = A.copy(), B.copy()
+            cref.jacobi_2d_kernel(5, ra, rb)
+            dA, dB = _dev(A), _dev(B)
+            stencils.jacobi_2d_kernel(5, dA, dB)
+            assert bits_equal(_host(dA), ra) and bits_equal(_host(dB), rb), (chunk, dt)
+    finally:
+        _lib.set_config(_lib.NPBGB_CFG_JACOBI_CHUNK, old)
+
+
+def test_bounded_device_wait_reports_timeout_and_context_survives():
+    """A wait that nothing completes gives up after its limit; the host reads the status."""
+    from npbench_gb300 import _lib
+    lib = _lib.load()
+    _lib.device_status()  # clean slate
+    st = torch.cuda.current_stream().cuda_stream
+    assert lib.npbgb_selftest_wait_timeout(20_000_000, st) == _lib.NPBGB_OK  # 20 ms
+    with pytest.raises(_lib.NpbgbError) as ei:
+        _lib.device_status()
+    assert ei.value.status == _lib.NPBGB_ERR_TIMEOUT
+    _lib.device_status()  # cleared after being reported
+    # the context is still usable
+    A, B = workloads.uniform_pair((50, 60), np.float64, seed=1)
+    dA, dB = _dev(A), _dev(B)
+    stencils.jacobi_2d_kernel(3, dA, dB)
+    cref.jacobi_2d_kernel(3, A, B)
+    assert bits_equal(_host(dA), A)
