@@ -53,6 +53,29 @@ extern "C" {
 #define NPBGB_CFG_HEAT_TMA 3      /* 1 (default): heat3d stages planes with TMA when the
                                      arrays allow it; 0: plain loads only */
 #define NPBGB_CFG_JACOBI_CHUNK 4  /* rows per warp in jacobi2d; 0 = automatic */
+#define NPBGB_CFG_HEAT_ROWS 5     /* axis-1 tile rows per thread in heat3d (TMA): 1, 2, 4 */
+#define NPBGB_CFG_HEAT_HW_ROWS 6  /* heat3d binary64: tile rows per CTA evaluated with
+                                     hardware binary64 next to the fixed-point rows */
+#define NPBGB_CFG_F64_CVT 7       /* 1: fixed-point conversions use the binary64
+                                     convert instructions; 0: integer bit operations */
+
+/* Grid kinds for batches. */
+#define NPBGB_KIND_JACOBI2D 0
+#define NPBGB_KIND_HEAT3D 1
+
+/* One grid of a batch: a ping-pong pair of device arrays and its own step
+ * count.  For NPBGB_KIND_JACOBI2D the arrays are (n0, n1) and n2 is ignored. */
+typedef struct npbgb_grid {
+  void* a;           /* holds the field at step 0 and the newest field at the end */
+  void* b;           /* second buffer (holds the previous field at the end) */
+  int64_t n0, n1, n2;
+  int32_t kind;      /* NPBGB_KIND_* */
+  int32_t dtype;     /* NPBGB_F64 or NPBGB_F32 */
+  int32_t tsteps;    /* the reference's TSTEPS: 2*(tsteps-1) half-sweeps */
+  int32_t band_rows; /* rows per scheduling band; 0 = the batch default */
+} npbgb_grid;
+
+typedef struct npbgb_batch npbgb_batch;
 
 /* Library identification: "npbgb <version> sm_103a". */
 NPBGB_API const char* npbgb_version(void);
@@ -107,6 +130,27 @@ NPBGB_API int32_t npbgb_heat3d(void* A, void* B, int64_t n0, int64_t n1, int64_t
  * NPBGB_F64 (the limiter's sign tests are kept in binary64). */
 NPBGB_API int32_t npbgb_hdiff(const void* in_field, void* out_field, const void* coeff, int64_t I,
                     int64_t J, int64_t K, int32_t dtype, void* stream);
+
+/* Batches: many independent grids advanced by one persistent launch.
+ *
+ * npbgb_batch_create plans a batch: each grid is cut into bands of
+ * band_rows rows (0 = 32, or the grid's own band_rows), bands are assigned
+ * to the CTAs of one cooperative launch with equal work per CTA, and the
+ * plan (band table, per-band step counters) is stored in device memory
+ * allocated here.  Each grid ends exactly as npbgb_jacobi2d would leave it
+ * (bit-identical), i.e. as the reference's kernel(TSTEPS, A, B) per grid,
+ * polybench/jacobi_2d/jacobi_2d_numpy.py:4-10.
+ * npbgb_batch_launch runs the whole batch: a counter reset and one
+ * persistent kernel on `stream`; with use_graph != 0 the two are captured
+ * once into a CUDA graph and replayed.  Bounded waits: a CTA that makes no
+ * progress for two seconds records an error reported by npbgb_device_status.
+ * The grids' arrays must stay allocated while the batch is in use. */
+NPBGB_API int32_t npbgb_batch_create(const npbgb_grid* grids, int64_t count, int32_t band_rows,
+                                     npbgb_batch** out);
+NPBGB_API int32_t npbgb_batch_launch(npbgb_batch* batch, int32_t use_graph, void* stream);
+NPBGB_API int32_t npbgb_batch_info(const npbgb_batch* batch, int64_t* nbands, int64_t* nctas,
+                                   int64_t* updates);
+NPBGB_API int32_t npbgb_batch_destroy(npbgb_batch* batch);
 
 #ifdef __cplusplus
 }

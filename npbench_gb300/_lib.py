@@ -23,6 +23,21 @@ NPBGB_CFG_F64_EMULATION = 1
 NPBGB_CFG_HEAT_CHUNK = 2
 NPBGB_CFG_HEAT_TMA = 3
 NPBGB_CFG_JACOBI_CHUNK = 4
+NPBGB_CFG_HEAT_ROWS = 5
+NPBGB_CFG_HEAT_HW_ROWS = 6
+NPBGB_CFG_F64_CVT = 7
+
+NPBGB_KIND_JACOBI2D = 0
+NPBGB_KIND_HEAT3D = 1
+
+
+class Grid(ctypes.Structure):
+    """npbgb_grid of include/npbgb.h."""
+    _fields_ = [("a", ctypes.c_void_p), ("b", ctypes.c_void_p), ("n0", ctypes.c_int64),
+                ("n1", ctypes.c_int64), ("n2", ctypes.c_int64), ("kind", ctypes.c_int32),
+                ("dtype", ctypes.c_int32), ("tsteps", ctypes.c_int32),
+                ("band_rows", ctypes.c_int32)]
+
 
 # Every symbol include/npbgb.h declares, with its ctypes signature.
 _i32, _i64, _vp, _cp = ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p, ctypes.c_char_p
@@ -34,6 +49,11 @@ SIGNATURES = {
     "npbgb_get_config": (_i32, [_i32, ctypes.POINTER(_i64)]),
     "npbgb_device_status": (_i32, [_vp]),
     "npbgb_selftest_wait_timeout": (_i32, [_i64, _vp]),
+    "npbgb_batch_create": (_i32, [ctypes.POINTER(Grid), _i64, _i32, ctypes.POINTER(_vp)]),
+    "npbgb_batch_launch": (_i32, [_vp, _i32, _vp]),
+    "npbgb_batch_info": (_i32, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64),
+                                 ctypes.POINTER(_i64)]),
+    "npbgb_batch_destroy": (_i32, [_vp]),
     "npbgb_jacobi2d": (_i32, [_vp, _vp, _i64, _i64, _i32, _i32, _vp]),
     "npbgb_heat3d": (_i32, [_vp, _vp, _i64, _i64, _i64, _i32, _i32, _vp]),
     "npbgb_hdiff": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i32, _vp]),

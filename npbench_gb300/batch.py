@@ -1,0 +1,84 @@
+"""Many independent Jacobi-2D grids advanced by one persistent launch (libnpbgb batches).
+
+    with Batch([(A0, B0, T0), (A1, B1, T1), ...]) as batch:
+        batch.launch()              # one counter reset + one cooperative persistent kernel
+        batch.launch(graph=True)    # the same, captured once into a CUDA graph and replayed
+
+Every (A, B, TSTEPS) is a pair of 2D CUDA tensors of one dtype (float32 or
+float64) and its own step count.  After a launch each pair holds what
+``kernel(TSTEPS, A, B)`` of polybench/jacobi_2d/jacobi_2d_numpy.py:4-10 leaves,
+bit for bit.  The tensors must stay alive while the batch is used.
+"""
+import ctypes
+
+from . import _lib
+
+__all__ = ["Batch"]
+
+
+class Batch:
+    def __init__(self, grids, band_rows=0, band_rows_of=None):
+        """grids: iterable of (A, B, TSTEPS); band_rows_of(A) may pick rows per band."""
+        import torch
+        self._keep = []
+        arr = (_lib.Grid * max(1, len(grids)))()
+        for n, (A, B, T) in enumerate(grids):
+            if not (isinstance(A, torch.Tensor) and isinstance(B, torch.Tensor)):
+                raise TypeError("batch grids must be CUDA tensors")
+            if A.device.type != "cuda" or B.device != A.device:
+                raise ValueError("batch grids must be on one CUDA device")
+            if A.dim() != 2 or A.shape != B.shape or A.dtype != B.dtype:
+                raise ValueError(f"grid {n}: A and B must be 2D with equal shape and dtype")
+            if not (A.is_contiguous() and B.is_contiguous()):
+                raise ValueError(f"grid {n}: tensors must be contiguous")
+            if A.dtype == torch.float64:
+                code = _lib.NPBGB_F64
+            elif A.dtype == torch.float32:
+                code = _lib.NPBGB_F32
+            else:
+                raise TypeError(f"grid {n}: unsupported dtype {A.dtype}")
+            g = arr[n]
+            g.a, g.b = A.data_ptr(), B.data_ptr()
+            g.n0, g.n1, g.n2 = A.shape[0], A.shape[1], 1
+            g.kind = _lib.NPBGB_KIND_JACOBI2D
+            g.dtype = code
+            g.tsteps = int(T)
+            g.band_rows = int(band_rows_of(A)) if band_rows_of else 0
+            self._keep.append((A, B))
+        self.device = self._keep[0][0].device if self._keep else None
+        h = ctypes.c_void_p()
+        _lib.check(_lib.load().npbgb_batch_create(arr, len(grids), int(band_rows), ctypes.byref(h)),
+                   "npbgb_batch_create")
+        self._h = h
+
+    def launch(self, graph=False, stream=None):
+        import torch
+        if self._h is None:
+            raise RuntimeError("batch destroyed")
+        if stream is None and self.device is not None:
+            stream = torch.cuda.current_stream(self.device).cuda_stream
+        _lib.check(_lib.load().npbgb_batch_launch(self._h, 1 if graph else 0, stream),
+                   "npbgb_batch_launch")
+
+    def info(self):
+        nb, nc, up = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _lib.check(_lib.load().npbgb_batch_info(self._h, ctypes.byref(nb), ctypes.byref(nc),
+                                                ctypes.byref(up)), "npbgb_batch_info")
+        return {"bands": nb.value, "ctas": nc.value, "updates": up.value}
+
+    def close(self):
+        if self._h is not None:
+            _lib.load().npbgb_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,355 @@
+// Batched time stepping of many independent Jacobi-2D grids in one persistent launch.
+//
+// Every grid of the batch (any shape, binary32 or binary64, its own TSTEPS) is
+// cut into bands of rows.  A band is owned by exactly one CTA of a
+// cooperative (all-resident) persistent kernel; the host assigns bands to
+// CTAs so that the CTAs carry equal work (longest-processing-time greedy).
+// Each band keeps in global memory the number of half-sweeps it has
+// completed.  A CTA advances one of its bands by one half-sweep when both
+// neighbouring bands of the same grid have completed at least as many
+// half-sweeps: that gives the band the rows it reads (read-after-write) and
+// guarantees that no neighbour still reads the rows it overwrites
+// (write-after-read).  Counters are published with release semantics after
+// the CTA's stores, read with acquire semantics, and grid data is read
+// through L2 (ld.global.cg) so no SM sees stale L1 lines.  The band whose
+// count is the global minimum is always ready, so the batch cannot deadlock;
+// every wait is still bounded (no progress for kBatchLimitNs -> error word,
+// kernel exits).
+//
+// Per point the arithmetic is that of jacobi2d.cu (bit-identical to
+// polybench/jacobi_2d/jacobi_2d_numpy.py:6-10), including the fixed-point
+// binary64 path.
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <queue>
+#include <vector>
+
+#include "jacobi_core.cuh"
+#include "npbgb_common.cuh"
+#include "tma.cuh"
+
+namespace npbgb {
+
+extern int64_t g_cfg_f64_emulation;
+
+namespace {
+
+constexpr int kBWarps = 8;
+constexpr int kBThreads = 32 * kBWarps;
+constexpr uint64_t kBatchLimitNs = 2000000000ull;  // two seconds without progress
+
+struct BandDesc {
+  void* a;          // array holding the field after an even number of half-sweeps
+  void* b;          // the other array
+  int32_t ny, nx;   // grid extents
+  int32_t r0, r1;   // interior rows [r0, r1) of this band
+  int32_t steps;    // half-sweeps to perform: 2 * (TSTEPS - 1)
+  int32_t dtype;    // NPBGB_F64 / NPBGB_F32
+  int32_t left;     // band above (rows < r0) of the same grid, or -1
+  int32_t right;    // band below (rows >= r1), or -1
+};
+
+__device__ unsigned int g_batch_error;  // bit 0: a CTA made no progress for the limit
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// One half-sweep of band rows [r0, r1) from src to dst over all interior
+// columns: the CTA's warps take the band's 32-column strips in turn.  Loads
+// and stores go through L2 (other CTAs wrote, or will read, these rows).
+template <typename T, bool FX>
+__device__ __noinline__ void band_half_sweep(const T* src, T* dst, int64_t nx, int r0, int r1,
+                                             uint32_t one) {
+  const int warp = threadIdx.x >> 5;
+  for (int64_t k0 = 1 + int64_t(warp) * 32; k0 < nx - 1; k0 += 32 * kBWarps)
+    jcore::strip_rows<T, FX, true, 4>(src, dst, nx, k0, r0, r1, one);
+}
+
+__global__ void __launch_bounds__(kBThreads)
+batch_persistent(const BandDesc* __restrict__ bands, uint32_t* done, const int32_t* __restrict__ cta_off,
+                 const int32_t* __restrict__ cta_bands, int f64_emulation, uint32_t one) {
+  __shared__ int s_flag;
+  const int tid = threadIdx.x;
+  const int b_begin = cta_off[blockIdx.x], b_end = cta_off[blockIdx.x + 1];
+  uint64_t last_progress = tma::globaltimer();
+  int cursor = b_begin;
+  for (;;) {
+    bool all_done = true, progressed = false;
+    for (int n = 0; n < b_end - b_begin; ++n) {
+      const int idx = cta_bands[cursor];
+      cursor = cursor + 1 < b_end ? cursor + 1 : b_begin;
+      const BandDesc d = bands[idx];
+      // Advance this band as far as its neighbours allow.
+      for (;;) {
+        if (tid == 0) {
+          const uint32_t s = done[idx];  // only this CTA writes it
+          int state = 0;                 // 0 finished, 1 ready, 2 blocked
+          if (int(s) < d.steps) {
+            const bool ok_l = d.left < 0 || ld_acquire(done + d.left) >= s;
+            const bool ok_r = d.right < 0 || ld_acquire(done + d.right) >= s;
+            state = (ok_l && ok_r) ? 1 : 2;
+          }
+          s_flag = state == 1 ? int(s) : (state == 0 ? -1 : -2);
+        }
+        __syncthreads();
+        const int s = s_flag;
+        __syncthreads();
+        if (s == -1) break;           // finished
+        all_done = false;
+        if (s == -2) break;           // blocked for now
+        const void* src = (s & 1) ? d.b : d.a;
+        void* dst = (s & 1) ? d.a : d.b;
+        if (d.dtype == NPBGB_F64) {
+          if (f64_emulation)
+            band_half_sweep<double, true>(static_cast<const double*>(src), static_cast<double*>(dst),
+                                          d.nx, d.r0, d.r1, one);
+          else
+            band_half_sweep<double, false>(static_cast<const double*>(src), static_cast<double*>(dst),
+                                           d.nx, d.r0, d.r1, one);
+        } else {
+          band_half_sweep<float, false>(static_cast<const float*>(src), static_cast<float*>(dst),
+                                        d.nx, d.r0, d.r1, one);
+        }
+        __syncthreads();
+        if (tid == 0) {
+          __threadfence();
+          st_release(done + idx, uint32_t(s + 1));
+        }
+        progressed = true;
+      }
+    }
+    if (all_done) return;
+    if (progressed) {
+      last_progress = tma::globaltimer();
+    } else {
+      if (tma::globaltimer() - last_progress > kBatchLimitNs) {
+        if (tid == 0) atomicOr(&g_batch_error, 1u);
+        return;
+      }
+      __nanosleep(200);
+    }
+  }
+}
+
+}  // namespace
+
+uint32_t take_batch_device_error() {
+  unsigned int v = 0, zero = 0;
+  if (cudaMemcpyFromSymbol(&v, g_batch_error, sizeof(v)) != cudaSuccess) return 0xffffffffu;
+  if (v) cudaMemcpyToSymbol(g_batch_error, &zero, sizeof(zero));
+  return v;
+}
+
+}  // namespace npbgb
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct npbgb_batch {
+  int device = 0;
+  int64_t nbands = 0;
+  int nctas = 0;
+  npbgb::BandDesc* d_bands = nullptr;
+  uint32_t* d_done = nullptr;
+  int32_t* d_cta_off = nullptr;
+  int32_t* d_cta_bands = nullptr;
+  int64_t updates = 0;
+  cudaGraphExec_t graph = nullptr;
+  cudaStream_t graph_stream = nullptr;
+};
+
+namespace {
+
+void free_batch(npbgb_batch* b) {
+  if (!b) return;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->d_bands);
+  cudaFree(b->d_done);
+  cudaFree(b->d_cta_off);
+  cudaFree(b->d_cta_bands);
+  delete b;
+}
+
+int32_t launch_batch(npbgb_batch* b, cudaStream_t st) {
+  using namespace npbgb;
+  cudaError_t e = cudaMemsetAsync(b->d_done, 0, sizeof(uint32_t) * size_t(b->nbands), st);
+  if (e != cudaSuccess) return cuda_status(e, "batch: reset counters");
+  int f64_emul = int(g_cfg_f64_emulation);
+  uint32_t one = 1;
+  void* args[] = {&b->d_bands, &b->d_done, &b->d_cta_off, &b->d_cta_bands, &f64_emul, &one};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(unsigned(b->nctas));
+  cfg.blockDim = dim3(kBThreads);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(batch_persistent), args);
+  if (e != cudaSuccess) return cuda_status(e, "batch: cooperative launch");
+  return NPBGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t npbgb_batch_create(const npbgb_grid* grids, int64_t count, int32_t band_rows,
+                           npbgb_batch** out) {
+  using namespace npbgb;
+  if (!out) return set_error(NPBGB_ERR_ARG, "batch: null output");
+  *out = nullptr;
+  if (count < 0 || (count > 0 && !grids)) return set_error(NPBGB_ERR_ARG, "batch: bad grid list");
+  if (band_rows < 0) return set_error(NPBGB_ERR_ARG, "batch: band_rows < 0");
+  std::vector<BandDesc> bands;
+  int64_t updates = 0;
+  for (int64_t g = 0; g < count; ++g) {
+    const npbgb_grid& G = grids[g];
+    if (G.kind != NPBGB_KIND_JACOBI2D)
+      return set_error(NPBGB_ERR_ARG, "batch: grid %lld: only jacobi2d grids are batched", (long long)g);
+    if (G.dtype != NPBGB_F64 && G.dtype != NPBGB_F32)
+      return set_error(NPBGB_ERR_DTYPE, "batch: grid %lld: dtype %d", (long long)g, G.dtype);
+    if (G.n0 < 0 || G.n1 < 0 || G.n0 > 0x7fffffff || G.n1 > 0x7fffffff)
+      return set_error(NPBGB_ERR_ARG, "batch: grid %lld: bad extents", (long long)g);
+    if (G.tsteps <= 1 || G.n0 < 3 || G.n1 < 3) continue;  // nothing to do, as in the reference
+    if (!G.a || !G.b || G.a == G.b)
+      return set_error(NPBGB_ERR_ARG, "batch: grid %lld: null or aliased arrays", (long long)g);
+    const int ny = int(G.n0), nx = int(G.n1);
+    int h = G.band_rows > 0 ? G.band_rows : (band_rows > 0 ? band_rows : 32);
+    const int interior = ny - 2;
+    const int nb = int(cdiv(interior, h));
+    const int first = int(bands.size());
+    for (int q = 0; q < nb; ++q) {
+      BandDesc d;
+      d.a = G.a;
+      d.b = G.b;
+      d.ny = ny;
+      d.nx = nx;
+      d.r0 = 1 + q * h;
+      d.r1 = std::min(1 + (q + 1) * h, ny - 1);
+      d.steps = 2 * (G.tsteps - 1);
+      d.dtype = G.dtype;
+      d.left = q > 0 ? first + q - 1 : -1;
+      d.right = q + 1 < nb ? first + q + 1 : -1;
+      bands.push_back(d);
+    }
+    updates += int64_t(2) * (G.tsteps - 1) * int64_t(interior) * (nx - 2);
+  }
+  auto* b = new (std::nothrow) npbgb_batch();
+  if (!b) return set_error(NPBGB_ERR_NOMEM, "batch: host allocation");
+  cudaGetDevice(&b->device);
+  b->nbands = int64_t(bands.size());
+  b->updates = updates;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_persistent, kBThreads, 0);
+  if (per_sm <= 0) per_sm = 1;
+  const int64_t slots = int64_t(sm_count()) * per_sm;
+  b->nctas = int(std::max<int64_t>(1, std::min<int64_t>(slots, b->nbands)));
+  // Longest-processing-time greedy assignment of bands to CTAs by work.
+  std::vector<std::vector<int32_t>> lists(size_t(b->nctas));
+  {
+    std::vector<int32_t> order(bands.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = int32_t(i);
+    auto work = [&](int32_t i) {
+      const BandDesc& d = bands[size_t(i)];
+      return double(d.r1 - d.r0) * double(d.nx - 2) * d.steps * (d.dtype == NPBGB_F64 ? 2.0 : 1.0);
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return work(x) > work(y); });
+    using Item = std::pair<double, int>;
+    std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
+    for (int c = 0; c < b->nctas; ++c) heap.push({0.0, c});
+    for (int32_t i : order) {
+      Item it = heap.top();
+      heap.pop();
+      lists[size_t(it.second)].push_back(i);
+      heap.push({it.first + work(i), it.second});
+    }
+  }
+  std::vector<int32_t> off(size_t(b->nctas) + 1, 0), flat;
+  flat.reserve(bands.size());
+  for (int c = 0; c < b->nctas; ++c) {
+    off[size_t(c)] = int32_t(flat.size());
+    flat.insert(flat.end(), lists[size_t(c)].begin(), lists[size_t(c)].end());
+  }
+  off[size_t(b->nctas)] = int32_t(flat.size());
+  auto fail = [&](cudaError_t e, const char* what) {
+    free_batch(b);
+    return cuda_status(e, what);
+  };
+  const size_t nb_alloc = std::max<size_t>(1, bands.size());
+  cudaError_t e;
+  if ((e = cudaMalloc(&b->d_bands, sizeof(BandDesc) * nb_alloc)) != cudaSuccess) return fail(e, "batch: alloc");
+  if ((e = cudaMalloc(&b->d_done, sizeof(uint32_t) * nb_alloc)) != cudaSuccess) return fail(e, "batch: alloc");
+  if ((e = cudaMalloc(&b->d_cta_off, sizeof(int32_t) * off.size())) != cudaSuccess) return fail(e, "batch: alloc");
+  if ((e = cudaMalloc(&b->d_cta_bands, sizeof(int32_t) * nb_alloc)) != cudaSuccess) return fail(e, "batch: alloc");
+  if (!bands.empty()) {
+    if ((e = cudaMemcpy(b->d_bands, bands.data(), sizeof(BandDesc) * bands.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return fail(e, "batch: upload");
+    if ((e = cudaMemcpy(b->d_cta_bands, flat.data(), sizeof(int32_t) * flat.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return fail(e, "batch: upload");
+  }
+  if ((e = cudaMemcpy(b->d_cta_off, off.data(), sizeof(int32_t) * off.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return fail(e, "batch: upload");
+  *out = b;
+  return NPBGB_OK;
+}
+
+int32_t npbgb_batch_launch(npbgb_batch* b, int32_t use_graph, void* stream) {
+  using namespace npbgb;
+  if (!b) return set_error(NPBGB_ERR_ARG, "batch: null handle");
+  if (b->nbands == 0) return NPBGB_OK;
+  cudaStream_t st = as_stream(stream);
+  if (!use_graph) return launch_batch(b, st);
+  if (!b->graph) {
+    cudaStream_t cap;
+    cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_status(e, "batch: capture stream");
+    e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+      cudaStreamDestroy(cap);
+      return cuda_status(e, "batch: begin capture");
+    }
+    const int32_t r = launch_batch(b, cap);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(cap, &graph);
+    cudaStreamDestroy(cap);
+    if (r != NPBGB_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return r;
+    }
+    if (e != cudaSuccess) return cuda_status(e, "batch: end capture");
+    e = cudaGraphInstantiate(&b->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      b->graph = nullptr;
+      return cuda_status(e, "batch: instantiate graph");
+    }
+  }
+  cudaError_t e = cudaGraphLaunch(b->graph, st);
+  if (e != cudaSuccess) return cuda_status(e, "batch: graph launch");
+  return NPBGB_OK;
+}
+
+int32_t npbgb_batch_info(const npbgb_batch* b, int64_t* nbands, int64_t* nctas, int64_t* updates) {
+  using namespace npbgb;
+  if (!b) return set_error(NPBGB_ERR_ARG, "batch: null handle");
+  if (nbands) *nbands = b->nbands;
+  if (nctas) *nctas = b->nctas;
+  if (updates) *updates = b->updates;
+  return NPBGB_OK;
+}
+
+int32_t npbgb_batch_destroy(npbgb_batch* b) {
+  free_batch(b);
+  return NPBGB_OK;
+}
+
+}  // extern "C"

@@ -14,9 +14,13 @@ static thread_local char g_last_error[512] = "";
 int64_t g_cfg_f64_emulation = 1;
 int64_t g_cfg_heat_chunk = 0;
 int64_t g_cfg_heat_tma = 1;
+int64_t g_cfg_heat_rows = 2;
+int64_t g_cfg_heat_hw_rows = 0;
+int64_t g_cfg_f64_cvt = 0;
 int64_t g_cfg_jacobi_chunk = 0;
 
 uint32_t take_heat_device_error();
+uint32_t take_batch_device_error();
 int32_t launch_wait_timeout_selftest(uint64_t limit_ns, cudaStream_t st);
 
 int32_t set_error(int32_t code, const char* fmt, ...) {
@@ -107,6 +111,18 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       if (value < 0 || value > (1 << 20)) return set_error(NPBGB_ERR_ARG, "jacobi chunk out of range");
       g_cfg_jacobi_chunk = value;
       return NPBGB_OK;
+    case NPBGB_CFG_HEAT_ROWS:
+      if (value != 1 && value != 2 && value != 4) return set_error(NPBGB_ERR_ARG, "heat rows: 1, 2 or 4");
+      g_cfg_heat_rows = value;
+      return NPBGB_OK;
+    case NPBGB_CFG_HEAT_HW_ROWS:
+      if (value < 0 || value > 32) return set_error(NPBGB_ERR_ARG, "heat hw rows: 0..32");
+      g_cfg_heat_hw_rows = value;
+      return NPBGB_OK;
+    case NPBGB_CFG_F64_CVT:
+      if (value != 0 && value != 1) return set_error(NPBGB_ERR_ARG, "f64 cvt: 0 or 1");
+      g_cfg_f64_cvt = value;
+      return NPBGB_OK;
     default:
       return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
   }
@@ -120,6 +136,9 @@ int32_t npbgb_get_config(int32_t key, int64_t* value) {
     case NPBGB_CFG_HEAT_CHUNK: *value = g_cfg_heat_chunk; return NPBGB_OK;
     case NPBGB_CFG_HEAT_TMA: *value = g_cfg_heat_tma; return NPBGB_OK;
     case NPBGB_CFG_JACOBI_CHUNK: *value = g_cfg_jacobi_chunk; return NPBGB_OK;
+    case NPBGB_CFG_HEAT_ROWS: *value = g_cfg_heat_rows; return NPBGB_OK;
+    case NPBGB_CFG_HEAT_HW_ROWS: *value = g_cfg_heat_hw_rows; return NPBGB_OK;
+    case NPBGB_CFG_F64_CVT: *value = g_cfg_f64_cvt; return NPBGB_OK;
     default: return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
   }
 }
@@ -129,8 +148,11 @@ int32_t npbgb_device_status(void* stream) {
   cudaError_t e = stream ? cudaStreamSynchronize(as_stream(stream)) : cudaDeviceSynchronize();
   if (e != cudaSuccess) return cuda_status(e, "device status");
   const uint32_t h = take_heat_device_error();
-  if (h == 0xffffffffu) return set_error(NPBGB_ERR_CUDA, "reading the device error word");
+  const uint32_t bt = take_batch_device_error();
+  if (h == 0xffffffffu || bt == 0xffffffffu)
+    return set_error(NPBGB_ERR_CUDA, "reading the device error words");
   if (h) return set_error(NPBGB_ERR_TIMEOUT, "a bounded device wait gave up (heat3d)");
+  if (bt) return set_error(NPBGB_ERR_TIMEOUT, "a batch CTA made no progress within its limit");
   return NPBGB_OK;
 }
 

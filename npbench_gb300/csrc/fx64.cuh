@@ -123,6 +123,73 @@ NPBGB_FX_FN int64_t from_f64_f59_or_poison(double x) {
 
 NPBGB_FX_FN uint32_t hi32(int64_t x) { return static_cast<uint32_t>(static_cast<uint64_t>(x) >> 32); }
 
+// x + y for 64-bit integers, issued as two 32-bit multiply-adds with the
+// multiplier `one` (== 1, passed at run time so the compiler cannot fold it
+// away).  On the GPU this moves the add from the integer ALU pipe, which the
+// rounding steps saturate, to the multiply-add pipe.
+NPBGB_FX_FN int64_t add64(int64_t x, int64_t y, uint32_t one) {
+#if defined(__CUDA_ARCH__)
+  uint64_t r;
+  const uint32_t ylo = static_cast<uint32_t>(y), yhi = static_cast<uint32_t>(static_cast<uint64_t>(y) >> 32);
+  asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(r) : "r"(ylo), "r"(one), "l"(x));
+  uint32_t rlo = static_cast<uint32_t>(r), rhi = static_cast<uint32_t>(r >> 32);
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(rhi) : "r"(yhi), "r"(one), "r"(rhi));
+  return static_cast<int64_t>((static_cast<uint64_t>(rhi) << 32) | rlo);
+#else
+  (void)one;
+  return static_cast<int64_t>(static_cast<uint64_t>(x) + static_cast<uint64_t>(y));
+#endif
+}
+
+// round53 with its final 64-bit add on the multiply-add pipe (see add64).
+NPBGB_FX_FN int64_t round53m(int64_t x, uint32_t one) {
+  const int32_t hi = static_cast<int32_t>(x >> 32);
+  const uint32_t h = static_cast<uint32_t>(hi ^ (hi >> 31));
+  int sh = (31 - clz32(h)) - 20;
+  sh = sh < 0 ? 0 : sh;
+  const uint32_t mask = (1u << sh) - 1u;
+  const uint32_t lo = static_cast<uint32_t>(x);
+  const uint32_t add = ((mask >> 1) + ((lo >> sh) & 1u)) & mask;
+#if defined(__CUDA_ARCH__)
+  uint64_t r;
+  asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(r) : "r"(add), "r"(one), "l"(x));
+#else
+  (void)one;
+  const uint64_t r = static_cast<uint64_t>(x) + add;
+#endif
+  return static_cast<int64_t>(r & ~static_cast<uint64_t>(mask));
+}
+
+// x -> frame-59 integer using the binary64 conversion path instead of integer
+// bit manipulation: x * 2^59 (an exponent change, exact for accepted x) is
+// converted with round-toward-zero, which is exact because the scaled value is
+// an integer.  +0.0 maps to a tiny positive double and then to 0.  Refused
+// values get the poison mark.
+NPBGB_FX_FN int64_t from_f64_f59_cvt(double x) {
+  const uint64_t b = bits_of(x);
+  const uint32_t hi = static_cast<uint32_t>(b >> 32);
+  const bool ok = ((hi >> 20) - 1016u <= 6u) || b == 0;
+#if defined(__CUDA_ARCH__)
+  const int64_t v = __double2ll_rz(double_of(b + (static_cast<uint64_t>(59) << 52)));
+#else
+  const int64_t v = static_cast<int64_t>(double_of(b + (static_cast<uint64_t>(59) << 52)));
+#endif
+  return ok ? v : static_cast<int64_t>(static_cast<uint64_t>(kPoisonHi) << 32);
+}
+
+// Frame-F integer (53 significant bits) -> double via the binary64 conversion
+// path: the integer converts exactly, then the exponent drops by F.
+template <int F>
+NPBGB_FX_FN double to_f64_cvt(int64_t w) {
+#if defined(__CUDA_ARCH__)
+  const double d = __ll2double_rn(w);
+#else
+  const double d = static_cast<double>(w);
+#endif
+  const uint64_t b = bits_of(d) - (static_cast<uint64_t>(F) << 52);
+  return w == 0 ? 0.0 : double_of(b);
+}
+
 // Frame-F integer (already rounded to 53 significant bits, |w| < 2^63) -> double.
 template <int F>
 NPBGB_FX_FN double to_f64(int64_t w) {

@@ -33,6 +33,9 @@ namespace npbgb {
 extern int64_t g_cfg_f64_emulation;
 extern int64_t g_cfg_heat_chunk;
 extern int64_t g_cfg_heat_tma;
+extern int64_t g_cfg_heat_rows;
+extern int64_t g_cfg_heat_hw_rows;
+extern int64_t g_cfg_f64_cvt;
 
 namespace {
 
@@ -86,10 +89,28 @@ __device__ __forceinline__ T eval_point(S c, S ip, S im, S jp, S jm, S kp, S km,
 // ---------------------------------------------------------------------------
 // TMA pipeline
 // ---------------------------------------------------------------------------
-template <typename T>
+// Fixed-point point update with its 64-bit adds on the multiply-add pipe.
+template <bool CVT>
+__device__ __forceinline__ double heat_point_fxm(int64_t c, int64_t ip, int64_t im, int64_t jp,
+                                                 int64_t jm, int64_t kp, int64_t km, uint32_t one) {
+  using fx::add64;
+  using fx::round53m;
+  const int64_t nc2 = -2 * c;
+  const int64_t s0 = round53m(add64(round53m(add64(ip, nc2, one), one), im, one), one);
+  const int64_t s1 = round53m(add64(round53m(add64(jp, nc2, one), one), jm, one), one);
+  const int64_t s2 = round53m(add64(round53m(add64(kp, nc2, one), one), km, one), one);
+  const int64_t u = round53m(add64(s0, s1, one), one);
+  const int64_t v = round53m(add64(u, s2, one), one);
+  const int64_t w = round53m(add64(v, c * 8, one), one);
+  if constexpr (CVT) return fx::to_f64_cvt<62>(w);
+  return fx::to_f64<62>(w);
+}
+
+template <typename T, int R>
 struct TmaGeom {
   static constexpr int BX = sizeof(T) == 8 ? 34 : 36;  // rows of a 16-byte multiple
-  static constexpr int BY = kTJ + 2;
+  static constexpr int TJ = kTJ * R;                   // tile rows (axis 1)
+  static constexpr int BY = TJ + 2;
   static constexpr int kElems = BX * BY;
   static constexpr int kBytes = kElems * int(sizeof(T));
   static constexpr int kStride = (kBytes + 127) / 128 * 128;  // stage pitch, 128-byte aligned
@@ -97,21 +118,25 @@ struct TmaGeom {
 
 constexpr int kStages = 8;
 
-template <typename T, bool FX>
+// R: tile rows per thread.  FX: binary64 in fixed point.  CVT: fixed-point
+// conversions through the binary64 conversion path.  hw_rows: the last
+// hw_rows tile rows are evaluated with hardware binary64 (from global memory)
+// so that the binary64 pipe works alongside the integer pipe.  one == 1.
+template <typename T, bool FX, int R, bool CVT>
 __global__ void __launch_bounds__(kThreads)
 heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ src,
-           T* __restrict__ dst, int64_t n0, int64_t n1, int64_t n2, int chunk) {
-  using G = TmaGeom<T>;
+           T* __restrict__ dst, int64_t n0, int64_t n1, int64_t n2, int chunk, int hw_rows,
+           uint32_t one) {
+  using G = TmaGeom<T, R>;
   using S = typename std::conditional<FX, int64_t, T>::type;
-  static_assert(sizeof(S) == sizeof(T) || FX, "in-place conversion keeps the element size");
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kStages * G::kStride);
 
   const int tid = threadIdx.x;
   const int tx = tid & 31, ty = tid >> 5;
-  const int64_t k0 = 1 + int64_t(blockIdx.x) * kTK, j0 = 1 + int64_t(blockIdx.y) * kTJ;
-  const int64_t k = k0 + tx, j = j0 + ty;
-  const bool active = k < n2 - 1 && j < n1 - 1;
+  const int64_t k0 = 1 + int64_t(blockIdx.x) * kTK, j0 = 1 + int64_t(blockIdx.y) * G::TJ;
+  const int64_t k = k0 + tx;
+  const bool k_ok = k < n2 - 1;
   const int64_t s0 = n1 * n2, s1 = n2;
   const int64_t ib = 1 + int64_t(blockIdx.z) * chunk;
   const int64_t ie = (ib + chunk < n0 - 1) ? ib + chunk : n0 - 1;
@@ -136,7 +161,8 @@ heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ sr
       unsigned char* base = smem + (q % kStages) * G::kStride;
       for (int e = tid; e < G::kElems; e += kThreads) {
         const double v = reinterpret_cast<const double*>(base)[e];
-        reinterpret_cast<int64_t*>(base)[e] = to_fx(v);
+        reinterpret_cast<int64_t*>(base)[e] =
+            CVT ? fx::from_f64_f59_cvt(v) : fx::from_f64_f59_or_poison(v);
       }
     }
   };
@@ -155,7 +181,6 @@ heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ sr
   ok = ok && wait(1);
   if (ok) convert(1);
 
-  const int off = (ty + 1) * G::BX + (tx + 1);
   for (int m = 0; m < M; ++m) {
     ok = ok && wait(m + 2);
     if (ok) convert(m + 2);
@@ -165,14 +190,37 @@ heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ sr
       return;
     }
     if (tid == 0 && m - 1 + kStages < Q) issue(m - 1 + kStages);  // refills the buffer of plane m-1
-    if (active) {
+    const int64_t i = ib + m;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int row = ty + kTJ * r;
+      const int64_t j = j0 + row;
+      if (!k_ok || j >= n1 - 1) continue;
+      const int off = (row + 1) * G::BX + (tx + 1);
       const S* pm = stage_ptr(m) + off;
       const S* pc = stage_ptr(m + 1) + off;
       const S* pp = stage_ptr(m + 2) + off;
-      const int64_t i = ib + m;
-      const T* q = src + i * s0 + j * s1 + k;
-      dst[i * s0 + j * s1 + k] = eval_point<T, FX>(pc[0], pp[0], pm[0], pc[G::BX], pc[-G::BX],
-                                                   pc[1], pc[-1], q, s0, s1);
+      const int64_t g = i * s0 + j * s1 + k;
+      const T* q = src + g;
+      T out;
+      if constexpr (FX) {
+        const bool hw = row >= G::TJ - hw_rows;  // warp-uniform
+        if (hw) {
+          out = heat_point<T>(q[0], q[s0], q[-s0], q[s1], q[-s1], q[1], q[-1]);
+        } else {
+          const int64_t c = pc[0], ip = pp[0], im = pm[0], jp = pc[G::BX], jm = pc[-G::BX],
+                        kp = pc[1], km = pc[-1];
+          const uint32_t tag =
+              hi32(c) | hi32(ip) | hi32(im) | hi32(jp) | hi32(jm) | hi32(kp) | hi32(km);
+          if (!(tag & kPoisonHi))
+            out = heat_point_fxm<CVT>(c, ip, im, jp, jm, kp, km, one);
+          else
+            out = heat_point<T>(q[0], q[s0], q[-s0], q[s1], q[-s1], q[1], q[-1]);
+        }
+      } else {
+        out = heat_point<T>(pc[0], pp[0], pm[0], pc[G::BX], pc[-G::BX], pc[1], pc[-1]);
+      }
+      dst[g] = out;
     }
   }
 }
@@ -241,13 +289,6 @@ heat3d_ldg(const T* __restrict__ src, T* __restrict__ dst, int64_t n0, int64_t n
   }
 }
 
-struct Plan {
-  bool tma = false;
-  int chunk = 0;
-  dim3 grid, block;
-  size_t smem = 0;
-};
-
 int auto_chunk(int64_t n0, int64_t tiles, int ctas_per_sm) {
   // Smallest number of axis-0 chunks that fills about two waves of CTAs.
   const int64_t slots = int64_t(sm_count()) * (ctas_per_sm > 0 ? ctas_per_sm : 1);
@@ -259,49 +300,78 @@ int auto_chunk(int64_t n0, int64_t tiles, int ctas_per_sm) {
   return int(c);
 }
 
-template <typename T, bool FX>
-int32_t run(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps, cudaStream_t st) {
-  if (tsteps <= 1 || n0 < 3 || n1 < 3 || n2 < 3) return NPBGB_OK;
-  const int64_t gx = cdiv(n2 - 2, kTK), gy = cdiv(n1 - 2, kTJ);
-  using G = TmaGeom<T>;
+template <typename T, bool FX, int R, bool CVT>
+int32_t launch_tma(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps, cudaStream_t st) {
+  using G = TmaGeom<T, R>;
   const size_t smem = size_t(kStages) * G::kStride + kStages * sizeof(uint64_t);
   CUtensorMap map_a, map_b;
-  bool use_tma = g_cfg_heat_tma != 0;
-  if (use_tma) {
-    const uint64_t dims[3] = {uint64_t(n2), uint64_t(n1), uint64_t(n0)};
-    const uint32_t box[3] = {uint32_t(G::BX), uint32_t(G::BY), 1u};
-    use_tma = tma::encode_3d(&map_a, sizeof(T), a, dims, box) == cudaSuccess &&
-              tma::encode_3d(&map_b, sizeof(T), b, dims, box) == cudaSuccess;
+  const uint64_t dims[3] = {uint64_t(n2), uint64_t(n1), uint64_t(n0)};
+  const uint32_t box[3] = {uint32_t(G::BX), uint32_t(G::BY), 1u};
+  if (tma::encode_3d(&map_a, sizeof(T), a, dims, box) != cudaSuccess ||
+      tma::encode_3d(&map_b, sizeof(T), b, dims, box) != cudaSuccess)
+    return NPBGB_ERR_STATE;  // caller falls back to plain staging
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(heat3d_tma<T, FX, R, CVT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return cuda_status(e, "heat3d: smem attribute");
+    attr_done = true;
   }
   int per_sm = 0;
-  if (use_tma) {
-    static bool attr_done[2][2] = {};
-    if (!attr_done[sizeof(T) == 8][FX]) {
-      cudaError_t e = cudaFuncSetAttribute(heat3d_tma<T, FX>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-      if (e != cudaSuccess) return cuda_status(e, "heat3d: smem attribute");
-      attr_done[sizeof(T) == 8][FX] = true;
-    }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heat3d_tma<T, FX>, kThreads, smem);
-  } else {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heat3d_ldg<T, FX>, kThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heat3d_tma<T, FX, R, CVT>, kThreads, smem);
+  const int64_t gx = cdiv(n2 - 2, kTK), gy = cdiv(n1 - 2, G::TJ);
+  const int chunk = g_cfg_heat_chunk > 0 ? int(g_cfg_heat_chunk) : auto_chunk(n0, gx * gy, per_sm);
+  const int64_t gz = cdiv(n0 - 2, chunk);
+  if (gy > 65535 || gz > 65535 || gx > 0x7fffffff)
+    return set_error(NPBGB_ERR_ARG, "heat3d: extent too large");
+  const dim3 grid{unsigned(gx), unsigned(gy), unsigned(gz)};
+  int hw = int(g_cfg_heat_hw_rows);
+  if (hw > G::TJ) hw = G::TJ;
+  for (int32_t t = 1; t < tsteps; ++t) {
+    heat3d_tma<T, FX, R, CVT><<<grid, kThreads, smem, st>>>(map_a, a, b, n0, n1, n2, chunk, hw, 1u);
+    heat3d_tma<T, FX, R, CVT><<<grid, kThreads, smem, st>>>(map_b, b, a, n0, n1, n2, chunk, hw, 1u);
   }
+  NPBGB_CHECK_LAUNCH("heat3d_tma");
+  return NPBGB_OK;
+}
+
+template <typename T, bool FX>
+int32_t launch_ldg(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps, cudaStream_t st) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heat3d_ldg<T, FX>, kThreads, 0);
+  const int64_t gx = cdiv(n2 - 2, kTK), gy = cdiv(n1 - 2, kTJ);
   const int chunk = g_cfg_heat_chunk > 0 ? int(g_cfg_heat_chunk) : auto_chunk(n0, gx * gy, per_sm);
   const int64_t gz = cdiv(n0 - 2, chunk);
   if (gy > 65535 || gz > 65535 || gx > 0x7fffffff)
     return set_error(NPBGB_ERR_ARG, "heat3d: extent too large");
   const dim3 grid{unsigned(gx), unsigned(gy), unsigned(gz)};
   for (int32_t t = 1; t < tsteps; ++t) {
-    if (use_tma) {
-      heat3d_tma<T, FX><<<grid, kThreads, smem, st>>>(map_a, a, b, n0, n1, n2, chunk);
-      heat3d_tma<T, FX><<<grid, kThreads, smem, st>>>(map_b, b, a, n0, n1, n2, chunk);
-    } else {
-      heat3d_ldg<T, FX><<<grid, kThreads, 0, st>>>(a, b, n0, n1, n2, chunk);
-      heat3d_ldg<T, FX><<<grid, kThreads, 0, st>>>(b, a, n0, n1, n2, chunk);
-    }
+    heat3d_ldg<T, FX><<<grid, kThreads, 0, st>>>(a, b, n0, n1, n2, chunk);
+    heat3d_ldg<T, FX><<<grid, kThreads, 0, st>>>(b, a, n0, n1, n2, chunk);
   }
-  NPBGB_CHECK_LAUNCH("heat3d");
+  NPBGB_CHECK_LAUNCH("heat3d_ldg");
   return NPBGB_OK;
+}
+
+template <typename T, bool FX>
+int32_t run(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps, cudaStream_t st) {
+  if (tsteps <= 1 || n0 < 3 || n1 < 3 || n2 < 3) return NPBGB_OK;
+  if (g_cfg_heat_tma) {
+    const int rows = int(g_cfg_heat_rows);
+    const bool cvt = g_cfg_f64_cvt != 0;
+    int32_t r;
+    if (rows >= 4)
+      r = cvt ? launch_tma<T, FX, 4, true>(a, b, n0, n1, n2, tsteps, st)
+              : launch_tma<T, FX, 4, false>(a, b, n0, n1, n2, tsteps, st);
+    else if (rows == 2)
+      r = cvt ? launch_tma<T, FX, 2, true>(a, b, n0, n1, n2, tsteps, st)
+              : launch_tma<T, FX, 2, false>(a, b, n0, n1, n2, tsteps, st);
+    else
+      r = cvt ? launch_tma<T, FX, 1, true>(a, b, n0, n1, n2, tsteps, st)
+              : launch_tma<T, FX, 1, false>(a, b, n0, n1, n2, tsteps, st);
+    if (r != NPBGB_ERR_STATE) return r;
+  }
+  return launch_ldg<T, FX>(a, b, n0, n1, n2, tsteps, st);
 }
 
 // One CTA waits, with a short limit, on an mbarrier that nothing completes;

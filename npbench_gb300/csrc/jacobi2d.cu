@@ -5,20 +5,16 @@
 // with w/e the column neighbours j-1/j+1 and s/n the row neighbours i+1/i-1.
 //
 // Kernel layout (one launch per half-sweep): every warp owns a strip of 32
-// columns (one per lane, the contiguous axis) and streams down a chunk of
-// rows, keeping rows i-1, i, i+1 of its own column in registers and taking
-// the w/e neighbours from the adjacent lanes with shuffles (lanes 0 and 31
-// also load the strip's halo columns).  Warps never wait on each other.
+// columns and streams down a chunk of rows (jacobi_core.cuh: rows i-1, i,
+// i+1 in registers, w/e neighbours by shuffle, kUnroll rows loaded ahead).
+// Warps never wait on each other.
 //
 // binary32 uses IEEE float operations.  binary64 runs its four additions
 // exactly in fixed point on the integer pipe (fx64.cuh) for every point whose
 // five inputs lie in [2^-7, 1) or are +0 (refused values carry a poison bit),
 // and uses hardware binary64 for any other point; the final product by 0.2 is
 // a hardware binary64 multiply.  Both paths give the IEEE result bit for bit.
-#include <type_traits>
-
-#include "fx64.cuh"
-#include "npbgb_common.cuh"
+#include "jacobi_core.cuh"
 
 namespace npbgb {
 
@@ -28,82 +24,19 @@ extern int64_t g_cfg_jacobi_chunk;
 namespace {
 
 constexpr int kWarps = 8;
+constexpr int kUnroll = 4;
 
-template <typename S>
-__device__ __forceinline__ S shfl_up1(S v) { return __shfl_up_sync(0xffffffffu, v, 1); }
-template <typename S>
-__device__ __forceinline__ S shfl_down1(S v) { return __shfl_down_sync(0xffffffffu, v, 1); }
-
+// Grid: x over groups of kWarps column strips, y over chunks of rows.
 template <typename T, bool FX>
 __global__ void __launch_bounds__(32 * kWarps)
-jacobi2d_strip(const T* __restrict__ src, T* __restrict__ dst, int64_t ny, int64_t nx, int chunk) {
-  using S = typename std::conditional<FX, int64_t, T>::type;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+jacobi2d_strip(const T* __restrict__ src, T* __restrict__ dst, int64_t ny, int64_t nx, int chunk,
+               uint32_t one) {
+  const int warp = threadIdx.x >> 5;
   const int64_t k0 = 1 + (int64_t(blockIdx.x) * kWarps + warp) * 32;
   if (k0 >= nx - 1) return;  // whole strip outside the interior (warp-uniform)
-  const int64_t j = k0 + lane;
-  const bool active_col = j < nx - 1;
-  const bool own_inb = j < nx;
   const int64_t ib = 1 + int64_t(blockIdx.y) * chunk;
   const int64_t ie = (ib + chunk < ny - 1) ? ib + chunk : ny - 1;
-  // Halo column: lane 0 reads k0-1, lane 31 reads k0+32 (when inside the array).
-  const int64_t hj = lane == 0 ? k0 - 1 : k0 + 32;
-  const bool has_halo = (lane == 0) || (lane == 31 && hj < nx);
-
-  auto load = [&](int64_t i, S& own, S& halo) {
-    const T* row = src + i * nx;
-    if (own_inb) {
-      const T v = row[j];
-      if constexpr (FX) own = fx::from_f64_f59_or_poison(v); else own = v;
-    }
-    if (has_halo) {
-      const T v = row[hj];
-      if constexpr (FX) halo = fx::from_f64_f59_or_poison(v); else halo = v;
-    }
-  };
-
-  S xp = S(0), xc = S(0), xn = S(0), hc = S(0), hn = S(0), hdummy = S(0);
-  load(ib - 1, xp, hdummy);
-  load(ib, xc, hc);
-  const T k02 = T(0.2);
-  for (int64_t i = ib; i < ie; ++i) {
-    load(i + 1, xn, hn);
-    // w/e of row i from the neighbouring lanes; the strip ends use the halo.
-    S w = shfl_up1(xc), e = shfl_down1(xc);
-    if (lane == 0) w = hc;
-    if (lane == 31) e = hc;
-    T out;
-    if constexpr (FX) {
-      using fx::hi32;
-      const uint32_t tag = hi32(xc) | hi32(w) | hi32(e) | hi32(xn) | hi32(xp);
-      if (!(tag & fx::kPoisonHi)) {
-        using fx::round53;
-        int64_t acc = round53(xc + w);
-        acc = round53(acc + e);
-        acc = round53(acc + xn);
-        acc = round53(acc + xp);
-        out = mul_rn(k02, fx::to_f64<59>(acc));
-      } else {
-        out = T(0);
-        if (active_col) {
-          const T* r = src + i * nx + j;
-          T acc = add_rn(r[0], r[-1]);
-          acc = add_rn(acc, r[1]);
-          acc = add_rn(acc, r[nx]);
-          acc = add_rn(acc, r[-nx]);
-          out = mul_rn(k02, acc);
-        }
-      }
-    } else {
-      T acc = add_rn(xc, w);
-      acc = add_rn(acc, e);
-      acc = add_rn(acc, xn);
-      acc = add_rn(acc, xp);
-      out = mul_rn(k02, acc);
-    }
-    if (active_col) dst[i * nx + j] = out;
-    xp = xc; xc = xn; hc = hn;
-  }
+  jcore::strip_rows<T, FX, false, kUnroll>(src, dst, nx, k0, ib, ie, one);
 }
 
 int pick_chunk(int64_t ny, int64_t col_blocks) {
@@ -126,8 +59,8 @@ int32_t run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st)
   if (gx > 0x7fffffff || gy > 65535) return set_error(NPBGB_ERR_ARG, "jacobi2d: extent too large");
   const dim3 grid{unsigned(gx), unsigned(gy)};
   for (int32_t t = 1; t < tsteps; ++t) {
-    jacobi2d_strip<T, FX><<<grid, 32 * kWarps, 0, st>>>(a, b, ny, nx, chunk);
-    jacobi2d_strip<T, FX><<<grid, 32 * kWarps, 0, st>>>(b, a, ny, nx, chunk);
+    jacobi2d_strip<T, FX><<<grid, 32 * kWarps, 0, st>>>(a, b, ny, nx, chunk, 1u);
+    jacobi2d_strip<T, FX><<<grid, 32 * kWarps, 0, st>>>(b, a, ny, nx, chunk, 1u);
   }
   NPBGB_CHECK_LAUNCH("jacobi2d_strip");
   return NPBGB_OK;

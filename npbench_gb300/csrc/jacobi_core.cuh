@@ -1,0 +1,134 @@
+// Warp-strip Jacobi-2D half-sweep shared by the single-grid and batched kernels.
+//
+// A warp owns 32 consecutive columns (one per lane, the contiguous axis) and
+// walks down rows [r0, r1).  Rows i-1, i, i+1 of the lane's column stay in
+// registers; the w/e neighbours come from the adjacent lanes by shuffle, and
+// lanes 0 and 31 also read the strip's halo columns.  Rows are loaded U at a
+// time ahead of use so that U independent loads per lane are in flight.
+//
+// Per point, in the reference's order (jacobi_2d_numpy.py:7-8):
+//   dst = 0.2 * ((((c + w) + e) + s) + n)
+// binary64 uses the exact fixed-point path (fx64.cuh) for points whose inputs
+// lie in [2^-7, 1) or are +0, hardware binary64 otherwise.
+#pragma once
+
+#include <type_traits>
+
+#include "fx64.cuh"
+#include "npbgb_common.cuh"
+
+namespace npbgb {
+namespace jcore {
+
+template <bool CG, typename T>
+__device__ __forceinline__ T ld(const T* p) {
+  if constexpr (CG) return __ldcg(p); else return *p;
+}
+template <bool CG, typename T>
+__device__ __forceinline__ void st(T* p, T v) {
+  if constexpr (CG) __stcg(p, v); else *p = v;
+}
+
+template <typename T, bool FX, bool CG>
+struct Strip {
+  using S = typename std::conditional<FX, int64_t, T>::type;
+  const T* src;
+  T* dst;
+  int64_t nx, j, hj;
+  bool active, own_inb, has_halo;
+  uint32_t one;
+
+  __device__ __forceinline__ Strip(const T* s, T* d, int64_t nx_, int64_t k0, uint32_t one_)
+      : src(s), dst(d), nx(nx_), one(one_) {
+    const int lane = threadIdx.x & 31;
+    j = k0 + lane;
+    active = j < nx - 1;
+    own_inb = j < nx;
+    hj = lane == 0 ? k0 - 1 : k0 + 32;
+    has_halo = (lane == 0) || (lane == 31 && hj < nx);
+  }
+
+  __device__ __forceinline__ void load(int64_t i, S& own, S& halo) const {
+    const T* row = src + i * nx;
+    if (own_inb) {
+      const T v = ld<CG>(row + j);
+      if constexpr (FX) own = fx::from_f64_f59_or_poison(v); else own = v;
+    }
+    if (has_halo) {
+      const T v = ld<CG>(row + hj);
+      if constexpr (FX) halo = fx::from_f64_f59_or_poison(v); else halo = v;
+    }
+  }
+
+  // Output row i from rows i-1 (xp), i (xc, halo hc) and i+1 (xn).
+  __device__ __forceinline__ void point(int64_t i, S xp, S xc, S xn, S hc) const {
+    const int lane = threadIdx.x & 31;
+    S w = __shfl_up_sync(0xffffffffu, xc, 1), e = __shfl_down_sync(0xffffffffu, xc, 1);
+    if (lane == 0) w = hc;
+    if (lane == 31) e = hc;
+    const T k02 = T(0.2);
+    T out;
+    if constexpr (FX) {
+      using fx::hi32;
+      const uint32_t tag = hi32(xc) | hi32(w) | hi32(e) | hi32(xn) | hi32(xp);
+      if (!(tag & fx::kPoisonHi)) {
+        int64_t acc = fx::round53m(fx::add64(xc, w, one), one);
+        acc = fx::round53m(fx::add64(acc, e, one), one);
+        acc = fx::round53m(fx::add64(acc, xn, one), one);
+        acc = fx::round53m(fx::add64(acc, xp, one), one);
+        out = mul_rn(k02, fx::to_f64<59>(acc));
+      } else {
+        out = T(0);
+        if (active) {
+          const T* r = src + i * nx + j;
+          T acc = add_rn(ld<CG>(r), ld<CG>(r - 1));
+          acc = add_rn(acc, ld<CG>(r + 1));
+          acc = add_rn(acc, ld<CG>(r + nx));
+          acc = add_rn(acc, ld<CG>(r - nx));
+          out = mul_rn(k02, acc);
+        }
+      }
+    } else {
+      T acc = add_rn(xc, w);
+      acc = add_rn(acc, e);
+      acc = add_rn(acc, xn);
+      acc = add_rn(acc, xp);
+      out = mul_rn(k02, acc);
+    }
+    if (active) st<CG>(dst + i * nx + j, out);
+  }
+};
+
+// One strip (columns k0 .. k0+31) over rows [r0, r1).  Warp-collective.
+template <typename T, bool FX, bool CG, int U>
+__device__ __forceinline__ void strip_rows(const T* src, T* dst, int64_t nx, int64_t k0, int64_t r0,
+                                           int64_t r1, uint32_t one) {
+  using St = Strip<T, FX, CG>;
+  using S = typename St::S;
+  const St s(src, dst, nx, k0, one);
+  S x[U + 2], h[U + 2];
+#pragma unroll
+  for (int u = 0; u < U + 2; ++u) { x[u] = S(0); h[u] = S(0); }
+  s.load(r0 - 1, x[0], h[0]);
+  s.load(r0, x[1], h[1]);
+  int64_t i = r0;
+  for (; i + U <= r1; i += U) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) s.load(i + 1 + u, x[2 + u], h[2 + u]);
+#pragma unroll
+    for (int u = 0; u < U; ++u) s.point(i + u, x[u], x[u + 1], x[u + 2], h[u + 1]);
+    x[0] = x[U];
+    x[1] = x[U + 1];
+    h[1] = h[U + 1];
+  }
+  for (; i < r1; ++i) {
+    s.load(i + 1, x[2], h[2]);
+    s.point(i, x[0], x[1], x[2], h[1]);
+    x[0] = x[1];
+    x[1] = x[2];
+    h[1] = h[2];
+  }
+}
+
+}  // namespace jcore
+}  // namespace npbgb

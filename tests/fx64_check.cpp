@@ -48,6 +48,10 @@ int main(int argc, char** argv) {
     const int64_t A = from_f64_f59(a, oka), B = from_f64_f59(b, okb);
     if (!oka || !okb) return fail("conversion rejected an in-range value", a, b, 0, 0);
     if (to_f64<59>(A) != a || bits(to_f64<59>(A)) != bits(a)) return fail("roundtrip", a, b, a, to_f64<59>(A));
+    if (from_f64_f59_cvt(a) != A) return fail("cvt conversion", a, b, a, 0);
+    if (to_f64_cvt<59>(A) != a || bits(to_f64_cvt<59>(A)) != bits(a)) return fail("cvt roundtrip", a, b, a, to_f64_cvt<59>(A));
+    if (round53m(A - 2 * B, 1u) != round53(A - 2 * B)) return fail("round53m", a, b, 0, 0);
+    if (add64(A, -2 * B, 1u) != A - 2 * B) return fail("add64", a, b, 0, 0);
     volatile double s = a + b, d = a - b, d2 = a - 2.0 * b;
     if (bits(to_f64<59>(round53(A + B))) != bits(s)) return fail("add", a, b, s, to_f64<59>(round53(A + B)));
     if (bits(to_f64<59>(round53(A - B))) != bits(d)) return fail("sub", a, b, d, to_f64<59>(round53(A - B)));
@@ -79,6 +83,7 @@ int main(int argc, char** argv) {
     const int64_t W = round53(round53(round53(S0 + S1) + S2) + X[0] * 8);
     const double got = to_f64<62>(W);
     if (bits(got) != bits(want)) return fail("heat", v[0], v[1], want, got);
+    if (bits(to_f64_cvt<62>(W)) != bits(want)) return fail("heat cvt", v[0], v[1], want, to_f64_cvt<62>(W));
     ++checks;
   }
   // Jacobi-2D sum (the 0.2 product stays a hardware multiply).
@@ -103,6 +108,8 @@ int main(int argc, char** argv) {
     bool ok;
     from_f64_f59(r, ok);
     if (ok) return fail("refuse", r, 0, 0, 0);
+    if (!(hi32(from_f64_f59_cvt(r)) & kPoisonHi)) return fail("refuse cvt", r, 0, 0, 0);
+    if (!(hi32(from_f64_f59_or_poison(r)) & kPoisonHi)) return fail("refuse poison", r, 0, 0, 0);
   }
   std::printf("OK %ld\n", checks);
   return 0;

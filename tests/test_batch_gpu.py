@@ -1,0 +1,98 @@
+"""Batched persistent launch == per-grid launches == the oracle, on the GPU."""
+import numpy as np
+import pytest
+
+from conftest import bits_equal, first_diff
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+from npbench_gb300 import _lib, stencils  # noqa: E402
+from npbench_gb300.batch import Batch  # noqa: E402
+from oracle import cref  # noqa: E402
+
+DEV = torch.device("cuda", 0)
+
+
+def _mixed_batch(n, seed, max_side=300, max_t=40):
+    rng = np.random.default_rng(seed)
+    grids = []
+    for g in range(n):
+        ny, nx = (int(x) for x in np.exp(rng.uniform(np.log(3), np.log(max_side), 2)).round())
+        dt = np.float32 if g % 2 else np.float64
+        T = int(rng.integers(0, max_t))
+        A = rng.random((ny, nx)).astype(dt)
+        B = rng.random((ny, nx)).astype(dt)
+        grids.append((A, B, T))
+    return grids
+
+
+@pytest.mark.parametrize("band_rows", [0, 1, 7, 64])
+def test_batch_matches_oracle_and_single_launches(band_rows):
+    grids = _mixed_batch(40, seed=band_rows)
+    dev = [(torch.from_numpy(A).to(DEV), torch.from_numpy(B).to(DEV), T) for A, B, T in grids]
+    with Batch(dev, band_rows=band_rows) as b:
+        info = b.info()
+        assert info["ctas"] >= 1
+        b.launch()
+        _lib.device_status()
+    for n, ((A, B, T), (dA, dB, _)) in enumerate(zip(grids, dev)):
+        ra, rb = A.copy(), B.copy()
+        cref.jacobi_2d_kernel(T, ra, rb)
+        assert bits_equal(dA.cpu().numpy(), ra), (n, A.shape, A.dtype, T, first_diff(dA.cpu().numpy(), ra))
+        assert bits_equal(dB.cpu().numpy(), rb), (n, A.shape, A.dtype, T)
+        sA, sB = torch.from_numpy(A).to(DEV), torch.from_numpy(B).to(DEV)
+        stencils.jacobi_2d_kernel(T, sA, sB)
+        assert torch.equal(sA, dA) and torch.equal(sB, dB), n
+
+
+def test_batch_graph_replay_is_repeatable():
+    grids = _mixed_batch(25, seed=99, max_side=500, max_t=30)
+    init = [(torch.from_numpy(A).to(DEV), torch.from_numpy(B).to(DEV), T) for A, B, T in grids]
+    work = [(a.clone(), b.clone(), T) for a, b, T in init]
+    results = []
+    with Batch(work) as b:
+        for rep in range(3):
+            for (a0, b0, _), (a, bb, _) in zip(init, work):
+                a.copy_(a0)
+                bb.copy_(b0)
+            b.launch(graph=True)
+            _lib.device_status()
+            results.append([(a.clone(), bb.clone()) for a, bb, _ in work])
+    for rep in (1, 2):
+        for (a1, b1), (a2, b2) in zip(results[0], results[rep]):
+            assert torch.equal(a1, a2) and torch.equal(b1, b2)
+    for (A, B, T), (a, bb) in zip(grids, results[0]):
+        ra, rb = A.copy(), B.copy()
+        cref.jacobi_2d_kernel(T, ra, rb)
+        assert bits_equal(a.cpu().numpy(), ra) and bits_equal(bb.cpu().numpy(), rb)
+
+
+def test_batch_f64_emulation_off_matches():
+    grids = _mixed_batch(12, seed=5)
+    dev = [(torch.from_numpy(A).to(DEV), torch.from_numpy(B).to(DEV), T) for A, B, T in grids]
+    old = _lib.set_config(_lib.NPBGB_CFG_F64_EMULATION, 0)
+    try:
+        with Batch(dev) as b:
+            b.launch()
+            _lib.device_status()
+    finally:
+        _lib.set_config(_lib.NPBGB_CFG_F64_EMULATION, old)
+    for (A, B, T), (dA, dB, _) in zip(grids, dev):
+        ra, rb = A.copy(), B.copy()
+        cref.jacobi_2d_kernel(T, ra, rb)
+        assert bits_equal(dA.cpu().numpy(), ra) and bits_equal(dB.cpu().numpy(), rb)
+
+
+def test_empty_and_trivial_batches():
+    with Batch([]) as b:
+        b.launch()
+    A = torch.rand(2, 9, dtype=torch.float64, device=DEV)
+    B = torch.rand(2, 9, dtype=torch.float64, device=DEV)
+    a0 = A.clone()
+    with Batch([(A, B, 50)]) as b:  # no interior: nothing to do, as in the reference
+        b.launch()
+        assert b.info()["bands"] == 0
+    assert torch.equal(A, a0)

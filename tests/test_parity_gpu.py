@@ -334,3 +334,29 @@ def test_bounded_device_wait_reports_timeout_and_context_survives():
     stencils.jacobi_2d_kernel(3, dA, dB)
     cref.jacobi_2d_kernel(3, A, B)
     assert bits_equal(_host(dA), A)
+
+
+@pytest.mark.parametrize("rows,cvt,hw", [(1, 0, 0), (2, 0, 0), (2, 1, 0), (4, 1, 3), (2, 0, 4),
+                                         (4, 0, 32)])
+def test_heat_kernel_variants_bit_exact(rows, cvt, hw):
+    """Every heat3d variant (rows per thread, conversion path, hardware rows) gives the oracle's bits."""
+    from npbench_gb300 import _lib
+    keys = (_lib.NPBGB_CFG_HEAT_ROWS, _lib.NPBGB_CFG_F64_CVT, _lib.NPBGB_CFG_HEAT_HW_ROWS)
+    old = [_lib.set_config(k, v) for k, v in zip(keys, (rows, cvt, hw))]
+    try:
+        for dtype in (np.float64, np.float32):
+            for field in ("uniform", "mixed"):
+                shape = (34, 70, 100)
+                A = (workloads.uniform_heat(shape, dtype, seed=rows)[0] if field == "uniform"
+                     else _mixed_range_field(shape, 50 + rows).astype(dtype))
+                ra, rb = A.copy(), A.copy()
+                cref.heat_3d_kernel(5, ra, rb)
+                dA, dB = _dev(A), _dev(A)
+                stencils.heat_3d_kernel(5, dA, dB)
+                _lib.device_status()
+                assert bits_equal(_host(dA), ra), (rows, cvt, hw, dtype, field,
+                                                   first_diff(_host(dA), ra))
+                assert bits_equal(_host(dB), rb)
+    finally:
+        for k, v in zip(keys, old):
+            _lib.set_config(k, v)
