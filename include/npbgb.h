@@ -152,6 +152,26 @@ NPBGB_API int32_t npbgb_batch_info(const npbgb_batch* batch, int64_t* nbands, in
                                    int64_t* updates);
 NPBGB_API int32_t npbgb_batch_destroy(npbgb_batch* batch);
 
+/* Runs a batch like npbgb_batch_create + npbgb_batch_launch, for callers that
+ * must not allocate device memory: a host whose pool or HBM budget owns every
+ * byte of the GPU (an allocation behind its back breaks its accounting or
+ * fails against a full pool), or a loop that cannot take the implicit device
+ * synchronisation of cudaMalloc/cudaFree.  No counterpart in the reference.
+ *
+ * Nothing on this path allocates.  The band table, CTA lists and step counters
+ * live in one fixed file-scope __device__ array of about 1.9 MB, which every
+ * GPU that loads the library holds until exit.  A call may plan at most 32768
+ * bands (NPBGB_ERR_NOMEM beyond, before any GPU work).  The first call on a
+ * device looks up that array's address (cudaGetSymbolAddress) with the device
+ * current; make that first call before any stream capture.  Every call shares
+ * the array and the counters are cleared each call, so calls whose work
+ * overlaps on the GPU (for example on two streams) race; calls on one stream
+ * are ordered.  The plan is copied from host memory with cudaMemcpyAsync, so
+ * the call returns once the plan is staged.  Results are bit-identical to
+ * npbgb_batch_create + npbgb_batch_launch. */
+NPBGB_API int32_t npbgb_batch_run_noalloc(const npbgb_grid* grids, int64_t count,
+                                          int32_t band_rows, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

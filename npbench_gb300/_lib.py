@@ -54,6 +54,7 @@ SIGNATURES = {
     "npbgb_batch_info": (_i32, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64),
                                  ctypes.POINTER(_i64)]),
     "npbgb_batch_destroy": (_i32, [_vp]),
+    "npbgb_batch_run_noalloc": (_i32, [ctypes.POINTER(Grid), _i64, _i32, _vp]),
     "npbgb_jacobi2d": (_i32, [_vp, _vp, _i64, _i64, _i32, _i32, _vp]),
     "npbgb_heat3d": (_i32, [_vp, _vp, _i64, _i64, _i64, _i32, _i32, _vp]),
     "npbgb_hdiff": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i32, _vp]),

@@ -21,8 +21,10 @@
 // binary64 path.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <queue>
+#include <utility>
 #include <vector>
 
 #include "jacobi_core.cuh"
@@ -353,3 +355,176 @@ int32_t npbgb_batch_destroy(npbgb_batch* b) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches without allocation
+// ---------------------------------------------------------------------------
+// npbgb_batch_run_noalloc serves callers that must not allocate device
+// memory: for example a host that owns every byte of the GPU through its own
+// pool or an HBM admission budget, where a cudaMalloc behind its back would
+// break the accounting or fail against a full pool, or a loop that cannot
+// afford the implicit device synchronisation of cudaMalloc/cudaFree.  It runs
+// the same persistent batch kernel, but its band table, CTA lists and step
+// counters live in one file-scope __device__ array of fixed size instead of
+// memory from cudaMalloc.  Nothing on its path allocates: host-side planning
+// uses fixed static buffers, and the plan reaches the device by copies into
+// that array.
+namespace {
+
+constexpr int kNoAllocMaxBands = 32768;  // bands per call (about 1.9 MB of scratch)
+constexpr int kNoAllocMaxCtas = 2048;
+
+struct NoAllocLayout {
+  npbgb::BandDesc bands[kNoAllocMaxBands];
+  uint32_t done[kNoAllocMaxBands];
+  int32_t cta_off[kNoAllocMaxCtas + 1];
+  int32_t cta_bands[kNoAllocMaxBands];
+};
+
+// Device scratch shared by every call on a device; it keeps the last call's
+// contents.  In host code this name is only a stand-in for the symbol, not a
+// device address: npbgb_batch_run_noalloc looks the address up with
+// cudaGetSymbolAddress once per device and passes that pointer to the kernel.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocLayout)];
+
+struct NoAllocDevice {
+  NoAllocLayout* scratch = nullptr;  // device address of g_noalloc_scratch
+  int slots = 0;                     // co-resident CTAs of batch_persistent
+};
+constexpr int kNoAllocMaxDevices = 64;
+NoAllocDevice g_noalloc_devices[kNoAllocMaxDevices];
+std::mutex g_noalloc_mutex;
+
+// Host staging for the plan (static: the call allocates nothing).
+npbgb::BandDesc g_na_bands[kNoAllocMaxBands];
+double g_na_work[kNoAllocMaxBands];
+int32_t g_na_order[kNoAllocMaxBands];
+int32_t g_na_cta_of[kNoAllocMaxBands];
+int32_t g_na_cta_bands[kNoAllocMaxBands];
+int32_t g_na_cta_off[kNoAllocMaxCtas + 1];
+int32_t g_na_fill[kNoAllocMaxCtas];
+std::pair<double, int32_t> g_na_heap[kNoAllocMaxCtas];
+
+}  // namespace
+
+extern "C" int32_t npbgb_batch_run_noalloc(const npbgb_grid* grids, int64_t count, int32_t band_rows,
+                                           void* stream) {
+  using namespace npbgb;
+  if (count < 0 || (count > 0 && !grids)) return set_error(NPBGB_ERR_ARG, "batch(no-alloc): bad grid list");
+  if (band_rows < 0) return set_error(NPBGB_ERR_ARG, "batch(no-alloc): band_rows < 0");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+
+  // Plan the bands exactly as npbgb_batch_create does, into static buffers.
+  int nb = 0;
+  for (int64_t g = 0; g < count; ++g) {
+    const npbgb_grid& G = grids[g];
+    if (G.kind != NPBGB_KIND_JACOBI2D)
+      return set_error(NPBGB_ERR_ARG, "batch(no-alloc): grid %lld: only jacobi2d grids", (long long)g);
+    if (G.dtype != NPBGB_F64 && G.dtype != NPBGB_F32)
+      return set_error(NPBGB_ERR_DTYPE, "batch(no-alloc): grid %lld: dtype %d", (long long)g, G.dtype);
+    if (G.n0 < 0 || G.n1 < 0 || G.n0 > 0x7fffffff || G.n1 > 0x7fffffff)
+      return set_error(NPBGB_ERR_ARG, "batch(no-alloc): grid %lld: bad extents", (long long)g);
+    if (G.tsteps <= 1 || G.n0 < 3 || G.n1 < 3) continue;
+    if (!G.a || !G.b || G.a == G.b)
+      return set_error(NPBGB_ERR_ARG, "batch(no-alloc): grid %lld: null or aliased arrays", (long long)g);
+    const int ny = int(G.n0), nx = int(G.n1);
+    const int h = G.band_rows > 0 ? G.band_rows : (band_rows > 0 ? band_rows : 32);
+    const int64_t bands_here = cdiv(ny - 2, h);
+    if (int64_t(nb) + bands_here > kNoAllocMaxBands)
+      return set_error(NPBGB_ERR_NOMEM,
+                       "batch(no-alloc): more than %d bands (its fixed scratch capacity); use "
+                       "larger band_rows, fewer grids, or npbgb_batch_create",
+                       kNoAllocMaxBands);
+    const int first = nb;
+    for (int q = 0; q < int(bands_here); ++q) {
+      BandDesc& d = g_na_bands[nb];
+      d.a = G.a;
+      d.b = G.b;
+      d.ny = ny;
+      d.nx = nx;
+      d.r0 = 1 + q * h;
+      d.r1 = std::min(1 + (q + 1) * h, ny - 1);
+      d.steps = 2 * (G.tsteps - 1);
+      d.dtype = G.dtype;
+      d.left = q > 0 ? first + q - 1 : -1;
+      d.right = q + 1 < int(bands_here) ? first + q + 1 : -1;
+      g_na_work[nb] = double(d.r1 - d.r0) * double(nx - 2) * d.steps * (d.dtype == NPBGB_F64 ? 2.0 : 1.0);
+      g_na_order[nb] = nb;
+      ++nb;
+    }
+  }
+  if (nb == 0) return NPBGB_OK;
+
+  // Once per device, with that device current: the scratch symbol's address.
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e, "batch(no-alloc): current device");
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return set_error(NPBGB_ERR_ARG, "batch(no-alloc): device %d", dev);
+  NoAllocDevice& D = g_noalloc_devices[dev];
+  if (!D.scratch) {
+    void* ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_status(e, "batch(no-alloc): cudaGetSymbolAddress");
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_persistent, kBThreads, 0);
+    if (e != cudaSuccess) return cuda_status(e, "batch(no-alloc): occupancy");
+    D.slots = std::max(1, per_sm) * sm_count();
+    D.scratch = static_cast<NoAllocLayout*>(ptr);
+  }
+
+  // Longest-processing-time greedy assignment, as npbgb_batch_create.
+  const int nctas = std::max(1, std::min({D.slots, nb, kNoAllocMaxCtas}));
+  std::sort(g_na_order, g_na_order + nb, [](int32_t x, int32_t y) {
+    return g_na_work[x] > g_na_work[y] || (g_na_work[x] == g_na_work[y] && x < y);
+  });
+  auto later = [](const std::pair<double, int32_t>& x, const std::pair<double, int32_t>& y) { return x > y; };
+  for (int c = 0; c < nctas; ++c) g_na_heap[c] = {0.0, c};
+  std::make_heap(g_na_heap, g_na_heap + nctas, later);
+  for (int c = 0; c < nctas; ++c) g_na_fill[c] = 0;
+  for (int n = 0; n < nb; ++n) {
+    const int32_t band = g_na_order[n];
+    std::pop_heap(g_na_heap, g_na_heap + nctas, later);
+    std::pair<double, int32_t>& top = g_na_heap[nctas - 1];
+    g_na_cta_of[band] = top.second;
+    ++g_na_fill[top.second];
+    top.first += g_na_work[band];
+    std::push_heap(g_na_heap, g_na_heap + nctas, later);
+  }
+  g_na_cta_off[0] = 0;
+  for (int c = 0; c < nctas; ++c) {
+    g_na_cta_off[c + 1] = g_na_cta_off[c] + g_na_fill[c];
+    g_na_fill[c] = g_na_cta_off[c];
+  }
+  for (int n = 0; n < nb; ++n) {
+    const int32_t band = g_na_order[n];
+    g_na_cta_bands[g_na_fill[g_na_cta_of[band]]++] = band;
+  }
+
+  // Upload the plan, clear the counters (they must start at zero), launch.
+  cudaStream_t st = as_stream(stream);
+  NoAllocLayout* S = D.scratch;
+  if ((e = cudaMemcpyAsync(S->bands, g_na_bands, sizeof(BandDesc) * size_t(nb), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(S->cta_off, g_na_cta_off, sizeof(int32_t) * size_t(nctas + 1), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(S->cta_bands, g_na_cta_bands, sizeof(int32_t) * size_t(nb), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+      (e = cudaMemsetAsync(S->done, 0, sizeof(uint32_t) * size_t(nb), st)) != cudaSuccess)
+    return cuda_status(e, "batch(no-alloc): upload plan");
+  const BandDesc* d_bands = S->bands;
+  uint32_t* d_done = S->done;
+  const int32_t* d_cta_off = S->cta_off;
+  const int32_t* d_cta_bands = S->cta_bands;
+  int f64_emul = int(g_cfg_f64_emulation);
+  uint32_t one = 1;
+  void* args[] = {&d_bands, &d_done, &d_cta_off, &d_cta_bands, &f64_emul, &one};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(unsigned(nctas));
+  cfg.blockDim = dim3(kBThreads);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(batch_persistent), args);
+  if (e != cudaSuccess) return cuda_status(e, "batch(no-alloc): cooperative launch");
+  return NPBGB_OK;
+}
