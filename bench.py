@@ -58,6 +58,18 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--workload", default="heat3d",
+                    choices=["heat3d", "jacobi2d", "hdiff", "batch", "serve"],
+                    help="heat3d (default): Heat-3D 256^3; jacobi2d: Jacobi-2D 1000^2 float64, "
+                         "TSTEPS=100; hdiff: 256x256x160 float64, one call per step; batch: "
+                         "4096 mixed Jacobi-2D grids in one persistent launch; serve: "
+                         "Poisson-arrival mixed solves through the continuous-batching server")
+    ap.add_argument("--batch-grids", type=int, default=4096)
+    ap.add_argument("--compare", action="store_true",
+                    help="batch/serve: also time the per-grid / sequential comparator")
+    ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--rate", type=float, default=1000.0)
+    ap.add_argument("--quantum", type=int, default=32)
     return ap.parse_args()
 
 
@@ -330,13 +342,230 @@ def run_gb300(args, world, rank, local):
         dist.destroy_process_group()
 
 
+def _timed_steps(torch, dev, stream, step, reset, steps, warmup, flush=None):
+    """Event time (ms) of `steps` calls of step(); reset() and flush() run untimed."""
+    for _ in range(warmup):
+        reset()
+        step()
+    torch.cuda.synchronize(dev)
+    ev = []
+    for _ in range(steps):
+        reset()
+        if flush is not None:
+            flush()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        ev.append((e0, e1))
+    torch.cuda.synchronize(dev)
+    return sum(a.elapsed_time(b) for a, b in ev)
+
+
+def _base_line(args, metric_value, ms_per_step, dtype, workload, extra_config, **kw):
+    line = {"metric": METRIC, "value": metric_value, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+            "data": "synthetic U[0,1), seeded",
+            "config": {"workload": workload, **extra_config}}
+    line.update(kw)
+    return line
+
+
+def run_jacobi2d(args):
+    """Jacobi-2D 1000^2 float64, TSTEPS=100 (16 MB: L2-resident, so L2 is flushed per step)."""
+    import torch
+    from npbench_gb300 import stencils, workloads
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    n, T = 1000, 100
+    A0, B0 = workloads.uniform_pair((n, n), np.float64, seed=0)
+    pA, pB = torch.from_numpy(A0).to(dev), torch.from_numpy(B0).to(dev)
+    A, B = torch.empty_like(pA), torch.empty_like(pB)
+    scrub = torch.empty(256 * 2**20 // 4, dtype=torch.float32, device=dev)
+
+    def reset():
+        A.copy_(pA)
+        B.copy_(pB)
+
+    with ClockSampler(0) as clk:
+        ms = _timed_steps(torch, dev, stream, lambda: stencils.jacobi_2d_kernel(T, A, B), reset,
+                          args.steps, args.warmup, flush=lambda: scrub.fill_(1.0))
+    hs = 2 * (T - 1)
+    ups = hs * (n - 2) ** 2
+    ms_step = ms / args.steps
+    peak, kind = measured_peaks()
+    ach = 16.0 * (n - 2) ** 2 / (ms_step / hs * 1e-3) / 1e9
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import stencils_np
+        a, b = A0.copy(), B0.copy()
+        t0 = time.perf_counter()
+        stencils_np.jacobi_2d_kernel(11, a, b)
+        dt = time.perf_counter() - t0
+        cpu = {"value": 20 * (n - 2) ** 2 / dt, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"TSTEPS=11 (20 half-sweeps) of the same grid, {dt:.2f} s"}
+    print(json.dumps(_base_line(
+        args, ups * args.steps / (ms * 1e-3), ms_step, "f64",
+        "jacobi_2d 1000^2 float64, TSTEPS=100 (198 half-sweeps)",
+        {"grid": [n, n], "TSTEPS": T, "l2": "16 MB grid is L2-resident; 256 MB scrub written "
+         "between timed steps"},
+        roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                  "peak_kind": kind, "traffic": ncu_traffic("jacobi2d_f64_1000"),
+                  "note": "inputs live in L2 within a step; frac may exceed what HBM alone allows"},
+        gpu_launches=hs * args.steps, clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
+
+
+def run_hdiff(args):
+    """hdiff 256x256x160 float64, one call per step (the harness repeats it)."""
+    import torch
+    from npbench_gb300 import stencils, workloads
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    I, J, K = 256, 256, 160
+    inf, out0, coeff = workloads.init_hdiff(I, J, K)
+    dIn, dOut, dC = (torch.from_numpy(x).to(dev) for x in (inf, out0, coeff))
+    scrub = torch.empty(256 * 2**20 // 4, dtype=torch.float32, device=dev)
+    with ClockSampler(0) as clk:
+        ms = _timed_steps(torch, dev, stream, lambda: stencils.hdiff(dIn, dOut, dC), lambda: None,
+                          args.steps, args.warmup, flush=lambda: scrub.fill_(1.0))
+    ms_step = ms / args.steps
+    pts = I * J * K
+    alg = 8.0 * ((I + 4) * (J + 4) * K + 2 * I * J * K)
+    peak, kind = measured_peaks()
+    ach = alg / (ms_step * 1e-3) / 1e9
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import stencils_np
+        o = out0.copy()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            stencils_np.hdiff(inf, o, coeff)
+        dt = (time.perf_counter() - t0) / 3
+        cpu = {"value": pts / dt, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"3 calls on the same 256x256x160 input, {dt:.2f} s each"}
+    print(json.dumps(_base_line(
+        args, pts * args.steps / (ms * 1e-3), ms_step, "f64",
+        "hdiff 256x256x160 float64 (reference initialize), one call per step",
+        {"shape": [I, J, K], "l2": "253 MB of inputs+output; 256 MB scrub between steps"},
+        unit_note="value counts output points per second",
+        roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                  "peak_kind": kind, "traffic": ncu_traffic("hdiff_f64_256"),
+                  "alg_bytes_per_launch": alg},
+        gpu_launches=args.steps, clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
+
+
+def run_batch(args):
+    """4096 independent Jacobi-2D grids (sides log-uniform in [64, 2048], half float32 and
+    half float64, TSTEPS uniform in [10, 500]) in one persistent launch per step."""
+    import torch
+    from npbench_gb300 import _lib, stencils, workloads
+    from npbench_gb300.batch import Batch
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    specs = workloads.batch_jacobi_specs(args.batch_grids, seed=0)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0)
+    init, work = [], []
+    for (ny, nx), dt, T in specs:
+        tdt = torch.float64 if dt == np.float64 else torch.float32
+        a = torch.rand((ny, nx), dtype=tdt, device=dev, generator=gen)
+        b = torch.rand((ny, nx), dtype=tdt, device=dev, generator=gen)
+        init.append((a, b))
+        work.append((a.clone(), b.clone(), T))
+
+    def reset():
+        for (a0, b0), (a, b, _) in zip(init, work):
+            a.copy_(a0)
+            b.copy_(b0)
+
+    ups = sum(2 * (T - 1) * (s[0] - 2) * (s[1] - 2) for s, _, T in specs)
+    alg = sum(2 * (T - 1) * (s[0] - 2) * (s[1] - 2) * 2 * np.dtype(dt).itemsize for s, dt, T in specs)
+    with Batch(work, band_rows=64) as batch:
+        info = batch.info()
+        with ClockSampler(0) as clk:
+            ms = _timed_steps(torch, dev, stream, lambda: batch.launch(graph=True), reset,
+                              args.steps, args.warmup)
+        _lib.device_status()
+    ms_step = ms / args.steps
+    peak, kind = measured_peaks()
+    ach = alg / (ms_step * 1e-3) / 1e9
+    comp = None
+    if args.compare:
+        def per_grid():
+            for a, b, T in work:
+                stencils.jacobi_2d_kernel(T, a, b)
+        ms_pg = _timed_steps(torch, dev, stream, per_grid, reset, 1, 0)
+        comp = {"per_grid_launches_updates_per_s": ups / (ms_pg * 1e-3),
+                "per_grid_ms": ms_pg, "batched_over_per_grid": ms_pg / ms_step,
+                "per_grid_kernel_launches": sum(2 * (T - 1) for _, _, T in specs)}
+    cells = sum(s[0] * s[1] for s, _, _ in specs)
+    print(json.dumps(_base_line(
+        args, ups * args.steps / (ms * 1e-3), ms_step, "f32+f64",
+        f"batched jacobi_2d: {args.batch_grids} grids, sides log-uniform [64, 2048], half "
+        f"float32 / half float64, TSTEPS uniform [10, 500]",
+        {"cells": cells, "updates_per_step": ups, "bands": info["bands"], "ctas": info["ctas"],
+         "band_rows": 64, "graph": True, "l2": f"{cells * 6 * 2 / 1e9:.1f} GB resident, "
+                                                "far above L2"},
+        roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                  "frac": ach / peak, "peak_kind": kind, "traffic": None},
+        comparator=comp, gpu_launches=args.steps, clocks=clk.summary())), flush=True)
+
+
+def run_serve(args):
+    """Poisson-arrival mixed solves through the continuous-batching server."""
+    import torch
+    from npbench_gb300 import workloads
+    from npbench_gb300.server import Request, StencilServer, latency_stats, run_sequential
+    arrivals, specs = workloads.served_requests(args.requests, args.rate, seed=0)
+
+    def make():
+        return [Request(shape=s, dtype=dt, tsteps=T, seed=sd, return_host=False)
+                for s, dt, T, sd in specs]
+
+    with StencilServer(quantum=args.quantum) as warm:
+        warm.submit(Request(shape=(64, 64), dtype=np.float32, tsteps=5, seed=1)).result()
+    reqs = make()
+    srv = StencilServer(quantum=args.quantum, hbm_budget_bytes=150e9).start()
+    t0 = time.perf_counter()
+    futs = []
+    with ClockSampler(0) as clk:
+        for r, at in zip(reqs, arrivals):
+            now = time.perf_counter() - t0
+            if at > now:
+                time.sleep(at - now)
+            futs.append(srv.submit(r))
+        for f in futs:
+            f.result()
+        srv.stop()
+    st = latency_stats(reqs)
+    comp = None
+    if args.compare:
+        seq = make()
+        run_sequential(seq, arrivals)
+        comp = latency_stats(seq)
+        comp["served_over_sequential_updates_per_s"] = st["updates_per_s"] / comp["updates_per_s"]
+    print(json.dumps(_base_line(
+        args, st["updates_per_s"], st["span_s"] * 1e3, "f32+f64",
+        f"served stream: {args.requests} requests, Poisson {args.rate:g} req/s, 2D Jacobi "
+        f"128^2-4096^2 and 3D heat 32^3-384^3 (log-uniform), 70% float32, TSTEPS 20-1000",
+        {"quantum_half_sweeps": args.quantum, "hbm_budget_gb": 150, "rounds": srv.rounds,
+         "peak_resident_gb": srv.admission.peak / 1e9},
+        latency={"p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"]},
+        comparator=comp, clocks=clk.summary())), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_info()
     if args.impl == "reference":
         run_reference(args, world, rank)
-    else:
+    elif args.workload == "heat3d":
         run_gb300(args, world, rank, local)
+    elif rank == 0:
+        {"jacobi2d": run_jacobi2d, "hdiff": run_hdiff, "batch": run_batch,
+         "serve": run_serve}[args.workload](args)
 
 
 if __name__ == "__main__":

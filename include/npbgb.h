@@ -53,9 +53,11 @@ extern "C" {
 #define NPBGB_CFG_HEAT_TMA 3      /* 1 (default): heat3d stages planes with TMA when the
                                      arrays allow it; 0: plain loads only */
 #define NPBGB_CFG_JACOBI_CHUNK 4  /* rows per warp in jacobi2d; 0 = automatic */
-#define NPBGB_CFG_HEAT_ROWS 5     /* axis-1 tile rows per thread in heat3d (TMA): 1, 2, 4 */
+#define NPBGB_CFG_HEAT_ROWS 5     /* axis-1 tile rows per thread in heat3d (TMA): 1, 2, 4;
+                                     0 (default) = 4 for binary32, 1 for binary64 */
 #define NPBGB_CFG_HEAT_HW_ROWS 6  /* heat3d binary64: tile rows per CTA evaluated with
-                                     hardware binary64 next to the fixed-point rows */
+                                     hardware binary64 next to the fixed-point rows;
+                                     -1 (default) = 2 */
 #define NPBGB_CFG_F64_CVT 7       /* 1: fixed-point conversions use the binary64
                                      convert instructions; 0: integer bit operations */
 
@@ -64,7 +66,12 @@ extern "C" {
 #define NPBGB_KIND_HEAT3D 1
 
 /* One grid of a batch: a ping-pong pair of device arrays and its own step
- * count.  For NPBGB_KIND_JACOBI2D the arrays are (n0, n1) and n2 is ignored. */
+ * count.  For NPBGB_KIND_JACOBI2D the arrays are (n0, n1) and n2 is ignored;
+ * for NPBGB_KIND_HEAT3D they are (n0, n1, n2).  A run may be split over
+ * several launches: step0 half-sweeps are taken as already applied (the
+ * first source is a for even step0, b for odd), and at most nsteps are
+ * performed (0 = all remaining), so consecutive launches with step0 advanced
+ * by what the previous one did reproduce the uninterrupted run bit for bit. */
 typedef struct npbgb_grid {
   void* a;           /* holds the field at step 0 and the newest field at the end */
   void* b;           /* second buffer (holds the previous field at the end) */
@@ -72,7 +79,10 @@ typedef struct npbgb_grid {
   int32_t kind;      /* NPBGB_KIND_* */
   int32_t dtype;     /* NPBGB_F64 or NPBGB_F32 */
   int32_t tsteps;    /* the reference's TSTEPS: 2*(tsteps-1) half-sweeps */
-  int32_t band_rows; /* rows per scheduling band; 0 = the batch default */
+  int32_t band_rows; /* axis-0 extent of a scheduling band; 0 = the batch default
+                        (32 rows for Jacobi-2D, 8 planes for Heat-3D) */
+  int32_t step0;     /* half-sweeps already applied (0 = start of the run) */
+  int32_t nsteps;    /* half-sweeps to perform now; 0 = all remaining */
 } npbgb_grid;
 
 typedef struct npbgb_batch npbgb_batch;
@@ -133,13 +143,15 @@ NPBGB_API int32_t npbgb_hdiff(const void* in_field, void* out_field, const void*
 
 /* Batches: many independent grids advanced by one persistent launch.
  *
- * npbgb_batch_create plans a batch: each grid is cut into bands of
- * band_rows rows (0 = 32, or the grid's own band_rows), bands are assigned
+ * npbgb_batch_create plans a batch of Jacobi-2D and Heat-3D grids: each grid
+ * is cut along axis 0 into bands (the grid's band_rows, else band_rows, else
+ * the kind's default), bands are assigned
  * to the CTAs of one cooperative launch with equal work per CTA, and the
  * plan (band table, per-band step counters) is stored in device memory
- * allocated here.  Each grid ends exactly as npbgb_jacobi2d would leave it
- * (bit-identical), i.e. as the reference's kernel(TSTEPS, A, B) per grid,
- * polybench/jacobi_2d/jacobi_2d_numpy.py:4-10.
+ * allocated here.  Each grid ends exactly as npbgb_jacobi2d / npbgb_heat3d
+ * would leave it (bit-identical), i.e. as the reference's kernel(TSTEPS, A, B)
+ * per grid, polybench/jacobi_2d/jacobi_2d_numpy.py:4-10 and
+ * polybench/heat_3d/heat_3d_numpy.py:4-20.
  * npbgb_batch_launch runs the whole batch: a counter reset and one
  * persistent kernel on `stream`; with use_graph != 0 the two are captured
  * once into a CUDA graph and replayed.  Bounded waits: a CTA that makes no
@@ -152,14 +164,14 @@ NPBGB_API int32_t npbgb_batch_info(const npbgb_batch* batch, int64_t* nbands, in
                                    int64_t* updates);
 NPBGB_API int32_t npbgb_batch_destroy(npbgb_batch* batch);
 
-/* Runs a batch like npbgb_batch_create + npbgb_batch_launch, for callers that
+/* Runs a batch of Jacobi-2D grids like npbgb_batch_create + npbgb_batch_launch, for callers that
  * must not allocate device memory: a host whose pool or HBM budget owns every
  * byte of the GPU (an allocation behind its back breaks its accounting or
  * fails against a full pool), or a loop that cannot take the implicit device
  * synchronisation of cudaMalloc/cudaFree.  No counterpart in the reference.
  *
  * Nothing on this path allocates.  The band table, CTA lists and step counters
- * live in one fixed file-scope __device__ array of about 1.9 MB, which every
+ * live in one fixed file-scope __device__ array of about 2.1 MB, which every
  * GPU that loads the library holds until exit.  A call may plan at most 32768
  * bands (NPBGB_ERR_NOMEM beyond, before any GPU work).  The first call on a
  * device looks up that array's address (cudaGetSymbolAddress) with the device

@@ -36,7 +36,8 @@ class Grid(ctypes.Structure):
     _fields_ = [("a", ctypes.c_void_p), ("b", ctypes.c_void_p), ("n0", ctypes.c_int64),
                 ("n1", ctypes.c_int64), ("n2", ctypes.c_int64), ("kind", ctypes.c_int32),
                 ("dtype", ctypes.c_int32), ("tsteps", ctypes.c_int32),
-                ("band_rows", ctypes.c_int32)]
+                ("band_rows", ctypes.c_int32), ("step0", ctypes.c_int32),
+                ("nsteps", ctypes.c_int32)]
 
 
 # Every symbol include/npbgb.h declares, with its ctypes signature.

@@ -1,13 +1,17 @@
-"""Many independent Jacobi-2D grids advanced by one persistent launch (libnpbgb batches).
+"""Many independent grids advanced by one persistent launch (libnpbgb batches).
 
     with Batch([(A0, B0, T0), (A1, B1, T1), ...]) as batch:
         batch.launch()              # one counter reset + one cooperative persistent kernel
         batch.launch(graph=True)    # the same, captured once into a CUDA graph and replayed
 
-Every (A, B, TSTEPS) is a pair of 2D CUDA tensors of one dtype (float32 or
-float64) and its own step count.  After a launch each pair holds what
-``kernel(TSTEPS, A, B)`` of polybench/jacobi_2d/jacobi_2d_numpy.py:4-10 leaves,
-bit for bit.  The tensors must stay alive while the batch is used.
+Every entry (A, B, TSTEPS) is a pair of CUDA tensors of one dtype (float32 or
+float64) with its own step count: 2D pairs are Jacobi-2D grids, 3D pairs
+Heat-3D grids.  After a launch each pair holds what ``kernel(TSTEPS, A, B)``
+of polybench/jacobi_2d/jacobi_2d_numpy.py:4-10 or
+polybench/heat_3d/heat_3d_numpy.py:4-20 leaves, bit for bit.  An entry
+(A, B, TSTEPS, step0, nsteps) resumes a run after step0 half-sweeps and
+performs at most nsteps (0 = all remaining).  The tensors must stay alive
+while the batch is used.
 """
 import ctypes
 
@@ -22,13 +26,15 @@ class Batch:
         import torch
         self._keep = []
         arr = (_lib.Grid * max(1, len(grids)))()
-        for n, (A, B, T) in enumerate(grids):
+        for n, entry in enumerate(grids):
+            A, B, T = entry[:3]
+            step0, nsteps = (entry[3], entry[4]) if len(entry) > 3 else (0, 0)
             if not (isinstance(A, torch.Tensor) and isinstance(B, torch.Tensor)):
                 raise TypeError("batch grids must be CUDA tensors")
             if A.device.type != "cuda" or B.device != A.device:
                 raise ValueError("batch grids must be on one CUDA device")
-            if A.dim() != 2 or A.shape != B.shape or A.dtype != B.dtype:
-                raise ValueError(f"grid {n}: A and B must be 2D with equal shape and dtype")
+            if A.dim() not in (2, 3) or A.shape != B.shape or A.dtype != B.dtype:
+                raise ValueError(f"grid {n}: A and B must be 2D or 3D with equal shape and dtype")
             if not (A.is_contiguous() and B.is_contiguous()):
                 raise ValueError(f"grid {n}: tensors must be contiguous")
             if A.dtype == torch.float64:
@@ -39,8 +45,13 @@ class Batch:
                 raise TypeError(f"grid {n}: unsupported dtype {A.dtype}")
             g = arr[n]
             g.a, g.b = A.data_ptr(), B.data_ptr()
-            g.n0, g.n1, g.n2 = A.shape[0], A.shape[1], 1
-            g.kind = _lib.NPBGB_KIND_JACOBI2D
+            if A.dim() == 2:
+                g.n0, g.n1, g.n2 = A.shape[0], A.shape[1], 1
+                g.kind = _lib.NPBGB_KIND_JACOBI2D
+            else:
+                g.n0, g.n1, g.n2 = A.shape
+                g.kind = _lib.NPBGB_KIND_HEAT3D
+            g.step0, g.nsteps = int(step0), int(nsteps)
             g.dtype = code
             g.tsteps = int(T)
             g.band_rows = int(band_rows_of(A)) if band_rows_of else 0

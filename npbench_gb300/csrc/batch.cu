@@ -27,6 +27,7 @@
 #include <utility>
 #include <vector>
 
+#include "heat_core.cuh"
 #include "jacobi_core.cuh"
 #include "npbgb_common.cuh"
 #include "tma.cuh"
@@ -44,12 +45,14 @@ constexpr uint64_t kBatchLimitNs = 2000000000ull;  // two seconds without progre
 struct BandDesc {
   void* a;          // array holding the field after an even number of half-sweeps
   void* b;          // the other array
-  int32_t ny, nx;   // grid extents
-  int32_t r0, r1;   // interior rows [r0, r1) of this band
-  int32_t steps;    // half-sweeps to perform: 2 * (TSTEPS - 1)
-  int32_t dtype;    // NPBGB_F64 / NPBGB_F32
-  int32_t left;     // band above (rows < r0) of the same grid, or -1
-  int32_t right;    // band below (rows >= r1), or -1
+  int32_t n0, n1, n2;  // grid extents (Jacobi-2D: n0 rows, n1 columns, n2 = 1)
+  int32_t r0, r1;   // interior range [r0, r1) of this band along axis 0
+  int32_t steps;    // half-sweeps to perform in this launch
+  int32_t step0;    // half-sweeps the grid has already had (parity of the first source)
+  int16_t dtype;    // NPBGB_F64 / NPBGB_F32
+  int16_t kind;     // NPBGB_KIND_JACOBI2D / NPBGB_KIND_HEAT3D
+  int32_t left;     // band before (axis-0 indices < r0) of the same grid, or -1
+  int32_t right;    // band after (indices >= r1), or -1
 };
 
 __device__ unsigned int g_batch_error;  // bit 0: a CTA made no progress for the limit
@@ -72,6 +75,21 @@ __device__ __noinline__ void band_half_sweep(const T* src, T* dst, int64_t nx, i
   const int warp = threadIdx.x >> 5;
   for (int64_t k0 = 1 + int64_t(warp) * 32; k0 < nx - 1; k0 += 32 * kBWarps)
     jcore::strip_rows<T, FX, true, 4>(src, dst, nx, k0, r0, r1, one);
+}
+
+// One half-sweep of Heat-3D planes [r0, r1): the CTA walks the plane's
+// 8 x 32 tiles and streams each along axis 0 (heat_core.cuh), through L2.
+template <typename T, bool FX>
+__device__ __noinline__ void heat_band_half_sweep(const T* src, T* dst, int64_t n1, int64_t n2,
+                                                  int r0, int r1) {
+  static_assert(hcore::kThreads == kBThreads, "tile streamer uses the whole CTA");
+  __shared__ hcore::PlaneBuf<T, FX> plane;
+  const int64_t tiles_j = (n1 - 2 + hcore::kTJ - 1) / hcore::kTJ;
+  const int64_t tiles_k = (n2 - 2 + hcore::kTK - 1) / hcore::kTK;
+  for (int64_t t = 0; t < tiles_j * tiles_k; ++t) {
+    const int64_t j0 = 1 + (t / tiles_k) * hcore::kTJ, k0 = 1 + (t % tiles_k) * hcore::kTK;
+    hcore::tile_stream<T, FX, true>(src, dst, n1, n2, j0, k0, r0, r1, plane);
+  }
 }
 
 __global__ void __launch_bounds__(kBThreads)
@@ -106,18 +124,31 @@ batch_persistent(const BandDesc* __restrict__ bands, uint32_t* done, const int32
         if (s == -1) break;           // finished
         all_done = false;
         if (s == -2) break;           // blocked for now
-        const void* src = (s & 1) ? d.b : d.a;
-        void* dst = (s & 1) ? d.a : d.b;
-        if (d.dtype == NPBGB_F64) {
+        const bool odd = ((d.step0 + s) & 1) != 0;
+        const void* src = odd ? d.b : d.a;
+        void* dst = odd ? d.a : d.b;
+        if (d.kind == NPBGB_KIND_HEAT3D) {
+          if (d.dtype == NPBGB_F64) {
+            if (f64_emulation)
+              heat_band_half_sweep<double, true>(static_cast<const double*>(src),
+                                                 static_cast<double*>(dst), d.n1, d.n2, d.r0, d.r1);
+            else
+              heat_band_half_sweep<double, false>(static_cast<const double*>(src),
+                                                  static_cast<double*>(dst), d.n1, d.n2, d.r0, d.r1);
+          } else {
+            heat_band_half_sweep<float, false>(static_cast<const float*>(src),
+                                               static_cast<float*>(dst), d.n1, d.n2, d.r0, d.r1);
+          }
+        } else if (d.dtype == NPBGB_F64) {
           if (f64_emulation)
             band_half_sweep<double, true>(static_cast<const double*>(src), static_cast<double*>(dst),
-                                          d.nx, d.r0, d.r1, one);
+                                          d.n1, d.r0, d.r1, one);
           else
             band_half_sweep<double, false>(static_cast<const double*>(src), static_cast<double*>(dst),
-                                           d.nx, d.r0, d.r1, one);
+                                           d.n1, d.r0, d.r1, one);
         } else {
           band_half_sweep<float, false>(static_cast<const float*>(src), static_cast<float*>(dst),
-                                        d.nx, d.r0, d.r1, one);
+                                        d.n1, d.r0, d.r1, one);
         }
         __syncthreads();
         if (tid == 0) {
@@ -169,6 +200,62 @@ struct npbgb_batch {
 
 namespace {
 
+// Validates grid g and describes its bands through emit(BandDesc) (left/right
+// are filled in relative to `first`, the index the grid's first band gets).
+// Returns NPBGB_OK with *nbands_out = 0 for grids with nothing to do.
+template <typename Emit>
+int32_t plan_grid(const npbgb_grid& G, int64_t g, int32_t band_rows, int first, int64_t* nbands_out,
+                  int64_t* updates_out, Emit emit, bool heat_allowed) {
+  using namespace npbgb;
+  *nbands_out = 0;
+  *updates_out = 0;
+  if (G.kind != NPBGB_KIND_JACOBI2D && !(heat_allowed && G.kind == NPBGB_KIND_HEAT3D))
+    return set_error(NPBGB_ERR_ARG, "batch: grid %lld: kind %d not supported here", (long long)g, G.kind);
+  if (G.dtype != NPBGB_F64 && G.dtype != NPBGB_F32)
+    return set_error(NPBGB_ERR_DTYPE, "batch: grid %lld: dtype %d", (long long)g, G.dtype);
+  const bool heat = G.kind == NPBGB_KIND_HEAT3D;
+  const int64_t n2 = heat ? G.n2 : 1;
+  if (G.n0 < 0 || G.n1 < 0 || n2 < 0 || G.n0 > 0x7fffffff || G.n1 > 0x7fffffff || n2 > 0x7fffffff)
+    return set_error(NPBGB_ERR_ARG, "batch: grid %lld: bad extents", (long long)g);
+  if (G.step0 < 0 || G.nsteps < 0)
+    return set_error(NPBGB_ERR_ARG, "batch: grid %lld: negative step0 or nsteps", (long long)g);
+  const int64_t total = G.tsteps > 1 ? 2 * int64_t(G.tsteps - 1) : 0;
+  int64_t todo = total - G.step0;
+  if (G.nsteps > 0 && G.nsteps < todo) todo = G.nsteps;
+  if (todo <= 0 || G.n0 < 3 || G.n1 < 3 || (heat && n2 < 3)) return NPBGB_OK;
+  if (!G.a || !G.b || G.a == G.b)
+    return set_error(NPBGB_ERR_ARG, "batch: grid %lld: null or aliased arrays", (long long)g);
+  const int n0 = int(G.n0), n1 = int(G.n1);
+  const int h = G.band_rows > 0 ? G.band_rows : (band_rows > 0 ? band_rows : (heat ? 8 : 32));
+  const int64_t nb = cdiv(n0 - 2, h);
+  for (int q = 0; q < int(nb); ++q) {
+    BandDesc d;
+    d.a = G.a;
+    d.b = G.b;
+    d.n0 = n0;
+    d.n1 = n1;
+    d.n2 = int32_t(n2);
+    d.r0 = 1 + q * h;
+    d.r1 = std::min(1 + (q + 1) * h, n0 - 1);
+    d.steps = int32_t(todo);
+    d.step0 = G.step0;
+    d.dtype = int16_t(G.dtype);
+    d.kind = int16_t(G.kind);
+    d.left = q > 0 ? first + q - 1 : -1;
+    d.right = q + 1 < int(nb) ? first + q + 1 : -1;
+    emit(d);
+  }
+  *nbands_out = nb;
+  *updates_out = todo * int64_t(n0 - 2) * (n1 - 2) * (heat ? (n2 - 2) : 1);
+  return NPBGB_OK;
+}
+
+double band_work(const npbgb::BandDesc& d) {
+  const double plane = d.kind == NPBGB_KIND_HEAT3D ? double(d.n1 - 2) * double(d.n2 - 2) * 2.0
+                                                    : double(d.n1 - 2);
+  return double(d.r1 - d.r0) * plane * d.steps * (d.dtype == NPBGB_F64 ? 2.0 : 1.0);
+}
+
 void free_batch(npbgb_batch* b) {
   if (!b) return;
   if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -214,36 +301,12 @@ int32_t npbgb_batch_create(const npbgb_grid* grids, int64_t count, int32_t band_
   std::vector<BandDesc> bands;
   int64_t updates = 0;
   for (int64_t g = 0; g < count; ++g) {
-    const npbgb_grid& G = grids[g];
-    if (G.kind != NPBGB_KIND_JACOBI2D)
-      return set_error(NPBGB_ERR_ARG, "batch: grid %lld: only jacobi2d grids are batched", (long long)g);
-    if (G.dtype != NPBGB_F64 && G.dtype != NPBGB_F32)
-      return set_error(NPBGB_ERR_DTYPE, "batch: grid %lld: dtype %d", (long long)g, G.dtype);
-    if (G.n0 < 0 || G.n1 < 0 || G.n0 > 0x7fffffff || G.n1 > 0x7fffffff)
-      return set_error(NPBGB_ERR_ARG, "batch: grid %lld: bad extents", (long long)g);
-    if (G.tsteps <= 1 || G.n0 < 3 || G.n1 < 3) continue;  // nothing to do, as in the reference
-    if (!G.a || !G.b || G.a == G.b)
-      return set_error(NPBGB_ERR_ARG, "batch: grid %lld: null or aliased arrays", (long long)g);
-    const int ny = int(G.n0), nx = int(G.n1);
-    int h = G.band_rows > 0 ? G.band_rows : (band_rows > 0 ? band_rows : 32);
-    const int interior = ny - 2;
-    const int nb = int(cdiv(interior, h));
-    const int first = int(bands.size());
-    for (int q = 0; q < nb; ++q) {
-      BandDesc d;
-      d.a = G.a;
-      d.b = G.b;
-      d.ny = ny;
-      d.nx = nx;
-      d.r0 = 1 + q * h;
-      d.r1 = std::min(1 + (q + 1) * h, ny - 1);
-      d.steps = 2 * (G.tsteps - 1);
-      d.dtype = G.dtype;
-      d.left = q > 0 ? first + q - 1 : -1;
-      d.right = q + 1 < nb ? first + q + 1 : -1;
-      bands.push_back(d);
-    }
-    updates += int64_t(2) * (G.tsteps - 1) * int64_t(interior) * (nx - 2);
+    int64_t nb = 0, up = 0;
+    const int32_t r = plan_grid(grids[g], g, band_rows, int(bands.size()), &nb, &up,
+                                [&](const BandDesc& d) { bands.push_back(d); }, true);
+    if (r != NPBGB_OK) return r;
+    if (int64_t(bands.size()) > 0x7fffffff) return set_error(NPBGB_ERR_NOMEM, "batch: too many bands");
+    updates += up;
   }
   auto* b = new (std::nothrow) npbgb_batch();
   if (!b) return set_error(NPBGB_ERR_NOMEM, "batch: host allocation");
@@ -260,10 +323,7 @@ int32_t npbgb_batch_create(const npbgb_grid* grids, int64_t count, int32_t band_
   {
     std::vector<int32_t> order(bands.size());
     for (size_t i = 0; i < order.size(); ++i) order[i] = int32_t(i);
-    auto work = [&](int32_t i) {
-      const BandDesc& d = bands[size_t(i)];
-      return double(d.r1 - d.r0) * double(d.nx - 2) * d.steps * (d.dtype == NPBGB_F64 ? 2.0 : 1.0);
-    };
+    auto work = [&](int32_t i) { return band_work(bands[size_t(i)]); };
     std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return work(x) > work(y); });
     using Item = std::pair<double, int>;
     std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
@@ -371,7 +431,7 @@ int32_t npbgb_batch_destroy(npbgb_batch* b) {
 // that array.
 namespace {
 
-constexpr int kNoAllocMaxBands = 32768;  // bands per call (about 1.9 MB of scratch)
+constexpr int kNoAllocMaxBands = 32768;  // bands per call (about 2.1 MB of scratch)
 constexpr int kNoAllocMaxCtas = 2048;
 
 struct NoAllocLayout {
@@ -417,41 +477,23 @@ extern "C" int32_t npbgb_batch_run_noalloc(const npbgb_grid* grids, int64_t coun
   // Plan the bands exactly as npbgb_batch_create does, into static buffers.
   int nb = 0;
   for (int64_t g = 0; g < count; ++g) {
-    const npbgb_grid& G = grids[g];
-    if (G.kind != NPBGB_KIND_JACOBI2D)
-      return set_error(NPBGB_ERR_ARG, "batch(no-alloc): grid %lld: only jacobi2d grids", (long long)g);
-    if (G.dtype != NPBGB_F64 && G.dtype != NPBGB_F32)
-      return set_error(NPBGB_ERR_DTYPE, "batch(no-alloc): grid %lld: dtype %d", (long long)g, G.dtype);
-    if (G.n0 < 0 || G.n1 < 0 || G.n0 > 0x7fffffff || G.n1 > 0x7fffffff)
-      return set_error(NPBGB_ERR_ARG, "batch(no-alloc): grid %lld: bad extents", (long long)g);
-    if (G.tsteps <= 1 || G.n0 < 3 || G.n1 < 3) continue;
-    if (!G.a || !G.b || G.a == G.b)
-      return set_error(NPBGB_ERR_ARG, "batch(no-alloc): grid %lld: null or aliased arrays", (long long)g);
-    const int ny = int(G.n0), nx = int(G.n1);
-    const int h = G.band_rows > 0 ? G.band_rows : (band_rows > 0 ? band_rows : 32);
-    const int64_t bands_here = cdiv(ny - 2, h);
-    if (int64_t(nb) + bands_here > kNoAllocMaxBands)
+    int64_t nbg = 0, up = 0;
+    bool overflow = false;
+    const int32_t r = plan_grid(grids[g], g, band_rows, nb, &nbg, &up,
+                                [&](const BandDesc& d) {
+                                  if (nb >= kNoAllocMaxBands) { overflow = true; return; }
+                                  g_na_bands[nb] = d;
+                                  g_na_work[nb] = band_work(d);
+                                  g_na_order[nb] = nb;
+                                  ++nb;
+                                },
+                                false);
+    if (r != NPBGB_OK) return r;
+    if (overflow)
       return set_error(NPBGB_ERR_NOMEM,
                        "batch(no-alloc): more than %d bands (its fixed scratch capacity); use "
                        "larger band_rows, fewer grids, or npbgb_batch_create",
                        kNoAllocMaxBands);
-    const int first = nb;
-    for (int q = 0; q < int(bands_here); ++q) {
-      BandDesc& d = g_na_bands[nb];
-      d.a = G.a;
-      d.b = G.b;
-      d.ny = ny;
-      d.nx = nx;
-      d.r0 = 1 + q * h;
-      d.r1 = std::min(1 + (q + 1) * h, ny - 1);
-      d.steps = 2 * (G.tsteps - 1);
-      d.dtype = G.dtype;
-      d.left = q > 0 ? first + q - 1 : -1;
-      d.right = q + 1 < int(bands_here) ? first + q + 1 : -1;
-      g_na_work[nb] = double(d.r1 - d.r0) * double(nx - 2) * d.steps * (d.dtype == NPBGB_F64 ? 2.0 : 1.0);
-      g_na_order[nb] = nb;
-      ++nb;
-    }
   }
   if (nb == 0) return NPBGB_OK;
 

@@ -14,8 +14,8 @@ static thread_local char g_last_error[512] = "";
 int64_t g_cfg_f64_emulation = 1;
 int64_t g_cfg_heat_chunk = 0;
 int64_t g_cfg_heat_tma = 1;
-int64_t g_cfg_heat_rows = 2;
-int64_t g_cfg_heat_hw_rows = 0;
+int64_t g_cfg_heat_rows = 0;     // 0: per-dtype default
+int64_t g_cfg_heat_hw_rows = -1; // -1: per-kernel default
 int64_t g_cfg_f64_cvt = 0;
 int64_t g_cfg_jacobi_chunk = 0;
 
@@ -112,11 +112,12 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       g_cfg_jacobi_chunk = value;
       return NPBGB_OK;
     case NPBGB_CFG_HEAT_ROWS:
-      if (value != 1 && value != 2 && value != 4) return set_error(NPBGB_ERR_ARG, "heat rows: 1, 2 or 4");
+      if (value != 0 && value != 1 && value != 2 && value != 4)
+        return set_error(NPBGB_ERR_ARG, "heat rows: 0 (automatic), 1, 2 or 4");
       g_cfg_heat_rows = value;
       return NPBGB_OK;
     case NPBGB_CFG_HEAT_HW_ROWS:
-      if (value < 0 || value > 32) return set_error(NPBGB_ERR_ARG, "heat hw rows: 0..32");
+      if (value < -1 || value > 32) return set_error(NPBGB_ERR_ARG, "heat hw rows: -1 (automatic) .. 32");
       g_cfg_heat_hw_rows = value;
       return NPBGB_OK;
     case NPBGB_CFG_F64_CVT:

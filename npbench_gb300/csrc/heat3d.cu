@@ -25,6 +25,7 @@
 #include <type_traits>
 
 #include "fx64.cuh"
+#include "heat_core.cuh"
 #include "npbgb_common.cuh"
 #include "tma.cuh"
 
@@ -41,67 +42,36 @@ namespace {
 
 __device__ unsigned int g_heat_error;  // bit 0: an mbarrier wait timed out
 
-constexpr int kTK = 32;   // tile extent along axis 2 (one warp)
-constexpr int kTJ = 8;    // tile extent along axis 1 (warps per CTA)
-constexpr int kThreads = kTK * kTJ;
+using hcore::kThreads;
+using hcore::kTJ;
+using hcore::kTK;
+using hcore::heat_point;
+using hcore::to_fx;
 using fx::hi32;
 using fx::kPoisonHi;
-
-template <typename T>
-__device__ __forceinline__ T heat_point(T c, T ip, T im, T jp, T jm, T kp, T km) {
-  const T two = T(2.0), eighth = T(0.125);
-  const T c2 = mul_rn(two, c);
-  const T t0 = mul_rn(eighth, add_rn(sub_rn(ip, c2), im));
-  const T t1 = mul_rn(eighth, add_rn(sub_rn(jp, c2), jm));
-  const T t2 = mul_rn(eighth, add_rn(sub_rn(kp, c2), km));
-  return add_rn(add_rn(add_rn(t0, t1), t2), c);
-}
-
-// Fixed-point form of heat_point; inputs in frame 59, result as a double.
-__device__ __forceinline__ double heat_point_fx(int64_t c, int64_t ip, int64_t im, int64_t jp,
-                                                int64_t jm, int64_t kp, int64_t km) {
-  using fx::round53;
-  const int64_t c2 = c * 2;
-  const int64_t s0 = round53(round53(ip - c2) + im);  // 8 * t0 in frame 59 == t0 in frame 62
-  const int64_t s1 = round53(round53(jp - c2) + jm);
-  const int64_t s2 = round53(round53(kp - c2) + km);
-  const int64_t w = round53(round53(round53(s0 + s1) + s2) + c * 8);
-  return fx::to_f64<62>(w);
-}
-
-__device__ __forceinline__ int64_t to_fx(double v) { return fx::from_f64_f59_or_poison(v); }
-
-// Evaluates one point from staged values (T for the plain path, frame-59
-// integers with poison marks for binary64), falling back to hardware binary64
-// from global memory `q` (pointer to the centre) when an input is poisoned.
-template <typename T, bool FX, typename S>
-__device__ __forceinline__ T eval_point(S c, S ip, S im, S jp, S jm, S kp, S km, const T* q,
-                                        int64_t s0, int64_t s1) {
-  if constexpr (FX) {
-    const uint32_t tag = hi32(c) | hi32(ip) | hi32(im) | hi32(jp) | hi32(jm) | hi32(kp) | hi32(km);
-    if (!(tag & kPoisonHi)) return heat_point_fx(c, ip, im, jp, jm, kp, km);
-    return heat_point<T>(q[0], q[s0], q[-s0], q[s1], q[-s1], q[1], q[-1]);
-  } else {
-    return heat_point<T>(c, ip, im, jp, jm, kp, km);
-  }
-}
 
 // ---------------------------------------------------------------------------
 // TMA pipeline
 // ---------------------------------------------------------------------------
-// Fixed-point point update with its 64-bit adds on the multiply-add pipe.
-template <bool CVT>
+// Fixed-point point update.  MAD: the 64-bit adds are issued as multiply-adds
+// (fx::add64 / fx::round53m) to shift work from the integer ALU pipe to the
+// multiply-add pipe; otherwise plain integer adds.
+template <bool CVT, bool MAD>
 __device__ __forceinline__ double heat_point_fxm(int64_t c, int64_t ip, int64_t im, int64_t jp,
                                                  int64_t jm, int64_t kp, int64_t km, uint32_t one) {
-  using fx::add64;
-  using fx::round53m;
+  auto add = [one](int64_t x, int64_t y) {
+    if constexpr (MAD) return fx::add64(x, y, one); else return int64_t(uint64_t(x) + uint64_t(y));
+  };
+  auto rnd = [one](int64_t x) {
+    if constexpr (MAD) return fx::round53m(x, one); else return fx::round53(x);
+  };
   const int64_t nc2 = -2 * c;
-  const int64_t s0 = round53m(add64(round53m(add64(ip, nc2, one), one), im, one), one);
-  const int64_t s1 = round53m(add64(round53m(add64(jp, nc2, one), one), jm, one), one);
-  const int64_t s2 = round53m(add64(round53m(add64(kp, nc2, one), one), km, one), one);
-  const int64_t u = round53m(add64(s0, s1, one), one);
-  const int64_t v = round53m(add64(u, s2, one), one);
-  const int64_t w = round53m(add64(v, c * 8, one), one);
+  const int64_t s0 = rnd(add(rnd(add(ip, nc2)), im));
+  const int64_t s1 = rnd(add(rnd(add(jp, nc2)), jm));
+  const int64_t s2 = rnd(add(rnd(add(kp, nc2)), km));
+  const int64_t u = rnd(add(s0, s1));
+  const int64_t v = rnd(add(u, s2));
+  const int64_t w = rnd(add(v, c * 8));
   if constexpr (CVT) return fx::to_f64_cvt<62>(w);
   return fx::to_f64<62>(w);
 }
@@ -213,7 +183,7 @@ heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ sr
           const uint32_t tag =
               hi32(c) | hi32(ip) | hi32(im) | hi32(jp) | hi32(jm) | hi32(kp) | hi32(km);
           if (!(tag & kPoisonHi))
-            out = heat_point_fxm<CVT>(c, ip, im, jp, jm, kp, km, one);
+            out = heat_point_fxm<CVT, false>(c, ip, im, jp, jm, kp, km, one);
           else
             out = heat_point<T>(q[0], q[s0], q[-s0], q[s1], q[-s1], q[1], q[-1]);
         }
@@ -232,61 +202,11 @@ template <typename T, bool FX>
 __global__ void __launch_bounds__(kThreads)
 heat3d_ldg(const T* __restrict__ src, T* __restrict__ dst, int64_t n0, int64_t n1, int64_t n2,
            int chunk) {
-  using S = typename std::conditional<FX, int64_t, T>::type;
-  __shared__ S plane[3][kTJ + 2][kTK + 2];
-
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  __shared__ hcore::PlaneBuf<T, FX> plane;
   const int64_t k0 = 1 + int64_t(blockIdx.x) * kTK, j0 = 1 + int64_t(blockIdx.y) * kTJ;
-  const int64_t k = k0 + tx, j = j0 + ty;
-  const bool active = k < n2 - 1 && j < n1 - 1;
-  const bool own_inb = k < n2 && j < n1;
-  const int64_t s0 = n1 * n2, s1 = n2;
   const int64_t ib = 1 + int64_t(blockIdx.z) * chunk;
   const int64_t ie = (ib + chunk < n0 - 1) ? ib + chunk : n0 - 1;
-
-  // Halo roles: warp 0 the row before the tile, warp 1 the row after, warps
-  // 2 and 3 (first kTJ lanes) the columns before and after.  No corners: the
-  // stencil has no diagonal neighbours.
-  int er = -1, ec = -1;
-  int64_t ej = 0, ek = 0;
-  if (ty == 0) { ej = j0 - 1; ek = k; er = 0; ec = tx + 1; }
-  else if (ty == 1) { ej = j0 + kTJ; ek = k; er = kTJ + 1; ec = tx + 1; }
-  else if (ty == 2 && tx < kTJ) { ej = j0 + tx; ek = k0 - 1; er = tx + 1; ec = 0; }
-  else if (ty == 3 && tx < kTJ) { ej = j0 + tx; ek = k0 + kTK; er = tx + 1; ec = kTK + 1; }
-  const bool has_extra = er >= 0 && ej < n1 && ek < n2;
-  const T* own_p = src + j * s1 + k;
-  const T* extra_p = src + ej * s1 + ek;
-
-  auto stage = [&](int64_t i, int b, S& own) {
-    if (own_inb) {
-      const T v = own_p[i * s0];
-      if constexpr (FX) own = to_fx(v); else own = v;
-      plane[b][ty + 1][tx + 1] = own;
-    }
-    if (has_extra) {
-      const T v = extra_p[i * s0];
-      if constexpr (FX) plane[b][er][ec] = to_fx(v); else plane[b][er][ec] = v;
-    }
-  };
-
-  S xp = S(0), xc = S(0), xn = S(0);
-  int bc = 1, bn = 2;
-  stage(ib - 1, 0, xp);
-  stage(ib, bc, xc);
-  for (int64_t i = ib; i < ie; ++i) {
-    stage(i + 1, bn, xn);
-    __syncthreads();
-    if (active) {
-      const S* P = &plane[bc][ty + 1][tx + 1];
-      dst[i * s0 + j * s1 + k] = eval_point<T, FX>(xc, xn, xp, P[kTK + 2], P[-(kTK + 2)], P[1],
-                                                   P[-1], own_p + i * s0, s0, s1);
-    }
-    const int t = (bn + 1) % 3;  // buffer of plane i-1, free after this barrier round
-    bc = bn;
-    bn = t;
-    xp = xc;
-    xc = xn;
-  }
+  hcore::tile_stream<T, FX, false>(src, dst, n1, n2, j0, k0, ib, ie, plane);
 }
 
 int auto_chunk(int64_t n0, int64_t tiles, int ctas_per_sm) {
@@ -325,7 +245,7 @@ int32_t launch_tma(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tstep
   if (gy > 65535 || gz > 65535 || gx > 0x7fffffff)
     return set_error(NPBGB_ERR_ARG, "heat3d: extent too large");
   const dim3 grid{unsigned(gx), unsigned(gy), unsigned(gz)};
-  int hw = int(g_cfg_heat_hw_rows);
+  int hw = g_cfg_heat_hw_rows >= 0 ? int(g_cfg_heat_hw_rows) : (FX ? 2 : 0);
   if (hw > G::TJ) hw = G::TJ;
   for (int32_t t = 1; t < tsteps; ++t) {
     heat3d_tma<T, FX, R, CVT><<<grid, kThreads, smem, st>>>(map_a, a, b, n0, n1, n2, chunk, hw, 1u);
@@ -357,7 +277,9 @@ template <typename T, bool FX>
 int32_t run(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps, cudaStream_t st) {
   if (tsteps <= 1 || n0 < 3 || n1 < 3 || n2 < 3) return NPBGB_OK;
   if (g_cfg_heat_tma) {
-    const int rows = int(g_cfg_heat_rows);
+    // Tuned on GB300 (256^3): binary32 is memory-latency bound and wants more
+    // rows per thread; binary64 (integer-pipe bound) wants one.
+    const int rows = g_cfg_heat_rows > 0 ? int(g_cfg_heat_rows) : (sizeof(T) == 4 ? 4 : 1);
     const bool cvt = g_cfg_f64_cvt != 0;
     int32_t r;
     if (rows >= 4)

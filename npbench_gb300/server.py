@@ -1,0 +1,324 @@
+"""Continuous-batching server for stencil solves on one GPU.
+
+A request is one grid solve, the reference's ``kernel(TSTEPS, A, B)`` of
+polybench/jacobi_2d/jacobi_2d_numpy.py:4-10 (2D) or
+polybench/heat_3d/heat_3d_numpy.py:4-20 (3D), in float32 or float64, with its
+own size and step count.
+
+Scheduling is iteration-level continuous batching:
+
+* ``submit`` queues a request and returns a ``concurrent.futures.Future``;
+* the serving thread admits queued requests, oldest first, while their two
+  device arrays fit in the HBM budget (``AdmissionController``).  Their grids
+  stay resident on the device until they finish;
+* each round advances every resident grid by up to ``quantum`` half-sweeps:
+  grids below ``direct_cells`` interior points share ONE persistent batch
+  launch (``npbench_gb300.batch``, libnpbgb's ``npbgb_batch_*``), so their
+  work overlaps on the device without a launch per grid; larger grids, each
+  of which fills the GPU on its own, run their quantum with the single-grid
+  kernels (TMA pipelines) in the same round;
+* finished grids are copied back, their memory is released, and requests that
+  arrived meanwhile are admitted for the next round.
+
+A grid advanced in rounds ends bit-identical to the same grid run alone (the
+batch kernel resumes runs exactly at ``step0``), which the tests check.
+``run_sequential`` is the comparator: the same requests, one at a time in
+arrival order, each with plain per-grid launches.
+"""
+import collections
+import concurrent.futures
+import itertools
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib, stencils
+from .batch import Batch
+
+__all__ = ["AdmissionController", "Request", "StencilServer", "run_sequential", "latency_stats"]
+
+
+class AdmissionController:
+    """Byte budget for resident grids.  Host logic only (no GPU)."""
+
+    def __init__(self, budget_bytes):
+        if budget_bytes <= 0:
+            raise ValueError("budget must be positive")
+        self.budget = int(budget_bytes)
+        self.in_use = 0
+        self.peak = 0
+        self._lock = threading.Lock()
+
+    def fits_ever(self, nbytes):
+        return nbytes <= self.budget
+
+    def try_admit(self, nbytes):
+        with self._lock:
+            if self.in_use + nbytes > self.budget:
+                return False
+            self.in_use += nbytes
+            self.peak = max(self.peak, self.in_use)
+            return True
+
+    def release(self, nbytes):
+        with self._lock:
+            if nbytes > self.in_use:
+                raise RuntimeError("released more bytes than admitted")
+            self.in_use -= nbytes
+
+
+@dataclass
+class Request:
+    """One solve.  Give host arrays ``a`` (and ``b`` for 2D), or a ``seed``
+    from which the server draws U[0,1) inputs on the device."""
+    shape: tuple
+    dtype: object
+    tsteps: int
+    a: np.ndarray = None
+    b: np.ndarray = None
+    seed: int = None
+    return_host: bool = True
+    # filled in by the server
+    id: int = -1
+    t_submit: float = 0.0
+    t_admit: float = 0.0
+    t_done: float = 0.0
+    half_sweeps: int = 0
+    done: int = 0
+    dev: tuple = None
+    future: concurrent.futures.Future = field(default=None, repr=False)
+
+    @property
+    def kind(self):
+        return "jacobi2d" if len(self.shape) == 2 else "heat3d"
+
+    @property
+    def nbytes(self):
+        return 2 * int(np.prod(self.shape)) * np.dtype(self.dtype).itemsize
+
+    @property
+    def updates(self):
+        inner = int(np.prod([max(0, s - 2) for s in self.shape]))
+        return max(0, 2 * (self.tsteps - 1)) * inner
+
+
+def _validate(req):
+    if len(req.shape) not in (2, 3):
+        raise ValueError("requests are 2D (Jacobi) or 3D (heat) grids")
+    if np.dtype(req.dtype) not in (np.dtype(np.float32), np.dtype(np.float64)):
+        raise TypeError(f"unsupported dtype {req.dtype}")
+    if req.a is None and req.seed is None:
+        raise ValueError("a request needs input arrays or a seed")
+    if req.a is not None:
+        if tuple(req.a.shape) != tuple(req.shape):
+            raise ValueError("input shape does not match the request")
+        if len(req.shape) == 2 and req.b is None:
+            raise ValueError("Jacobi-2D requests need both A and B")
+
+
+def _materialise(req, device):
+    """Device arrays for an admitted request (allocation happens here)."""
+    import torch
+    tdt = torch.float64 if np.dtype(req.dtype) == np.float64 else torch.float32
+    if req.a is not None:
+        A = torch.from_numpy(np.ascontiguousarray(req.a, dtype=req.dtype)).to(device)
+        B = (torch.from_numpy(np.ascontiguousarray(req.b, dtype=req.dtype)).to(device)
+             if req.b is not None else A.clone())
+    else:
+        g = torch.Generator(device=device)
+        g.manual_seed(int(req.seed))
+        A = torch.rand(req.shape, dtype=torch.float64, device=device, generator=g).to(tdt)
+        B = (torch.rand(req.shape, dtype=torch.float64, device=device, generator=g).to(tdt)
+             if len(req.shape) == 2 else A.clone())
+    return A, B
+
+
+class StencilServer:
+    """Serving thread with an HBM admission budget and continuous batching."""
+
+    def __init__(self, device=0, hbm_budget_bytes=150e9, quantum=32, band_rows=0,
+                 direct_cells=1 << 20):
+        import torch
+        self.device = torch.device("cuda", device) if isinstance(device, int) else device
+        self.admission = AdmissionController(hbm_budget_bytes)
+        if quantum < 2 or quantum % 2:
+            raise ValueError("quantum must be an even number of half-sweeps >= 2")
+        self.quantum = int(quantum)
+        self.direct_cells = int(direct_cells)
+        self.band_rows = int(band_rows)
+        self._queue = collections.deque()
+        self._active = []
+        self._cv = threading.Condition()
+        self._stop = False
+        self._ids = itertools.count()
+        self._thread = None
+        self.rounds = 0
+        self.completed = []
+        self.error = None
+
+    # -- client side ------------------------------------------------------
+    def submit(self, req):
+        _validate(req)
+        if not self.admission.fits_ever(req.nbytes):
+            raise ValueError(f"request needs {req.nbytes} bytes, above the HBM budget "
+                             f"{self.admission.budget}")
+        req.id = next(self._ids)
+        req.t_submit = time.perf_counter()
+        req.half_sweeps = max(0, 2 * (req.tsteps - 1))
+        req.future = concurrent.futures.Future()
+        with self._cv:
+            if self._stop:
+                raise RuntimeError("server stopped")
+            if self.error is not None:
+                raise RuntimeError("server failed") from self.error
+            self._queue.append(req)
+            self._cv.notify()
+        return req.future
+
+    def start(self):
+        _lib.load()
+        self._thread = threading.Thread(target=self._serve, name="npbgb-server", daemon=True)
+        self._thread.start()
+        return self
+
+    def stop(self, drain=True):
+        """Stop after the queued and resident requests finish (drain) or now."""
+        with self._cv:
+            self._stop = True
+            if not drain:
+                for r in list(self._queue):
+                    r.future.cancel()
+                self._queue.clear()
+            self._cv.notify()
+        if self._thread is not None:
+            self._thread.join()
+
+    def __enter__(self):
+        return self.start()
+
+    def __exit__(self, *exc):
+        self.stop(drain=exc[0] is None)
+
+    # -- serving thread ---------------------------------------------------
+    def _admit(self):
+        while self._queue:
+            req = self._queue[0]
+            if req.future.cancelled():
+                self._queue.popleft()
+                continue
+            if not self.admission.try_admit(req.nbytes):
+                break  # oldest first: later requests wait behind it
+            self._queue.popleft()
+            req.dev = _materialise(req, self.device)
+            req.t_admit = time.perf_counter()
+            if req.half_sweeps == 0:
+                self._finish(req)
+            else:
+                self._active.append(req)
+
+    def _finish(self, req):
+        import torch
+        A, B = req.dev
+        if req.return_host:
+            torch.cuda.synchronize(self.device)
+            out = (A.cpu().numpy(), B.cpu().numpy())
+        else:
+            out = (A, B)
+        req.dev = None
+        self.admission.release(req.nbytes)
+        req.t_done = time.perf_counter()
+        self.completed.append(req)
+        req.future.set_result(out)
+
+    def _round(self):
+        import torch
+        small, large = [], []
+        for r in self._active:
+            inner = int(np.prod([max(0, x - 2) for x in r.shape]))
+            (large if inner >= self.direct_cells else small).append(r)
+        if small:
+            entries = [(r.dev[0], r.dev[1], r.tsteps, r.done, self.quantum) for r in small]
+            with Batch(entries, band_rows=self.band_rows) as b:
+                b.launch()
+        for r in large:
+            # done is even (the quantum is even), so the next half-sweep reads A:
+            # kernel(n/2 + 1, A, B) performs exactly the next n half-sweeps.
+            n = min(self.quantum, r.half_sweeps - r.done)
+            A, B = r.dev
+            (stencils.jacobi_2d_kernel if A.dim() == 2 else stencils.heat_3d_kernel)(
+                n // 2 + 1, A, B)
+        torch.cuda.current_stream(self.device).synchronize()
+        _lib.device_status()
+        self.rounds += 1
+        still = []
+        for r in self._active:
+            r.done = min(r.half_sweeps, r.done + self.quantum)
+            if r.done >= r.half_sweeps:
+                self._finish(r)
+            else:
+                still.append(r)
+        self._active = still
+
+    def _serve(self):
+        import torch
+        torch.cuda.set_device(self.device)
+        try:
+            while True:
+                with self._cv:
+                    while not self._queue and not self._active and not self._stop:
+                        self._cv.wait(timeout=0.05)
+                    if self._stop and not self._queue and not self._active:
+                        return
+                    self._admit()
+                if self._active:
+                    self._round()
+                elif self._queue:
+                    # nothing resident and the oldest request does not fit: cannot happen
+                    # (fits_ever was checked at submit); back off briefly
+                    time.sleep(0.001)
+        except Exception as e:  # fail every outstanding request loudly
+            self.error = e
+            with self._cv:
+                pending = list(self._queue) + list(self._active)
+                self._queue.clear()
+                self._active = []
+            for r in pending:
+                if not r.future.done():
+                    r.future.set_exception(e)
+
+
+def run_sequential(requests, arrivals, device=0):
+    """Comparator: the requests one at a time, in arrival order, each with plain
+    per-grid launches (``stencils.jacobi_2d_kernel`` / ``heat_3d_kernel``).
+    ``arrivals`` are offsets in seconds from the start.  Returns the requests
+    with t_submit/t_done filled in."""
+    import torch
+    dev = torch.device("cuda", device) if isinstance(device, int) else device
+    t0 = time.perf_counter()
+    for req, at in zip(requests, arrivals):
+        now = time.perf_counter() - t0
+        if at > now:
+            time.sleep(at - now)
+        req.t_submit = t0 + at
+        A, B = _materialise(req, dev)
+        (stencils.jacobi_2d_kernel if A.dim() == 2 else stencils.heat_3d_kernel)(req.tsteps, A, B)
+        if req.return_host:
+            A.cpu()
+            B.cpu()
+        torch.cuda.synchronize(dev)
+        req.t_done = time.perf_counter()
+    return requests
+
+
+def latency_stats(requests):
+    lat = np.array([r.t_done - r.t_submit for r in requests])
+    if lat.size == 0:
+        return {"p50_ms": None, "p99_ms": None, "count": 0}
+    span = max(r.t_done for r in requests) - min(r.t_submit for r in requests)
+    ups = sum(r.updates for r in requests)
+    return {"count": int(lat.size), "p50_ms": float(np.percentile(lat, 50) * 1e3),
+            "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3),
+            "span_s": float(span), "updates": int(ups),
+            "updates_per_s": float(ups / span) if span > 0 else None}

@@ -60,3 +60,42 @@ def uniform_heat(shape, dtype=np.float64, seed=0):
 def uniform_hdiff(I, J, K, seed=0):
     rng = np.random.default_rng(seed)
     return rng.random((I + 4, J + 4, K)), rng.random((I, J, K)), rng.random((I, J, K))
+
+
+def batch_jacobi_specs(n_grids=4096, seed=0, side=(64, 2048), tsteps=(10, 500)):
+    """Batched Jacobi-2D configuration: per grid (shape, dtype, TSTEPS).
+
+    Side lengths are drawn log-uniform in [side[0], side[1]] per axis (non-square),
+    half the grids float32 and half float64 (alternating), TSTEPS uniform in
+    [tsteps[0], tsteps[1]].
+    """
+    rng = np.random.default_rng(seed)
+    lo, hi = np.log(side[0]), np.log(side[1])
+    shapes = np.exp(rng.uniform(lo, hi, size=(n_grids, 2))).round().astype(np.int64)
+    steps = rng.integers(tsteps[0], tsteps[1] + 1, size=n_grids)
+    return [((int(s[0]), int(s[1])), np.float32 if g % 2 else np.float64, int(t))
+            for g, (s, t) in enumerate(zip(shapes, steps))]
+
+
+def served_requests(n, rate_hz, seed=0, side2d=(128, 4096), side3d=(32, 384),
+                    tsteps=(20, 1000), f32_share=0.7):
+    """Served-stream configuration: Poisson arrivals and mixed solves.
+
+    Returns (arrival_offsets_s, [(shape, dtype, TSTEPS, data_seed)]): half the
+    requests 2D Jacobi with sides log-uniform in side2d, half 3D heat with
+    sides log-uniform in side3d, 70% float32 / 30% float64, TSTEPS uniform in
+    tsteps, inter-arrival times exponential with mean 1/rate_hz.
+    """
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate_hz, size=n))
+    out = []
+    for i in range(n):
+        if rng.random() < 0.5:
+            lo, hi = np.log(side2d[0]), np.log(side2d[1])
+            shape = tuple(int(x) for x in np.exp(rng.uniform(lo, hi, 2)).round())
+        else:
+            lo, hi = np.log(side3d[0]), np.log(side3d[1])
+            shape = tuple(int(x) for x in np.exp(rng.uniform(lo, hi, 3)).round())
+        dt = np.float32 if rng.random() < f32_share else np.float64
+        out.append((shape, dt, int(rng.integers(tsteps[0], tsteps[1] + 1)), int(rng.integers(1 << 31))))
+    return arrivals, out

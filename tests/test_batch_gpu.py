@@ -96,3 +96,49 @@ def test_empty_and_trivial_batches():
         b.launch()
         assert b.info()["bands"] == 0
     assert torch.equal(A, a0)
+
+
+def _heat_grids(n, seed, max_side=40, max_t=12):
+    rng = np.random.default_rng(seed)
+    grids = []
+    for g in range(n):
+        shape = tuple(int(x) for x in np.exp(rng.uniform(np.log(3), np.log(max_side), 3)).round())
+        dt = np.float32 if g % 2 else np.float64
+        T = int(rng.integers(0, max_t))
+        A = rng.random(shape).astype(dt)
+        grids.append((A, A.copy(), T))
+    return grids
+
+
+@pytest.mark.parametrize("band_rows", [0, 1, 5])
+def test_batch_mixed_jacobi_and_heat(band_rows):
+    grids = _mixed_batch(15, seed=7, max_side=200, max_t=20) + _heat_grids(15, seed=8)
+    dev = [(torch.from_numpy(A).to(DEV), torch.from_numpy(B).to(DEV), T) for A, B, T in grids]
+    with Batch(dev, band_rows=band_rows) as b:
+        b.launch()
+        _lib.device_status()
+    for n, ((A, B, T), (dA, dB, _)) in enumerate(zip(grids, dev)):
+        ra, rb = A.copy(), B.copy()
+        (cref.jacobi_2d_kernel if A.ndim == 2 else cref.heat_3d_kernel)(T, ra, rb)
+        assert bits_equal(dA.cpu().numpy(), ra), (n, A.shape, A.dtype, T, first_diff(dA.cpu().numpy(), ra))
+        assert bits_equal(dB.cpu().numpy(), rb), (n, A.shape, A.dtype, T)
+
+
+def test_batch_resumed_in_pieces_equals_one_run():
+    """step0/nsteps: a run split over several launches gives the uninterrupted bits."""
+    grids = _mixed_batch(8, seed=11, max_side=120, max_t=30) + _heat_grids(8, seed=12, max_t=20)
+    dev = [(torch.from_numpy(A).to(DEV), torch.from_numpy(B).to(DEV), T) for A, B, T in grids]
+    done = [0] * len(dev)
+    total = [max(0, 2 * (T - 1)) for _, _, T in grids]
+    piece = 3
+    while any(d < t for d, t in zip(done, total)):
+        entries = [(a, b, T, done[n], piece) for n, (a, b, T) in enumerate(dev) if done[n] < total[n]]
+        with Batch(entries) as b:
+            b.launch()
+            _lib.device_status()
+        for n in range(len(dev)):
+            done[n] = min(total[n], done[n] + piece)
+    for n, ((A, B, T), (dA, dB, _)) in enumerate(zip(grids, dev)):
+        ra, rb = A.copy(), B.copy()
+        (cref.jacobi_2d_kernel if A.ndim == 2 else cref.heat_3d_kernel)(T, ra, rb)
+        assert bits_equal(dA.cpu().numpy(), ra) and bits_equal(dB.cpu().numpy(), rb), n
