@@ -69,15 +69,13 @@ def parse():
                     help="batch/serve: also time the per-grid / sequential comparator")
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--rate", type=float, default=1000.0)
-    ap.add_argument("--quantum", type=int, default=32)
+    ap.add_argument("--quantum", type=int, default=64)
     return ap.parse_args()
 
 
 def dist_info():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from npbench_gb300 import replicas
+    return replicas.dist_info()
 
 
 def measured_peaks():
@@ -251,14 +249,10 @@ def run_gb300(args, world, rank, local):
     with ClockSampler(local) as clk:
         ms64, A64, B64, A0 = timed(np.float64)
     clocks = clk.summary()
-    ms_max = ms64
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms64], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
+    from npbench_gb300 import replicas
+    ms_max = replicas.max_over_ranks(ms64, device=dev)
     ms_per_step = ms_max / args.steps
-    value = world * UPDATES_PER_STEP * args.steps / (ms_max * 1e-3)
+    value = replicas.job_throughput(UPDATES_PER_STEP * args.steps, world, ms_max * 1e-3)
 
     # Roofline of the dominant kernel (one half-sweep launch).
     peak, peak_kind = measured_peaks()

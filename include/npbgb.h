@@ -60,6 +60,11 @@ extern "C" {
                                      -1 (default) = 2 */
 #define NPBGB_CFG_F64_CVT 7       /* 1: fixed-point conversions use the binary64
                                      convert instructions; 0: integer bit operations */
+#define NPBGB_CFG_JACOBI_HW_WARPS 8 /* jacobi2d / batch binary64: warps per CTA (of 8)
+                                       that use hardware binary64 next to the
+                                       fixed-point warps; -1 (default) = 1 */
+#define NPBGB_CFG_BATCH_CTAS_PER_SM 9 /* persistent batch kernel: 2 or 3 (default)
+                                         CTAs per SM (read when a batch is planned) */
 
 /* Grid kinds for batches. */
 #define NPBGB_KIND_JACOBI2D 0
@@ -141,6 +146,22 @@ NPBGB_API int32_t npbgb_heat3d(void* A, void* B, int64_t n0, int64_t n1, int64_t
 NPBGB_API int32_t npbgb_hdiff(const void* in_field, void* out_field, const void* coeff, int64_t I,
                     int64_t J, int64_t K, int32_t dtype, void* stream);
 
+/* 1D 3-point Jacobi, the whole time loop of
+ *   kernel(TSTEPS, A, B)   polybench/jacobi_1d/jacobi_1d_numpy.py:4-8
+ * A and B have n points; tsteps-1 times: dst[i] = 0.33333 * ((src[i-1] + src[i]) + src[i+1])
+ * over [1, n-1), A -> B then B -> A.  Temporal blocking in shared memory: one
+ * launch per 32 half-sweeps. */
+NPBGB_API int32_t npbgb_jacobi1d(void* A, void* B, int64_t n, int32_t tsteps, int32_t dtype,
+                                 void* stream);
+
+/* 2D FDTD, the whole time loop of
+ *   kernel(TMAX, ex, ey, hz, _fict_)   polybench/fdtd_2d/fdtd_2d_numpy.py:4-11
+ * ex, ey, hz are (nx, ny); fict has fict_len >= tmax entries (NPBGB_ERR_ARG
+ * otherwise, where the reference raises IndexError).  Updates ex, ey, hz in
+ * place. */
+NPBGB_API int32_t npbgb_fdtd2d(void* ex, void* ey, void* hz, const void* fict, int64_t fict_len,
+                               int64_t nx, int64_t ny, int32_t tmax, int32_t dtype, void* stream);
+
 /* Batches: many independent grids advanced by one persistent launch.
  *
  * npbgb_batch_create plans a batch of Jacobi-2D and Heat-3D grids: each grid
@@ -160,6 +181,11 @@ NPBGB_API int32_t npbgb_hdiff(const void* in_field, void* out_field, const void*
 NPBGB_API int32_t npbgb_batch_create(const npbgb_grid* grids, int64_t count, int32_t band_rows,
                                      npbgb_batch** out);
 NPBGB_API int32_t npbgb_batch_launch(npbgb_batch* batch, int32_t use_graph, void* stream);
+/* Re-plans an existing batch for a new grid list (for example the next round
+ * of a server), reusing its device buffers when they are large enough.
+ * A captured graph is dropped and recaptured by the next graph launch. */
+NPBGB_API int32_t npbgb_batch_replan(npbgb_batch* batch, const npbgb_grid* grids, int64_t count,
+                                     int32_t band_rows);
 NPBGB_API int32_t npbgb_batch_info(const npbgb_batch* batch, int64_t* nbands, int64_t* nctas,
                                    int64_t* updates);
 NPBGB_API int32_t npbgb_batch_destroy(npbgb_batch* batch);

@@ -7,6 +7,8 @@ and run hand-written CUDA kernels from ``libnpbgb.so`` through its C ABI
 plugin (``framework_info`` JSON, ``Framework`` subclass, kernel modules).
 """
 from ._lib import NpbgbError, load, version  # noqa: F401
-from .stencils import hdiff, heat_3d_kernel, jacobi_2d_kernel  # noqa: F401
+from .stencils import (fdtd_2d_kernel, hdiff, heat_3d_kernel, jacobi_1d_kernel,  # noqa: F401
+                       jacobi_2d_kernel)
 
-__all__ = ["NpbgbError", "load", "version", "jacobi_2d_kernel", "heat_3d_kernel", "hdiff"]
+__all__ = ["NpbgbError", "load", "version", "jacobi_2d_kernel", "heat_3d_kernel", "hdiff",
+           "jacobi_1d_kernel", "fdtd_2d_kernel"]

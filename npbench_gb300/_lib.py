@@ -26,6 +26,8 @@ NPBGB_CFG_JACOBI_CHUNK = 4
 NPBGB_CFG_HEAT_ROWS = 5
 NPBGB_CFG_HEAT_HW_ROWS = 6
 NPBGB_CFG_F64_CVT = 7
+NPBGB_CFG_JACOBI_HW_WARPS = 8
+NPBGB_CFG_BATCH_CTAS_PER_SM = 9
 
 NPBGB_KIND_JACOBI2D = 0
 NPBGB_KIND_HEAT3D = 1
@@ -52,6 +54,7 @@ SIGNATURES = {
     "npbgb_selftest_wait_timeout": (_i32, [_i64, _vp]),
     "npbgb_batch_create": (_i32, [ctypes.POINTER(Grid), _i64, _i32, ctypes.POINTER(_vp)]),
     "npbgb_batch_launch": (_i32, [_vp, _i32, _vp]),
+    "npbgb_batch_replan": (_i32, [_vp, ctypes.POINTER(Grid), _i64, _i32]),
     "npbgb_batch_info": (_i32, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64),
                                  ctypes.POINTER(_i64)]),
     "npbgb_batch_destroy": (_i32, [_vp]),
@@ -59,6 +62,8 @@ SIGNATURES = {
     "npbgb_jacobi2d": (_i32, [_vp, _vp, _i64, _i64, _i32, _i32, _vp]),
     "npbgb_heat3d": (_i32, [_vp, _vp, _i64, _i64, _i64, _i32, _i32, _vp]),
     "npbgb_hdiff": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i32, _vp]),
+    "npbgb_jacobi1d": (_i32, [_vp, _vp, _i64, _i32, _i32, _vp]),
+    "npbgb_fdtd2d": (_i32, [_vp, _vp, _vp, _vp, _i64, _i64, _i64, _i32, _i32, _vp]),
 }
 
 _lock = threading.Lock()

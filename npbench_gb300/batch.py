@@ -23,6 +23,22 @@ __all__ = ["Batch"]
 class Batch:
     def __init__(self, grids, band_rows=0, band_rows_of=None):
         """grids: iterable of (A, B, TSTEPS); band_rows_of(A) may pick rows per band."""
+        self._h = None
+        arr = self._structs(grids, band_rows_of)
+        h = ctypes.c_void_p()
+        _lib.check(_lib.load().npbgb_batch_create(arr, len(grids), int(band_rows), ctypes.byref(h)),
+                   "npbgb_batch_create")
+        self._h = h
+
+    def replan(self, grids, band_rows=0, band_rows_of=None):
+        """Re-plan this batch for a new grid list, reusing its device buffers."""
+        if self._h is None:
+            raise RuntimeError("batch destroyed")
+        arr = self._structs(grids, band_rows_of)
+        _lib.check(_lib.load().npbgb_batch_replan(self._h, arr, len(grids), int(band_rows)),
+                   "npbgb_batch_replan")
+
+    def _structs(self, grids, band_rows_of):
         import torch
         self._keep = []
         arr = (_lib.Grid * max(1, len(grids)))()
@@ -57,10 +73,7 @@ class Batch:
             g.band_rows = int(band_rows_of(A)) if band_rows_of else 0
             self._keep.append((A, B))
         self.device = self._keep[0][0].device if self._keep else None
-        h = ctypes.c_void_p()
-        _lib.check(_lib.load().npbgb_batch_create(arr, len(grids), int(band_rows), ctypes.byref(h)),
-                   "npbgb_batch_create")
-        self._h = h
+        return arr
 
     def launch(self, graph=False, stream=None):
         import torch

@@ -35,6 +35,8 @@
 namespace npbgb {
 
 extern int64_t g_cfg_f64_emulation;
+extern int64_t g_cfg_jacobi_hw_warps;
+extern int64_t g_cfg_batch_ctas_per_sm;
 
 namespace {
 
@@ -71,10 +73,14 @@ __device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
 // and stores go through L2 (other CTAs wrote, or will read, these rows).
 template <typename T, bool FX>
 __device__ __noinline__ void band_half_sweep(const T* src, T* dst, int64_t nx, int r0, int r1,
-                                             uint32_t one) {
+                                             int hw_warps, uint32_t one) {
   const int warp = threadIdx.x >> 5;
-  for (int64_t k0 = 1 + int64_t(warp) * 32; k0 < nx - 1; k0 += 32 * kBWarps)
-    jcore::strip_rows<T, FX, true, 4>(src, dst, nx, k0, r0, r1, one);
+  for (int64_t k0 = 1 + int64_t(warp) * 32; k0 < nx - 1; k0 += 32 * kBWarps) {
+    if (FX && warp < hw_warps)
+      jcore::strip_rows<T, false, true, 1>(src, dst, nx, k0, r0, r1, one);
+    else
+      jcore::strip_rows<T, FX, true, 4>(src, dst, nx, k0, r0, r1, one);
+  }
 }
 
 // One half-sweep of Heat-3D planes [r0, r1): the CTA walks the plane's
@@ -92,9 +98,13 @@ __device__ __noinline__ void heat_band_half_sweep(const T* src, T* dst, int64_t 
   }
 }
 
-__global__ void __launch_bounds__(kBThreads)
+// MINB: CTAs per SM the register allocation aims for (more CTAs hide more
+// memory latency; fewer registers spill more).
+template <int MINB>
+__global__ void __launch_bounds__(kBThreads, MINB)
 batch_persistent(const BandDesc* __restrict__ bands, uint32_t* done, const int32_t* __restrict__ cta_off,
-                 const int32_t* __restrict__ cta_bands, int f64_emulation, uint32_t one) {
+                 const int32_t* __restrict__ cta_bands, int f64_emulation, int hw_warps,
+                 uint32_t one) {
   __shared__ int s_flag;
   const int tid = threadIdx.x;
   const int b_begin = cta_off[blockIdx.x], b_end = cta_off[blockIdx.x + 1];
@@ -142,13 +152,13 @@ batch_persistent(const BandDesc* __restrict__ bands, uint32_t* done, const int32
         } else if (d.dtype == NPBGB_F64) {
           if (f64_emulation)
             band_half_sweep<double, true>(static_cast<const double*>(src), static_cast<double*>(dst),
-                                          d.n1, d.r0, d.r1, one);
+                                          d.n1, d.r0, d.r1, hw_warps, one);
           else
             band_half_sweep<double, false>(static_cast<const double*>(src), static_cast<double*>(dst),
-                                           d.n1, d.r0, d.r1, one);
+                                           d.n1, d.r0, d.r1, hw_warps, one);
         } else {
           band_half_sweep<float, false>(static_cast<const float*>(src), static_cast<float*>(dst),
-                                        d.n1, d.r0, d.r1, one);
+                                        d.n1, d.r0, d.r1, hw_warps, one);
         }
         __syncthreads();
         if (tid == 0) {
@@ -169,6 +179,13 @@ batch_persistent(const BandDesc* __restrict__ bands, uint32_t* done, const int32
       __nanosleep(200);
     }
   }
+}
+
+using PersistentFn = void (*)(const BandDesc*, uint32_t*, const int32_t*, const int32_t*, int, int,
+                              uint32_t);
+
+PersistentFn persistent_kernel(int ctas_per_sm) {
+  return ctas_per_sm >= 3 ? batch_persistent<3> : batch_persistent<2>;
 }
 
 }  // namespace
@@ -194,6 +211,9 @@ struct npbgb_batch {
   int32_t* d_cta_off = nullptr;
   int32_t* d_cta_bands = nullptr;
   int64_t updates = 0;
+  int64_t cap_bands = 0;  // allocated capacity of d_bands / d_done / d_cta_bands
+  int64_t cap_ctas = 0;   // allocated capacity of d_cta_off
+  int ctas_per_sm = 2;  // persistent kernel variant chosen when planned
   cudaGraphExec_t graph = nullptr;
   cudaStream_t graph_stream = nullptr;
 };
@@ -271,8 +291,9 @@ int32_t launch_batch(npbgb_batch* b, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(b->d_done, 0, sizeof(uint32_t) * size_t(b->nbands), st);
   if (e != cudaSuccess) return cuda_status(e, "batch: reset counters");
   int f64_emul = int(g_cfg_f64_emulation);
+  int hw_warps = int(g_cfg_jacobi_hw_warps >= 0 ? g_cfg_jacobi_hw_warps : 1);
   uint32_t one = 1;
-  void* args[] = {&b->d_bands, &b->d_done, &b->d_cta_off, &b->d_cta_bands, &f64_emul, &one};
+  void* args[] = {&b->d_bands, &b->d_done, &b->d_cta_off, &b->d_cta_bands, &f64_emul, &hw_warps, &one};
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(unsigned(b->nctas));
   cfg.blockDim = dim3(kBThreads);
@@ -282,20 +303,19 @@ int32_t launch_batch(npbgb_batch* b, cudaStream_t st) {
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  e = cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(batch_persistent), args);
+  e = cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(persistent_kernel(b->ctas_per_sm)), args);
   if (e != cudaSuccess) return cuda_status(e, "batch: cooperative launch");
   return NPBGB_OK;
 }
 
 }  // namespace
 
-extern "C" {
+namespace {
 
-int32_t npbgb_batch_create(const npbgb_grid* grids, int64_t count, int32_t band_rows,
-                           npbgb_batch** out) {
+// Plans `grids` into batch b, reusing its device buffers when they are large
+// enough (they grow otherwise).  Invalidates a captured graph.
+int32_t plan_into(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int32_t band_rows) {
   using namespace npbgb;
-  if (!out) return set_error(NPBGB_ERR_ARG, "batch: null output");
-  *out = nullptr;
   if (count < 0 || (count > 0 && !grids)) return set_error(NPBGB_ERR_ARG, "batch: bad grid list");
   if (band_rows < 0) return set_error(NPBGB_ERR_ARG, "batch: band_rows < 0");
   std::vector<BandDesc> bands;
@@ -308,18 +328,14 @@ int32_t npbgb_batch_create(const npbgb_grid* grids, int64_t count, int32_t band_
     if (int64_t(bands.size()) > 0x7fffffff) return set_error(NPBGB_ERR_NOMEM, "batch: too many bands");
     updates += up;
   }
-  auto* b = new (std::nothrow) npbgb_batch();
-  if (!b) return set_error(NPBGB_ERR_NOMEM, "batch: host allocation");
-  cudaGetDevice(&b->device);
-  b->nbands = int64_t(bands.size());
-  b->updates = updates;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_persistent, kBThreads, 0);
+  const int ctas_per_sm = int(g_cfg_batch_ctas_per_sm);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_kernel(ctas_per_sm), kBThreads, 0);
   if (per_sm <= 0) per_sm = 1;
   const int64_t slots = int64_t(sm_count()) * per_sm;
-  b->nctas = int(std::max<int64_t>(1, std::min<int64_t>(slots, b->nbands)));
+  const int nctas = int(std::max<int64_t>(1, std::min<int64_t>(slots, int64_t(bands.size()))));
   // Longest-processing-time greedy assignment of bands to CTAs by work.
-  std::vector<std::vector<int32_t>> lists(size_t(b->nctas));
+  std::vector<std::vector<int32_t>> lists(static_cast<size_t>(nctas));
   {
     std::vector<int32_t> order(bands.size());
     for (size_t i = 0; i < order.size(); ++i) order[i] = int32_t(i);
@@ -327,7 +343,7 @@ int32_t npbgb_batch_create(const npbgb_grid* grids, int64_t count, int32_t band_
     std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return work(x) > work(y); });
     using Item = std::pair<double, int>;
     std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
-    for (int c = 0; c < b->nctas; ++c) heap.push({0.0, c});
+    for (int c = 0; c < nctas; ++c) heap.push({0.0, c});
     for (int32_t i : order) {
       Item it = heap.top();
       heap.pop();
@@ -335,33 +351,81 @@ int32_t npbgb_batch_create(const npbgb_grid* grids, int64_t count, int32_t band_
       heap.push({it.first + work(i), it.second});
     }
   }
-  std::vector<int32_t> off(size_t(b->nctas) + 1, 0), flat;
+  std::vector<int32_t> off(static_cast<size_t>(nctas) + 1, 0), flat;
   flat.reserve(bands.size());
-  for (int c = 0; c < b->nctas; ++c) {
+  for (int c = 0; c < nctas; ++c) {
     off[size_t(c)] = int32_t(flat.size());
     flat.insert(flat.end(), lists[size_t(c)].begin(), lists[size_t(c)].end());
   }
-  off[size_t(b->nctas)] = int32_t(flat.size());
-  auto fail = [&](cudaError_t e, const char* what) {
-    free_batch(b);
-    return cuda_status(e, what);
-  };
-  const size_t nb_alloc = std::max<size_t>(1, bands.size());
+  off[size_t(nctas)] = int32_t(flat.size());
+
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
   cudaError_t e;
-  if ((e = cudaMalloc(&b->d_bands, sizeof(BandDesc) * nb_alloc)) != cudaSuccess) return fail(e, "batch: alloc");
-  if ((e = cudaMalloc(&b->d_done, sizeof(uint32_t) * nb_alloc)) != cudaSuccess) return fail(e, "batch: alloc");
-  if ((e = cudaMalloc(&b->d_cta_off, sizeof(int32_t) * off.size())) != cudaSuccess) return fail(e, "batch: alloc");
-  if ((e = cudaMalloc(&b->d_cta_bands, sizeof(int32_t) * nb_alloc)) != cudaSuccess) return fail(e, "batch: alloc");
+  const int64_t need_bands = std::max<int64_t>(1, int64_t(bands.size()));
+  if (need_bands > b->cap_bands) {
+    cudaFree(b->d_bands);
+    cudaFree(b->d_done);
+    cudaFree(b->d_cta_bands);
+    b->d_bands = nullptr;
+    b->d_done = nullptr;
+    b->d_cta_bands = nullptr;
+    b->cap_bands = 0;
+    if ((e = cudaMalloc(&b->d_bands, sizeof(BandDesc) * size_t(need_bands))) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_done, sizeof(uint32_t) * size_t(need_bands))) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_cta_bands, sizeof(int32_t) * size_t(need_bands))) != cudaSuccess)
+      return cuda_status(e, "batch: alloc");
+    b->cap_bands = need_bands;
+  }
+  if (int64_t(off.size()) > b->cap_ctas) {
+    cudaFree(b->d_cta_off);
+    b->d_cta_off = nullptr;
+    b->cap_ctas = 0;
+    if ((e = cudaMalloc(&b->d_cta_off, sizeof(int32_t) * off.size())) != cudaSuccess)
+      return cuda_status(e, "batch: alloc");
+    b->cap_ctas = int64_t(off.size());
+  }
   if (!bands.empty()) {
-    if ((e = cudaMemcpy(b->d_bands, bands.data(), sizeof(BandDesc) * bands.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
-      return fail(e, "batch: upload");
-    if ((e = cudaMemcpy(b->d_cta_bands, flat.data(), sizeof(int32_t) * flat.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
-      return fail(e, "batch: upload");
+    if ((e = cudaMemcpy(b->d_bands, bands.data(), sizeof(BandDesc) * bands.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(b->d_cta_bands, flat.data(), sizeof(int32_t) * flat.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return cuda_status(e, "batch: upload");
   }
   if ((e = cudaMemcpy(b->d_cta_off, off.data(), sizeof(int32_t) * off.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
-    return fail(e, "batch: upload");
+    return cuda_status(e, "batch: upload");
+  b->nbands = int64_t(bands.size());
+  b->updates = updates;
+  b->nctas = nctas;
+  b->ctas_per_sm = ctas_per_sm;
+  return NPBGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t npbgb_batch_create(const npbgb_grid* grids, int64_t count, int32_t band_rows,
+                           npbgb_batch** out) {
+  using namespace npbgb;
+  if (!out) return set_error(NPBGB_ERR_ARG, "batch: null output");
+  *out = nullptr;
+  auto* b = new (std::nothrow) npbgb_batch();
+  if (!b) return set_error(NPBGB_ERR_NOMEM, "batch: host allocation");
+  cudaGetDevice(&b->device);
+  const int32_t r = plan_into(b, grids, count, band_rows);
+  if (r != NPBGB_OK) {
+    free_batch(b);
+    return r;
+  }
   *out = b;
   return NPBGB_OK;
+}
+
+int32_t npbgb_batch_replan(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int32_t band_rows) {
+  using namespace npbgb;
+  if (!b) return set_error(NPBGB_ERR_ARG, "batch: null handle");
+  return plan_into(b, grids, count, band_rows);
 }
 
 int32_t npbgb_batch_launch(npbgb_batch* b, int32_t use_graph, void* stream) {
@@ -508,7 +572,7 @@ extern "C" int32_t npbgb_batch_run_noalloc(const npbgb_grid* grids, int64_t coun
     e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_status(e, "batch(no-alloc): cudaGetSymbolAddress");
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_persistent, kBThreads, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_persistent<2>, kBThreads, 0);
     if (e != cudaSuccess) return cuda_status(e, "batch(no-alloc): occupancy");
     D.slots = std::max(1, per_sm) * sm_count();
     D.scratch = static_cast<NoAllocLayout*>(ptr);
@@ -555,8 +619,9 @@ extern "C" int32_t npbgb_batch_run_noalloc(const npbgb_grid* grids, int64_t coun
   const int32_t* d_cta_off = S->cta_off;
   const int32_t* d_cta_bands = S->cta_bands;
   int f64_emul = int(g_cfg_f64_emulation);
+  int hw_warps = int(g_cfg_jacobi_hw_warps >= 0 ? g_cfg_jacobi_hw_warps : 1);
   uint32_t one = 1;
-  void* args[] = {&d_bands, &d_done, &d_cta_off, &d_cta_bands, &f64_emul, &one};
+  void* args[] = {&d_bands, &d_done, &d_cta_off, &d_cta_bands, &f64_emul, &hw_warps, &one};
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(unsigned(nctas));
   cfg.blockDim = dim3(kBThreads);
@@ -566,7 +631,7 @@ extern "C" int32_t npbgb_batch_run_noalloc(const npbgb_grid* grids, int64_t coun
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  e = cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(batch_persistent), args);
+  e = cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(batch_persistent<2>), args);
   if (e != cudaSuccess) return cuda_status(e, "batch(no-alloc): cooperative launch");
   return NPBGB_OK;
 }

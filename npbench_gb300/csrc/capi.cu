@@ -17,6 +17,8 @@ int64_t g_cfg_heat_tma = 1;
 int64_t g_cfg_heat_rows = 0;     // 0: per-dtype default
 int64_t g_cfg_heat_hw_rows = -1; // -1: per-kernel default
 int64_t g_cfg_f64_cvt = 0;
+int64_t g_cfg_jacobi_hw_warps = -1;  // -1: default
+int64_t g_cfg_batch_ctas_per_sm = 3;
 int64_t g_cfg_jacobi_chunk = 0;
 
 uint32_t take_heat_device_error();
@@ -124,6 +126,14 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       if (value != 0 && value != 1) return set_error(NPBGB_ERR_ARG, "f64 cvt: 0 or 1");
       g_cfg_f64_cvt = value;
       return NPBGB_OK;
+    case NPBGB_CFG_JACOBI_HW_WARPS:
+      if (value < -1 || value > 8) return set_error(NPBGB_ERR_ARG, "jacobi hw warps: -1 .. 8");
+      g_cfg_jacobi_hw_warps = value;
+      return NPBGB_OK;
+    case NPBGB_CFG_BATCH_CTAS_PER_SM:
+      if (value != 2 && value != 3) return set_error(NPBGB_ERR_ARG, "batch CTAs per SM: 2 or 3");
+      g_cfg_batch_ctas_per_sm = value;
+      return NPBGB_OK;
     default:
       return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
   }
@@ -140,6 +150,8 @@ int32_t npbgb_get_config(int32_t key, int64_t* value) {
     case NPBGB_CFG_HEAT_ROWS: *value = g_cfg_heat_rows; return NPBGB_OK;
     case NPBGB_CFG_HEAT_HW_ROWS: *value = g_cfg_heat_hw_rows; return NPBGB_OK;
     case NPBGB_CFG_F64_CVT: *value = g_cfg_f64_cvt; return NPBGB_OK;
+    case NPBGB_CFG_JACOBI_HW_WARPS: *value = g_cfg_jacobi_hw_warps; return NPBGB_OK;
+    case NPBGB_CFG_BATCH_CTAS_PER_SM: *value = g_cfg_batch_ctas_per_sm; return NPBGB_OK;
     default: return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
   }
 }

@@ -1,50 +1,107 @@
 // Horizontal diffusion with flux limiter (weather_stencils/hdiff/hdiff_numpy.py:5-29).
 //
-// One CTA owns a TI x TJ tile of output columns and 32 consecutive k (the
-// contiguous axis, one k per lane).  It stages, in shared memory,
-//   lap on the (TI+2) x (TJ+2) ring around the tile   (hdiff_numpy.py:7-9)
-//   flx on (TI+1) x TJ,  fly on TI x (TJ+1)            (hdiff_numpy.py:11-25)
-// so each Laplacian and each flux is evaluated once per tile, then writes
-//   out = c - coeff * (((flx[i+1] - flx[i]) + fly[j+1]) - fly[j])   (:27-29)
-// Every operator is one correctly rounded binary64 operation in the
-// reference's order; the limiter keeps the reference's product test
-// `res * grad > 0`, including its underflow and NaN behaviour.
+// In in_field coordinates (x, y) = (i + 2, j + 2), the reference computes
+//   L(x, y)   = 4*in(x,y) - (((in(x+1,y) + in(x-1,y)) + in(x,y+1)) + in(x,y-1))      (:7-9)
+//   F(x, y)   = L(x+1,y) - L(x,y), set to +0 where F * (in(x+1,y) - in(x,y)) > 0  (:11-17)
+//   G(x, y)   = L(x,y+1) - L(x,y), set to +0 where G * (in(x,y+1) - in(x,y)) > 0  (:19-25)
+//   out(x, y) = in(x,y) - coeff * (((F(x,y) - F(x-1,y)) + G(x,y)) - G(x,y-1))     (:27-29)
+// with every operator one correctly rounded binary64 operation.
+//
+// Layout: a CTA owns a kTI x kTJ tile of output columns (x, y) and 32
+// consecutive k (the contiguous axis, one per lane).  It evaluates into
+// shared memory the Laplacian on the (kTI+2) x (kTJ+2) ring around the tile,
+// then F on (kTI+1) x kTJ and G on kTI x (kTJ+1), each once per tile, and
+// writes out.  All points of a stage are independent, which keeps the
+// binary64 pipe fed; two CTA barriers per tile.  (A variant streaming along x
+// with one Laplacian plane per step does fewer redundant Laplacians but
+// serialises three barriers and the binary64 latency per plane; measured
+// slower on GB300.)
+//
+// binary64 work per output point is about 13.5 operations (the binary64 pipe
+// bounds this kernel on GB300):
+// * 4*c - s is one fused multiply-add: 4*c is exact, so fma(4, c, -s) rounds
+//   exactly as the reference's two operations (unless 4*c would overflow,
+//   which takes the two-operation path);
+// * the limiter's test `res * grad > 0` is decided from signs, with no
+//   multiply and no subtraction, whenever the product cannot underflow to
+//   zero (|res| >= 2^-500 or res == 0, and both in values >= 2^-448 in
+//   magnitude or equal); otherwise it is evaluated literally.  Signs give the
+//   same answer for infinities and NaNs (all comparisons with NaN are false);
+//   those comparisons are integer operations on the bit patterns.
 #include "npbgb_common.cuh"
 
 namespace npbgb {
 namespace {
 
 constexpr int kTI = 8, kTJ = 8, kLanes = 32, kRows = 8;
+constexpr int kThreads = kLanes * kRows;
 constexpr int kLapN = (kTI + 2) * (kTJ + 2);
 constexpr int kFlxN = (kTI + 1) * kTJ;
 constexpr int kFlyN = kTI * (kTJ + 1);
 constexpr size_t kSmemBytes = size_t(kLapN + kFlxN + kFlyN) * kLanes * sizeof(double);
 
-__device__ __forceinline__ double limit(double res, double grad) {
-  return (mul_rn(res, grad) > 0.0) ? 0.0 : res;
+__device__ __forceinline__ int64_t bits(double v) { return __double_as_longlong(v); }
+__device__ __forceinline__ uint32_t exp_field(int64_t b) {
+  return static_cast<uint32_t>(static_cast<uint64_t>(b) >> 52) & 0x7ffu;
 }
 
-__global__ void __launch_bounds__(kLanes * kRows)
+// The two-operation forms, kept out of line so that the compiler does not
+// predicate them into the common path (binary64 instructions, predicated or
+// not, occupy GB300's small binary64 pipe).
+__device__ __noinline__ double lap_literal(double c, double s) { return sub_rn(mul_rn(4.0, c), s); }
+__device__ __noinline__ bool product_positive(double res, double hi, double lo) {
+  return mul_rn(res, sub_rn(hi, lo)) > 0.0;
+}
+
+// 4*c - s, rounded as the reference's fl(fl(4*c) - s).
+__device__ __forceinline__ double lap_of(double c, double s) {
+  if (exp_field(bits(c)) < 2044u) return __fma_rn(4.0, c, -s);  // |c| < 2^1021: 4*c exact
+  return lap_literal(c, s);
+}
+
+// res, or +0 where res * (hi - lo) > 0 (the reference's limiter).  When the
+// product can neither underflow to zero nor involve a non-finite value, its
+// sign decides: res != 0 and hi != lo with matching signs.  The comparisons
+// run on the integer pipe: for finite non-zero doubles the key b ^ (b >> 63
+// masked to the magnitude bits) orders as the values do.
+__device__ __forceinline__ double limit(double res, double hi, double lo) {
+  const int64_t br = bits(res), bh = bits(hi), bl = bits(lo);
+  const uint32_t er = exp_field(br), eh = exp_field(bh), el = exp_field(bl);
+  const bool r_zero = (static_cast<uint64_t>(br) << 1) == 0;
+  const bool res_ok = r_zero || (er >= 523u && er <= 2046u);  // 0 or finite, |res| >= 2^-500
+  const bool in_ok = bh == bl || (eh >= 575u && eh <= 2046u && el >= 575u && el <= 2046u);
+  bool positive;
+  if (res_ok && in_ok) {
+    const int64_t kh = bh ^ ((bh >> 63) & 0x7fffffffffffffffll);
+    const int64_t kl = bl ^ ((bl >> 63) & 0x7fffffffffffffffll);
+    positive = !r_zero && ((br > 0 && kh > kl) || (br < 0 && kh < kl));
+  } else {
+    positive = product_positive(res, hi, lo);
+  }
+  return positive ? 0.0 : res;
+}
+
+__global__ void __launch_bounds__(kThreads)
 hdiff_tile(const double* __restrict__ in, double* __restrict__ out,
-           const double* __restrict__ coeff, int64_t I, int64_t J, int64_t K,
-           int64_t tiles_i, int64_t tiles_j) {
+           const double* __restrict__ coeff, int64_t I, int64_t J, int64_t K, int64_t tiles_i,
+           int64_t tiles_j) {
   extern __shared__ double smem[];
   double* lap = smem;                      // [kLapN][kLanes]
   double* flx = lap + kLapN * kLanes;      // [kFlxN][kLanes]
   double* fly = flx + kFlxN * kLanes;      // [kFlyN][kLanes]
 
+  const int lane = threadIdx.x & 31, row = threadIdx.x >> 5;
   int64_t bid = blockIdx.x;
   const int64_t tj = bid % tiles_j;  bid /= tiles_j;
   const int64_t ti = bid % tiles_i;  bid /= tiles_i;
-  const int64_t k = bid * kLanes + threadIdx.x;
+  const int64_t k = bid * kLanes + lane;
   const int64_t i0 = ti * kTI, j0 = tj * kTJ;
   const bool k_ok = k < K;
   const int64_t s0 = (J + 4) * K, s1 = K;
-  // in-field point (x, y) at this lane's k
   auto in_at = [&](int64_t x, int64_t y) -> double { return in[x * s0 + y * s1 + k]; };
 
-  // Laplacian at lap_field[i0 + a, j0 + b] = in-field centre (i0+a+1, j0+b+1).
-  for (int idx = threadIdx.y; idx < kLapN; idx += kRows) {
+  // L at lap_field[i0 + a, j0 + b] = in-field centre (i0+a+1, j0+b+1).
+  for (int idx = row; idx < kLapN; idx += kRows) {
     const int a = idx / (kTJ + 2), b = idx % (kTJ + 2);
     const int64_t x = i0 + a + 1, y = j0 + b + 1;
     double v = 0.0;
@@ -52,48 +109,47 @@ hdiff_tile(const double* __restrict__ in, double* __restrict__ out,
       double nb = add_rn(in_at(x + 1, y), in_at(x - 1, y));
       nb = add_rn(nb, in_at(x, y + 1));
       nb = add_rn(nb, in_at(x, y - 1));
-      v = sub_rn(mul_rn(4.0, in_at(x, y)), nb);
+      v = lap_of(in_at(x, y), nb);
     }
-    lap[idx * kLanes + threadIdx.x] = v;
+    lap[idx * kLanes + lane] = v;
   }
   __syncthreads();
 
-  // flx_field[i0 + a, j0 + b] = lap[a+1][b+1] - lap[a][b+1], limited by
+  // F at flx_field[i0 + a, j0 + b]: lap[a+1][b+1] - lap[a][b+1], limited by
   // in(i0+a+2, j0+b+2) - in(i0+a+1, j0+b+2).
-  for (int idx = threadIdx.y; idx < kFlxN; idx += kRows) {
+  for (int idx = row; idx < kFlxN; idx += kRows) {
     const int a = idx / kTJ, b = idx % kTJ;
     const int64_t x = i0 + a + 1, y = j0 + b + 2;
     double v = 0.0;
     if (k_ok && i0 + a < I + 1 && j0 + b < J) {
-      const double res = sub_rn(lap[((a + 1) * (kTJ + 2) + b + 1) * kLanes + threadIdx.x],
-                                lap[(a * (kTJ + 2) + b + 1) * kLanes + threadIdx.x]);
-      v = limit(res, sub_rn(in_at(x + 1, y), in_at(x, y)));
+      const double res = sub_rn(lap[((a + 1) * (kTJ + 2) + b + 1) * kLanes + lane],
+                                lap[(a * (kTJ + 2) + b + 1) * kLanes + lane]);
+      v = limit(res, in_at(x + 1, y), in_at(x, y));
     }
-    flx[idx * kLanes + threadIdx.x] = v;
+    flx[idx * kLanes + lane] = v;
   }
-  // fly_field[i0 + a, j0 + b] = lap[a+1][b+1] - lap[a+1][b], limited by
+  // G at fly_field[i0 + a, j0 + b]: lap[a+1][b+1] - lap[a+1][b], limited by
   // in(i0+a+2, j0+b+2) - in(i0+a+2, j0+b+1).
-  for (int idx = threadIdx.y; idx < kFlyN; idx += kRows) {
+  for (int idx = row; idx < kFlyN; idx += kRows) {
     const int a = idx / (kTJ + 1), b = idx % (kTJ + 1);
     const int64_t x = i0 + a + 2, y = j0 + b + 1;
     double v = 0.0;
     if (k_ok && i0 + a < I && j0 + b < J + 1) {
-      const double res = sub_rn(lap[((a + 1) * (kTJ + 2) + b + 1) * kLanes + threadIdx.x],
-                                lap[((a + 1) * (kTJ + 2) + b) * kLanes + threadIdx.x]);
-      v = limit(res, sub_rn(in_at(x, y + 1), in_at(x, y)));
+      const double res = sub_rn(lap[((a + 1) * (kTJ + 2) + b + 1) * kLanes + lane],
+                                lap[((a + 1) * (kTJ + 2) + b) * kLanes + lane]);
+      v = limit(res, in_at(x, y + 1), in_at(x, y));
     }
-    fly[idx * kLanes + threadIdx.x] = v;
+    fly[idx * kLanes + lane] = v;
   }
   __syncthreads();
 
-  for (int idx = threadIdx.y; idx < kTI * kTJ; idx += kRows) {
+  for (int idx = row; idx < kTI * kTJ; idx += kRows) {
     const int a = idx / kTJ, b = idx % kTJ;
     const int64_t i = i0 + a, j = j0 + b;
     if (!k_ok || i >= I || j >= J) continue;
-    double div = sub_rn(flx[((a + 1) * kTJ + b) * kLanes + threadIdx.x],
-                        flx[(a * kTJ + b) * kLanes + threadIdx.x]);
-    div = add_rn(div, fly[(a * (kTJ + 1) + b + 1) * kLanes + threadIdx.x]);
-    div = sub_rn(div, fly[(a * (kTJ + 1) + b) * kLanes + threadIdx.x]);
+    double div = sub_rn(flx[((a + 1) * kTJ + b) * kLanes + lane], flx[(a * kTJ + b) * kLanes + lane]);
+    div = add_rn(div, fly[(a * (kTJ + 1) + b + 1) * kLanes + lane]);
+    div = sub_rn(div, fly[(a * (kTJ + 1) + b) * kLanes + lane]);
     const int64_t o = (i * J + j) * K + k;
     out[o] = sub_rn(in_at(i + 2, j + 2), mul_rn(coeff[o], div));
   }
@@ -121,7 +177,7 @@ extern "C" int32_t npbgb_hdiff(const void* in_field, void* out_field, const void
     if (e != cudaSuccess) return cuda_status(e, "hdiff: smem attribute");
     attr_set = true;
   }
-  hdiff_tile<<<unsigned(blocks), dim3(kLanes, kRows), kSmemBytes, as_stream(stream)>>>(
+  hdiff_tile<<<unsigned(blocks), kThreads, kSmemBytes, as_stream(stream)>>>(
       static_cast<const double*>(in_field), static_cast<double*>(out_field),
       static_cast<const double*>(coeff), I, J, K, tiles_i, tiles_j);
   NPBGB_CHECK_LAUNCH("hdiff_tile");

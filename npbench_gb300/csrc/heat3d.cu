@@ -161,16 +161,22 @@ heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ sr
     }
     if (tid == 0 && m - 1 + kStages < Q) issue(m - 1 + kStages);  // refills the buffer of plane m-1
     const int64_t i = ib + m;
+    // This warp's rows row0 .. row0+R-1; the column of plane i for rows
+    // row0-1 .. row0+R is read once and reused as the rows' j-neighbours.
+    const int row0 = ty * R;
+    const S* pm = stage_ptr(m);
+    const S* pc = stage_ptr(m + 1);
+    const S* pp = stage_ptr(m + 2);
+    S col[R + 2];
+#pragma unroll
+    for (int r = 0; r < R + 2; ++r) col[r] = pc[(row0 + r) * G::BX + tx + 1];
+    const int64_t gbase = i * s0 + (j0 + row0) * s1 + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      const int row = ty + kTJ * r;
-      const int64_t j = j0 + row;
-      if (!k_ok || j >= n1 - 1) continue;
+      const int row = row0 + r;
+      if (!k_ok || j0 + row >= n1 - 1) continue;
       const int off = (row + 1) * G::BX + (tx + 1);
-      const S* pm = stage_ptr(m) + off;
-      const S* pc = stage_ptr(m + 1) + off;
-      const S* pp = stage_ptr(m + 2) + off;
-      const int64_t g = i * s0 + j * s1 + k;
+      const int64_t g = gbase + r * s1;
       const T* q = src + g;
       T out;
       if constexpr (FX) {
@@ -178,8 +184,8 @@ heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ sr
         if (hw) {
           out = heat_point<T>(q[0], q[s0], q[-s0], q[s1], q[-s1], q[1], q[-1]);
         } else {
-          const int64_t c = pc[0], ip = pp[0], im = pm[0], jp = pc[G::BX], jm = pc[-G::BX],
-                        kp = pc[1], km = pc[-1];
+          const int64_t c = col[r + 1], ip = pp[off], im = pm[off], jp = col[r + 2], jm = col[r],
+                        kp = pc[off + 1], km = pc[off - 1];
           const uint32_t tag =
               hi32(c) | hi32(ip) | hi32(im) | hi32(jp) | hi32(jm) | hi32(kp) | hi32(km);
           if (!(tag & kPoisonHi))
@@ -188,7 +194,8 @@ heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ sr
             out = heat_point<T>(q[0], q[s0], q[-s0], q[s1], q[-s1], q[1], q[-1]);
         }
       } else {
-        out = heat_point<T>(pc[0], pp[0], pm[0], pc[G::BX], pc[-G::BX], pc[1], pc[-1]);
+        out = heat_point<T>(col[r + 1], pp[off], pm[off], col[r + 2], col[r], pc[off + 1],
+                            pc[off - 1]);
       }
       dst[g] = out;
     }

@@ -1,0 +1,94 @@
+// 1D 3-point Jacobi time loop (polybench/jacobi_1d/jacobi_1d_numpy.py:4-8).
+//
+// Per interior point, in the reference's order:
+//   dst[i] = 0.33333 * ((src[i-1] + src[i]) + src[i+1])
+// for t in 1..TSTEPS-1: A -> B, then B -> A.
+//
+// The arrays are small (NPBench's presets go up to 34000 points), so a plain
+// one-launch-per-half-sweep loop is bound by launch latency.  Instead each
+// launch performs kSteps half-sweeps with temporal blocking: a CTA stages its
+// segment of kW points plus kSteps halo points on each side into shared
+// memory, runs the half-sweeps there (the valid region shrinks by one point
+// per side and half-sweep, so every kept value is computed exactly as the
+// reference computes it), and writes back its segment of both arrays: A
+// holds the state after the launch's last half-sweep and B the one before,
+// exactly what the reference leaves after the same number of half-sweeps.
+// Points 0 and n-1 are never written, in either array.
+#include "npbgb_common.cuh"
+
+namespace npbgb {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kW = 1024;              // segment written per CTA
+constexpr int kSteps = 32;            // half-sweeps per launch (even)
+constexpr int kSpan = kW + 2 * kSteps;  // staged points per CTA
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+jacobi1d_block(T* __restrict__ a, T* __restrict__ b, int64_t n, int steps) {
+  __shared__ T buf[2][kSpan];
+  const T k = T(0.33333);
+  const int64_t seg = int64_t(blockIdx.x) * kW;       // first written point - 1 (interior starts at 1)
+  const int64_t base = 1 + seg - kSteps;              // global index of buf[.][0]
+  // Stage A (state h) into buf[0] and B into buf[1]; points outside [0, n) are unused.
+  for (int q = threadIdx.x; q < kSpan; q += kThreads) {
+    const int64_t g = base + q;
+    const bool in = g >= 0 && g < n;
+    buf[0][q] = in ? a[g] : T(0);
+    buf[1][q] = in ? b[g] : T(0);
+  }
+  __syncthreads();
+  // Half-sweep s reads buf[s & 1] and writes buf[(s + 1) & 1] for local points
+  // q in [s + 1, kSpan - 1 - s) whose global index is an interior point.
+  for (int s = 0; s < steps; ++s) {
+    const T* src = buf[s & 1];
+    T* dst = buf[(s + 1) & 1];
+    for (int q = s + 1 + threadIdx.x; q < kSpan - 1 - s; q += kThreads) {
+      const int64_t g = base + q;
+      if (g >= 1 && g < n - 1) dst[q] = mul_rn(k, add_rn(add_rn(src[q - 1], src[q]), src[q + 1]));
+    }
+    __syncthreads();
+  }
+  // steps is even: buf[0] holds the newest field (A) and buf[1] the one before (B).
+  for (int q = kSteps + threadIdx.x; q < kSteps + kW; q += kThreads) {
+    const int64_t g = base + q;
+    if (g >= 1 && g < n - 1) {
+      a[g] = buf[0][q];
+      b[g] = buf[1][q];
+    }
+  }
+}
+
+template <typename T>
+int32_t run(T* a, T* b, int64_t n, int32_t tsteps, cudaStream_t st) {
+  if (tsteps <= 1 || n < 3) return NPBGB_OK;
+  const int64_t blocks = cdiv(n - 2, kW);
+  if (blocks > 0x7fffffff) return set_error(NPBGB_ERR_ARG, "jacobi1d: extent too large");
+  int64_t left = 2 * int64_t(tsteps - 1);  // half-sweeps, even
+  while (left > 0) {
+    const int s = int(left < kSteps ? left : kSteps);
+    jacobi1d_block<T><<<unsigned(blocks), kThreads, 0, st>>>(a, b, n, s);
+    left -= s;
+  }
+  NPBGB_CHECK_LAUNCH("jacobi1d_block");
+  return NPBGB_OK;
+}
+
+}  // namespace
+}  // namespace npbgb
+
+extern "C" int32_t npbgb_jacobi1d(void* A, void* B, int64_t n, int32_t tsteps, int32_t dtype,
+                                  void* stream) {
+  using namespace npbgb;
+  if (n < 0) return set_error(NPBGB_ERR_ARG, "jacobi1d: negative extent");
+  if (tsteps > 1 && n >= 3) {
+    if (!A || !B) return set_error(NPBGB_ERR_ARG, "jacobi1d: null array");
+    if (A == B) return set_error(NPBGB_ERR_ARG, "jacobi1d: A and B alias");
+  }
+  if (dtype == NPBGB_F64)
+    return run<double>(static_cast<double*>(A), static_cast<double*>(B), n, tsteps, as_stream(stream));
+  if (dtype == NPBGB_F32)
+    return run<float>(static_cast<float*>(A), static_cast<float*>(B), n, tsteps, as_stream(stream));
+  return set_error(NPBGB_ERR_DTYPE, "jacobi1d: dtype %d", dtype);
+}

@@ -20,23 +20,31 @@ namespace npbgb {
 
 extern int64_t g_cfg_f64_emulation;
 extern int64_t g_cfg_jacobi_chunk;
+extern int64_t g_cfg_jacobi_hw_warps;
 
 namespace {
 
 constexpr int kWarps = 8;
 constexpr int kUnroll = 4;
 
-// Grid: x over groups of kWarps column strips, y over chunks of rows.
+// Grid: x over groups of kWarps column strips, y over chunks of rows.  With
+// FX, warps below hw_warps take the hardware binary64 path so that the
+// binary64 pipe works next to the integer pipe (same results either way).
 template <typename T, bool FX>
 __global__ void __launch_bounds__(32 * kWarps)
 jacobi2d_strip(const T* __restrict__ src, T* __restrict__ dst, int64_t ny, int64_t nx, int chunk,
-               uint32_t one) {
+               int hw_warps, uint32_t one) {
   const int warp = threadIdx.x >> 5;
   const int64_t k0 = 1 + (int64_t(blockIdx.x) * kWarps + warp) * 32;
   if (k0 >= nx - 1) return;  // whole strip outside the interior (warp-uniform)
   const int64_t ib = 1 + int64_t(blockIdx.y) * chunk;
   const int64_t ie = (ib + chunk < ny - 1) ? ib + chunk : ny - 1;
-  jcore::strip_rows<T, FX, false, kUnroll>(src, dst, nx, k0, ib, ie, one);
+  // Rows loaded ahead: 4 for the memory-bound forms; 1 for the fixed-point
+  // form, which is integer-pipe bound and wants the registers for occupancy.
+  if (FX && warp < hw_warps)
+    jcore::strip_rows<T, false, false, 1>(src, dst, nx, k0, ib, ie, one);
+  else
+    jcore::strip_rows<T, FX, false, FX ? 1 : kUnroll>(src, dst, nx, k0, ib, ie, one);
 }
 
 int pick_chunk(int64_t ny, int64_t col_blocks) {
@@ -58,9 +66,10 @@ int32_t run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st)
   const int64_t gy = cdiv(ny - 2, chunk);
   if (gx > 0x7fffffff || gy > 65535) return set_error(NPBGB_ERR_ARG, "jacobi2d: extent too large");
   const dim3 grid{unsigned(gx), unsigned(gy)};
+  const int hw = int(g_cfg_jacobi_hw_warps >= 0 ? g_cfg_jacobi_hw_warps : 1);
   for (int32_t t = 1; t < tsteps; ++t) {
-    jacobi2d_strip<T, FX><<<grid, 32 * kWarps, 0, st>>>(a, b, ny, nx, chunk, 1u);
-    jacobi2d_strip<T, FX><<<grid, 32 * kWarps, 0, st>>>(b, a, ny, nx, chunk, 1u);
+    jacobi2d_strip<T, FX><<<grid, 32 * kWarps, 0, st>>>(a, b, ny, nx, chunk, hw, 1u);
+    jacobi2d_strip<T, FX><<<grid, 32 * kWarps, 0, st>>>(b, a, ny, nx, chunk, hw, 1u);
   }
   NPBGB_CHECK_LAUNCH("jacobi2d_strip");
   return NPBGB_OK;

@@ -11,6 +11,8 @@ Adds, under NPBENCH_ROOT (the directory holding ``framework_info/``,
 * ``npbench/benchmarks/polybench/jacobi_2d/jacobi_2d_gb300.py``
 * ``npbench/benchmarks/polybench/heat_3d/heat_3d_gb300.py``
 * ``npbench/benchmarks/weather_stencils/hdiff/hdiff_gb300.py``
+* ``npbench/benchmarks/polybench/jacobi_1d/jacobi_1d_gb300.py``
+* ``npbench/benchmarks/polybench/fdtd_2d/fdtd_2d_gb300.py``
 
 and appends ``from .gb300_framework import *`` to
 ``npbench/infrastructure/__init__.py`` (once).  ``--copy-from`` first copies a
@@ -30,6 +32,8 @@ FILES = [
     "benchmarks/polybench/jacobi_2d/jacobi_2d_gb300.py",
     "benchmarks/polybench/heat_3d/heat_3d_gb300.py",
     "benchmarks/weather_stencils/hdiff/hdiff_gb300.py",
+    "benchmarks/polybench/jacobi_1d/jacobi_1d_gb300.py",
+    "benchmarks/polybench/fdtd_2d/fdtd_2d_gb300.py",
 ]
 IMPORT_LINE = "from .gb300_framework import *\n"
 

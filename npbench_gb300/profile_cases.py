@@ -1,0 +1,66 @@
+"""Small single-kernel cases for ncu captures.
+
+    python -m npbench_gb300.profile_cases <case>
+
+Each case runs one kernel family on an input still larger than L2 where the
+real workload is, with few launches, so that one capture
+(``ncu --set full -k regex:<kernel> -s <n> -c 1``) ends in seconds:
+
+========== ============================================== ===================
+case       what                                           kernel to capture
+========== ============================================== ===================
+heat_f64   Heat-3D 256^3 float64, TSTEPS=3 (4 launches)   heat3d_tma, -s 2
+heat_f32   Heat-3D 256^3 float32, TSTEPS=3                heat3d_tma, -s 2
+jacobi_f64 Jacobi-2D 4096^2 float64, TSTEPS=3             jacobi2d_strip, -s 2
+jacobi_f32 Jacobi-2D 4096^2 float32, TSTEPS=3             jacobi2d_strip, -s 2
+hdiff      hdiff 256x256x160 float64, 3 calls             hdiff_tile, -s 1
+batch      256 mixed Jacobi-2D grids, 2 launches          batch_persistent, -s 1
+========== ============================================== ===================
+"""
+import sys
+
+import numpy as np
+
+
+def run(case):
+    import torch
+
+    from npbench_gb300 import _lib, stencils, workloads
+    dev = torch.device("cuda", 0)
+    if case in ("heat_f64", "heat_f32"):
+        dt = np.float64 if case.endswith("64") else np.float32
+        A, B = workloads.uniform_heat((256,) * 3, dt, seed=0)
+        a, b = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+        stencils.heat_3d_kernel(3, a, b)
+    elif case in ("jacobi_f64", "jacobi_f32"):
+        dt = np.float64 if case.endswith("64") else np.float32
+        A, B = workloads.uniform_pair((4096, 4096), dt, seed=0)
+        a, b = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+        stencils.jacobi_2d_kernel(3, a, b)
+    elif case == "hdiff":
+        inf, out, co = workloads.init_hdiff(256, 256, 160)
+        x, y, z = (torch.from_numpy(t).to(dev) for t in (inf, out, co))
+        for _ in range(3):
+            stencils.hdiff(x, y, z)
+    elif case == "batch":
+        from npbench_gb300.batch import Batch
+        specs = workloads.batch_jacobi_specs(256, seed=0, tsteps=(10, 40))
+        g = torch.Generator(device=dev)
+        g.manual_seed(0)
+        work = []
+        for (ny, nx), dtp, T in specs:
+            tdt = torch.float64 if dtp == np.float64 else torch.float32
+            work.append((torch.rand((ny, nx), dtype=tdt, device=dev, generator=g),
+                         torch.rand((ny, nx), dtype=tdt, device=dev, generator=g), T))
+        with Batch(work, band_rows=64) as bt:
+            bt.launch()
+            bt.launch()
+    else:
+        raise SystemExit(f"unknown case {case!r}")
+    torch.cuda.synchronize()
+    _lib.device_status()
+    print("ok", case)
+
+
+if __name__ == "__main__":
+    run(sys.argv[1])

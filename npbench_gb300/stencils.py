@@ -5,6 +5,8 @@ These are drop-ins for the reference NumPy kernels:
 * ``jacobi_2d_kernel(TSTEPS, A, B)``   -- polybench/jacobi_2d/jacobi_2d_numpy.py:4
 * ``heat_3d_kernel(TSTEPS, A, B)``     -- polybench/heat_3d/heat_3d_numpy.py:4
 * ``hdiff(in_field, out_field, coeff)`` -- weather_stencils/hdiff/hdiff_numpy.py:5
+* ``jacobi_1d_kernel(TSTEPS, A, B)``   -- polybench/jacobi_1d/jacobi_1d_numpy.py:4
+* ``fdtd_2d_kernel(TMAX, ex, ey, hz, _fict_)`` -- polybench/fdtd_2d/fdtd_2d_numpy.py:4
 
 Arguments are updated in place and nothing is returned, as in the reference.
 They may be
@@ -24,7 +26,7 @@ import numpy as np
 
 from . import _lib
 
-__all__ = ["jacobi_2d_kernel", "heat_3d_kernel", "hdiff"]
+__all__ = ["jacobi_2d_kernel", "heat_3d_kernel", "hdiff", "jacobi_1d_kernel", "fdtd_2d_kernel"]
 
 
 def _torch():
@@ -167,4 +169,34 @@ def hdiff(in_field, out_field, coeff):
     with torch.cuda.device(view.device):
         st = lib.npbgb_hdiff(view.ptr(0), view.ptr(1), view.ptr(2), I, J, K, code, view.stream)
         _lib.check(st, "hdiff")
+        view.finish()
+
+
+def jacobi_1d_kernel(TSTEPS, A, B):
+    """``kernel(TSTEPS, A, B)`` of polybench/jacobi_1d/jacobi_1d_numpy.py:4-8, on the GPU."""
+    _pingpong("jacobi_1d", lambda lib: lib.npbgb_jacobi1d, 1, TSTEPS, A, B)
+
+
+def fdtd_2d_kernel(TMAX, ex, ey, hz, _fict_):
+    """``kernel(TMAX, ex, ey, hz, _fict_)`` of polybench/fdtd_2d/fdtd_2d_numpy.py:4-11."""
+    _check_same((ex, ey, hz), ("ex", "ey", "hz"))
+    if len(ex.shape) != 2:
+        raise ValueError(f"fdtd_2d: expected 2-D fields, got shape {tuple(ex.shape)}")
+    if len(_fict_.shape) != 1 or _fict_.dtype != ex.dtype:
+        raise TypeError("fdtd_2d: _fict_ must be 1-D with the fields' dtype")
+    T = int(TMAX)
+    if T > _fict_.shape[0]:
+        raise IndexError(f"fdtd_2d: _fict_ has {_fict_.shape[0]} entries, TMAX is {T}")
+    for x, y, nx, ny in (("ex", "ey", ex, ey), ("ex", "hz", ex, hz), ("ey", "hz", ey, hz)):
+        if _shares_memory(nx, ny):
+            raise ValueError(f"fdtd_2d: {x} and {y} share memory")
+    code = _dtype_code(ex.dtype)
+    lib = _lib.load()
+    torch = _torch()
+    view = _DeviceView((ex, ey, hz, _fict_), (True, True, True, False))
+    with torch.cuda.device(view.device):
+        st = lib.npbgb_fdtd2d(view.ptr(0), view.ptr(1), view.ptr(2), view.ptr(3),
+                              int(_fict_.shape[0]), int(ex.shape[0]), int(ex.shape[1]), T, code,
+                              view.stream)
+        _lib.check(st, "fdtd_2d")
         view.finish()

@@ -20,6 +20,11 @@ PRESETS = {
                 "L": {"TSTEPS": 100, "N": 70}, "paper": {"TSTEPS": 500, "N": 120}},
     "hdiff": {"S": {"I": 64, "J": 64, "K": 60}, "M": {"I": 128, "J": 128, "K": 160},
               "L": {"I": 384, "J": 384, "K": 160}, "paper": {"I": 256, "J": 256, "K": 160}},
+    "jacobi_1d": {"S": {"TSTEPS": 800, "N": 3200}, "M": {"TSTEPS": 3000, "N": 12000},
+                  "L": {"TSTEPS": 8500, "N": 34000}, "paper": {"TSTEPS": 4000, "N": 32000}},
+    "fdtd_2d": {"S": {"TMAX": 20, "NX": 200, "NY": 220}, "M": {"TMAX": 60, "NX": 400, "NY": 450},
+                "L": {"TMAX": 150, "NX": 800, "NY": 900},
+                "paper": {"TMAX": 500, "NX": 1000, "NY": 1200}},
 }
 
 
@@ -32,6 +37,23 @@ def init_jacobi_2d(N, dtype=np.float64):
 def init_heat_3d(N, dtype=np.float64):
     A = np.fromfunction(lambda i, j, k: (i + j + (N - k)) * 10 / N, (N, N, N), dtype=dtype)
     return A, np.copy(A)
+
+
+def init_jacobi_1d(N, dtype=np.float64):
+    """polybench/jacobi_1d/jacobi_1d.py:6-10: A = (i+2)/N, B = (i+3)/N."""
+    A = np.fromfunction(lambda i: (i + 2) / N, (N,), dtype=dtype)
+    B = np.fromfunction(lambda i: (i + 3) / N, (N,), dtype=dtype)
+    return A, B
+
+
+def init_fdtd_2d(TMAX, NX, NY, dtype=np.float64):
+    """polybench/fdtd_2d/fdtd_2d.py:6-17: ex = i(j+1)/NX, ey = i(j+2)/NY,
+    hz = i(j+3)/NX, _fict_ = i."""
+    ex = np.fromfunction(lambda i, j: (i * (j + 1)) / NX, (NX, NY), dtype=dtype)
+    ey = np.fromfunction(lambda i, j: (i * (j + 2)) / NY, (NX, NY), dtype=dtype)
+    hz = np.fromfunction(lambda i, j: (i * (j + 3)) / NX, (NX, NY), dtype=dtype)
+    fict = np.fromfunction(lambda i: i, (TMAX,), dtype=dtype)
+    return ex, ey, hz, fict
 
 
 def init_hdiff(I, J, K):

@@ -7,6 +7,8 @@ with the same call shapes as the reference kernels:
 * ``jacobi_2d_kernel(TSTEPS, A, B)``   -- polybench/jacobi_2d/jacobi_2d_numpy.py:4
 * ``heat_3d_kernel(TSTEPS, A, B)``     -- polybench/heat_3d/heat_3d_numpy.py:4
 * ``hdiff(in_field, out_field, coeff)`` -- weather_stencils/hdiff/hdiff_numpy.py:5
+* ``jacobi_1d_kernel(TSTEPS, A, B)``   -- polybench/jacobi_1d/jacobi_1d_numpy.py:4
+* ``fdtd_2d_kernel(TMAX, ex, ey, hz, _fict_)`` -- polybench/fdtd_2d/fdtd_2d_numpy.py:4
 """
 import ctypes
 import os
@@ -36,6 +38,9 @@ def _bind(lib):
         getattr(lib, "oracle_heat3d_" + sfx).argtypes = [vp, vp, i64, i64, i64, i32]
         getattr(lib, "oracle_heat3d_half_" + sfx).argtypes = [vp, vp, i64, i64, i64]
     lib.oracle_hdiff_f64.argtypes = [vp, vp, vp, i64, i64, i64]
+    for sfx in ("f64", "f32"):
+        getattr(lib, "oracle_jacobi1d_" + sfx).argtypes = [vp, vp, i64, i32]
+        getattr(lib, "oracle_fdtd2d_" + sfx).argtypes = [vp, vp, vp, vp, i64, i64, i32]
     return lib
 
 
@@ -90,3 +95,16 @@ def hdiff(in_field, out_field, coeff):
     if in_field.shape != (I + 4, J + 4, K) or coeff.shape != (I, J, K):
         raise ValueError("hdiff shapes: in (I+4, J+4, K), out/coeff (I, J, K)")
     lib().oracle_hdiff_f64(_p(in_field), _p(out_field), _p(coeff), I, J, K)
+
+
+def jacobi_1d_kernel(TSTEPS, A, B):
+    sfx = _sfx(A, B)
+    getattr(lib(), "oracle_jacobi1d_" + sfx)(_p(A), _p(B), A.shape[0], int(TSTEPS))
+
+
+def fdtd_2d_kernel(TMAX, ex, ey, hz, _fict_):
+    sfx = _sfx(ex, ey, hz, _fict_)
+    if int(TMAX) > _fict_.shape[0]:
+        raise ValueError("_fict_ shorter than TMAX")
+    getattr(lib(), "oracle_fdtd2d_" + sfx)(_p(ex), _p(ey), _p(hz), _p(_fict_), ex.shape[0],
+                                          ex.shape[1], int(TMAX))

@@ -137,3 +137,46 @@ void oracle_hdiff_f64(const double* in, double* out, const double* coeff,
     }
   }
 }
+
+/* jacobi_1d: polybench/jacobi_1d/jacobi_1d_numpy.py:4-8
+ *   dst[i] = 0.33333 * ((src[i-1] + src[i]) + src[i+1]),  A -> B then B -> A. */
+#define DEF_JACOBI1D(T, SUFFIX, K)                                              \
+  void oracle_jacobi1d_##SUFFIX(T* a, T* b, int64_t n, int32_t tsteps) {        \
+    if (n < 3) return;                                                         \
+    for (int32_t t = 1; t < tsteps; ++t) {                                     \
+      for (int64_t i = 1; i < n - 1; ++i) b[i] = K * ((a[i - 1] + a[i]) + a[i + 1]); \
+      for (int64_t i = 1; i < n - 1; ++i) a[i] = K * ((b[i - 1] + b[i]) + b[i + 1]); \
+    }                                                                          \
+  }
+DEF_JACOBI1D(double, f64, 0.33333)
+DEF_JACOBI1D(float, f32, 0.33333f)
+
+/* fdtd_2d: polybench/fdtd_2d/fdtd_2d_numpy.py:4-11, (nx, ny) arrays, per step:
+ *   ey[0,:] = fict[t]; ey[i,j] -= 0.5 * (hz[i,j] - hz[i-1,j])  (i >= 1);
+ *   ex[i,j] -= 0.5 * (hz[i,j] - hz[i,j-1])  (j >= 1);
+ *   hz[i,j] -= 0.7 * (((ex[i,j+1] - ex[i,j]) + ey[i+1,j]) - ey[i,j])  (i < nx-1, j < ny-1). */
+#define DEF_FDTD(T, SUFFIX, HALF, C07)                                          \
+  void oracle_fdtd2d_##SUFFIX(T* ex, T* ey, T* hz, const T* fict, int64_t nx,    \
+                              int64_t ny, int32_t tmax) {                       \
+    for (int32_t t = 0; t < tmax; ++t) {                                       \
+      for (int64_t j = 0; j < ny; ++j) ey[j] = fict[t];                        \
+      _Pragma("omp parallel for schedule(static)")                             \
+      for (int64_t i = 1; i < nx; ++i)                                         \
+        for (int64_t j = 0; j < ny; ++j)                                       \
+          ey[i * ny + j] = ey[i * ny + j] - HALF * (hz[i * ny + j] - hz[(i - 1) * ny + j]); \
+      _Pragma("omp parallel for schedule(static)")                             \
+      for (int64_t i = 0; i < nx; ++i)                                         \
+        for (int64_t j = 1; j < ny; ++j)                                       \
+          ex[i * ny + j] = ex[i * ny + j] - HALF * (hz[i * ny + j] - hz[i * ny + j - 1]); \
+      _Pragma("omp parallel for schedule(static)")                             \
+      for (int64_t i = 0; i < nx - 1; ++i)                                     \
+        for (int64_t j = 0; j < ny - 1; ++j) {                                 \
+          T d = ex[i * ny + j + 1] - ex[i * ny + j];                           \
+          d = d + ey[(i + 1) * ny + j];                                        \
+          d = d - ey[i * ny + j];                                              \
+          hz[i * ny + j] = hz[i * ny + j] - C07 * d;                           \
+        }                                                                      \
+    }                                                                          \
+  }
+DEF_FDTD(double, f64, 0.5, 0.7)
+DEF_FDTD(float, f32, 0.5f, 0.7f)

@@ -21,7 +21,7 @@ Evaluation orders restated here:
 import numpy as np
 
 __all__ = ["jacobi_2d_kernel", "heat_3d_kernel", "hdiff", "jacobi_2d_half_sweep",
-           "heat_3d_half_sweep"]
+           "heat_3d_half_sweep", "jacobi_1d_kernel", "fdtd_2d_kernel"]
 
 
 def jacobi_2d_half_sweep(src, dst):
@@ -117,3 +117,43 @@ def hdiff(in_field, out_field, coeff):
     np.subtract(div, fly[:, :-1, :], out=div)
     np.multiply(coeff, div, out=div)
     np.subtract(f[2:I + 2, 2:J + 2, :], div, out=out_field)
+
+
+def jacobi_1d_kernel(TSTEPS, A, B):
+    """``kernel(TSTEPS, A, B)`` of polybench/jacobi_1d/jacobi_1d_numpy.py:4-8.
+
+    dst[1:-1] = 0.33333 * ((src[:-2] + src[1:-1]) + src[2:]), A->B then B->A.
+    """
+    k = A.dtype.type(0.33333)
+
+    def half(src, dst):
+        acc = np.add(src[:-2], src[1:-1])
+        np.add(acc, src[2:], out=acc)
+        np.multiply(k, acc, out=dst[1:-1])
+
+    for _ in range(1, TSTEPS):
+        half(A, B)
+        half(B, A)
+
+
+def fdtd_2d_kernel(TMAX, ex, ey, hz, _fict_):
+    """``kernel(TMAX, ex, ey, hz, _fict_)`` of polybench/fdtd_2d/fdtd_2d_numpy.py:4-11.
+
+    Per step, in place and in this order: ey[0,:] = fict[t];
+    ey[1:,:] -= 0.5 * (hz[1:,:] - hz[:-1,:]); ex[:,1:] -= 0.5 * (hz[:,1:] - hz[:,:-1]);
+    hz[:-1,:-1] -= 0.7 * (((ex[:-1,1:] - ex[:-1,:-1]) + ey[1:,:-1]) - ey[:-1,:-1]).
+    """
+    half, c07 = ex.dtype.type(0.5), ex.dtype.type(0.7)
+    for t in range(TMAX):
+        ey[0, :] = _fict_[t]
+        d = np.subtract(hz[1:, :], hz[:-1, :])
+        np.multiply(half, d, out=d)
+        np.subtract(ey[1:, :], d, out=ey[1:, :])
+        d = np.subtract(hz[:, 1:], hz[:, :-1])
+        np.multiply(half, d, out=d)
+        np.subtract(ex[:, 1:], d, out=ex[:, 1:])
+        d = np.subtract(ex[:-1, 1:], ex[:-1, :-1])
+        np.add(d, ey[1:, :-1], out=d)
+        np.subtract(d, ey[:-1, :-1], out=d)
+        np.multiply(c07, d, out=d)
+        np.subtract(hz[:-1, :-1], d, out=hz[:-1, :-1])

@@ -57,6 +57,8 @@ def main():
     from npbench.benchmarks.polybench.jacobi_2d import jacobi_2d_numpy, jacobi_2d
     from npbench.benchmarks.polybench.heat_3d import heat_3d_numpy, heat_3d
     from npbench.benchmarks.weather_stencils.hdiff import hdiff_numpy, hdiff
+    from npbench.benchmarks.polybench.jacobi_1d import jacobi_1d_numpy, jacobi_1d
+    from npbench.benchmarks.polybench.fdtd_2d import fdtd_2d_numpy, fdtd_2d
 
     arrays, cases = {}, []
     rng = np.random.default_rng(20211)
@@ -135,6 +137,48 @@ def main():
     cases.append(dict(name="hdiff/float64/presetS", bench="hdiff", dtype="float64",
                       shape=[64, 64, 60], init="reference", sha_in=sha(inf), sha_coeff=sha(coeff),
                       sha_out=sha(o)))
+
+    # Jacobi-1D.
+    for dt in (np.float64, np.float32):
+        for n in (2, 3, 4, 17, 300):
+            for T in ((0, 1, 2, 3, 17) if n < 100 else (2, 40)):
+                A = rng.random(n).astype(dt)
+                B = rng.random(n).astype(dt)
+                add_tsteps_case("jacobi_1d", jacobi_1d_numpy.kernel, f"jacobi_1d/{dt.__name__}/{n}/T{T}",
+                                T, A, B)
+        A, B = special_values(rng, (41,), dt), special_values(rng, (41,), dt)
+        add_tsteps_case("jacobi_1d", jacobi_1d_numpy.kernel, f"jacobi_1d/{dt.__name__}/special/T5", 5,
+                        A, B, special=True)
+        A, B = jacobi_1d.initialize(3200, dt)
+        add_tsteps_case("jacobi_1d", jacobi_1d_numpy.kernel, f"jacobi_1d/{dt.__name__}/presetS", 800,
+                        A, B, store=False, init="reference", N=3200)
+
+    # FDTD-2D (TMAX steps over ex, ey, hz; _fict_ of length TMAX).
+    def add_fdtd_case(name, tmax, ex, ey, hz, fict, store=True, **meta):
+        e1, e2, h = ex.copy(), ey.copy(), hz.copy()
+        fdtd_2d_numpy.kernel(tmax, e1, e2, h, fict)
+        case = dict(name=name, bench="fdtd_2d", tsteps=int(tmax), dtype=ex.dtype.name,
+                    shape=list(ex.shape), **meta)
+        if store:
+            for k, v in (("ex_in", ex), ("ey_in", ey), ("hz_in", hz), ("fict", fict),
+                         ("ex_out", e1), ("ey_out", e2), ("hz_out", h)):
+                arrays[f"{name}/{k}"] = v
+        else:
+            case.update(sha_ex_out=sha(e1), sha_ey_out=sha(e2), sha_hz_out=sha(h))
+        cases.append(case)
+
+    for dt in (np.float64, np.float32):
+        for shape in [(1, 1), (2, 3), (5, 7), (20, 22), (33, 9)]:
+            for T in (0, 1, 3, 10):
+                ex, ey, hz = (rng.random(shape).astype(dt) for _ in range(3))
+                fict = rng.random(max(T, 1)).astype(dt)
+                add_fdtd_case(f"fdtd_2d/{dt.__name__}/{shape[0]}x{shape[1]}/T{T}", T, ex, ey, hz, fict)
+        ex, ey, hz = (special_values(rng, (9, 11), dt) for _ in range(3))
+        add_fdtd_case(f"fdtd_2d/{dt.__name__}/special/T4", 4, ex, ey, hz,
+                      special_values(rng, (4,), dt), special=True)
+        ex, ey, hz, fict = fdtd_2d.initialize(20, 200, 220, dt)
+        add_fdtd_case(f"fdtd_2d/{dt.__name__}/presetS", 20, ex, ey, hz, fict, store=False,
+                      init="reference", TMAX=20, NX=200, NY=220)
 
     np.savez_compressed(os.path.join(HERE, "cases.npz"), **arrays)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:

@@ -31,7 +31,8 @@ def _cases(golden, bench, stored=True):
 
 @pytest.mark.parametrize("which", sorted(ORACLES))
 @pytest.mark.parametrize("bench,fn", [("jacobi_2d", "jacobi_2d_kernel"),
-                                      ("heat_3d", "heat_3d_kernel")])
+                                      ("heat_3d", "heat_3d_kernel"),
+                                      ("jacobi_1d", "jacobi_1d_kernel")])
 def test_pingpong_golden(golden, which, bench, fn):
     _, arrays = golden
     kern = getattr(ORACLES[which], fn)
@@ -62,6 +63,21 @@ def test_hdiff_golden(golden, which):
 
 
 @pytest.mark.parametrize("which", sorted(ORACLES))
+def test_fdtd_golden(golden, which):
+    _, arrays = golden
+    n = 0
+    with np.errstate(all="ignore"):
+        for c in _cases(golden, "fdtd_2d"):
+            name = c["name"]
+            ex, ey, hz = (arrays[f"{name}/{k}_in"].copy() for k in ("ex", "ey", "hz"))
+            ORACLES[which].fdtd_2d_kernel(c["tsteps"], ex, ey, hz, arrays[f"{name}/fict"])
+            for k, v in (("ex", ex), ("ey", ey), ("hz", hz)):
+                assert bits_equal(v, arrays[f"{name}/{k}_out"]), (name, k)
+            n += 1
+    assert n >= 20
+
+
+@pytest.mark.parametrize("which", sorted(ORACLES))
 def test_reference_initializer_presets(golden, which):
     """Preset S with the reference's own initializers, checked by SHA-256."""
     o = ORACLES[which]
@@ -70,7 +86,17 @@ def test_reference_initializer_presets(golden, which):
         if c.get("init") != "reference":
             continue
         dt = np.dtype(c["dtype"])
-        if c["bench"] == "jacobi_2d":
+        if c["bench"] == "fdtd_2d":
+            ex, ey, hz, fict = workloads.init_fdtd_2d(c["TMAX"], c["NX"], c["NY"], dt.type)
+            o.fdtd_2d_kernel(c["tsteps"], ex, ey, hz, fict)
+            assert (_sha(ex), _sha(ey), _sha(hz)) == (c["sha_ex_out"], c["sha_ey_out"],
+                                                      c["sha_hz_out"]), c["name"]
+            seen += 1
+            continue
+        if c["bench"] == "jacobi_1d":
+            A, B = workloads.init_jacobi_1d(c["N"], dt.type)
+            kern = o.jacobi_1d_kernel
+        elif c["bench"] == "jacobi_2d":
             A, B = workloads.init_jacobi_2d(c["N"], dt.type)
             kern = o.jacobi_2d_kernel
         elif c["bench"] == "heat_3d":
@@ -88,7 +114,7 @@ def test_reference_initializer_presets(golden, which):
         kern(c["tsteps"], A, B)
         assert _sha(A) == c["sha_A_out"] and _sha(B) == c["sha_B_out"], c["name"]
         seen += 1
-    assert seen == 5
+    assert seen == 9
 
 
 def test_oracles_agree_on_random_nonsquare():

@@ -41,10 +41,13 @@ def _sha(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-KERNELS = {"jacobi_2d": stencils.jacobi_2d_kernel, "heat_3d": stencils.heat_3d_kernel}
+KERNELS = {"jacobi_2d": stencils.jacobi_2d_kernel, "heat_3d": stencils.heat_3d_kernel,
+           "jacobi_1d": stencils.jacobi_1d_kernel}
+INITS = {"jacobi_2d": workloads.init_jacobi_2d, "heat_3d": workloads.init_heat_3d,
+         "jacobi_1d": workloads.init_jacobi_1d}
 
 
-@pytest.mark.parametrize("bench", ["jacobi_2d", "heat_3d"])
+@pytest.mark.parametrize("bench", ["jacobi_2d", "heat_3d", "jacobi_1d"])
 def test_golden_pingpong_bit_exact(golden, bench):
     manifest, arrays = golden
     n = 0
@@ -76,25 +79,80 @@ def test_golden_hdiff_bit_exact(golden):
     assert n >= 6
 
 
+def test_golden_fdtd_bit_exact(golden):
+    manifest, arrays = golden
+    n = 0
+    for c in manifest["cases"]:
+        if c["bench"] != "fdtd_2d" or "init" in c:
+            continue
+        name = c["name"]
+        ex, ey, hz = (_dev(arrays[f"{name}/{k}_in"]) for k in ("ex", "ey", "hz"))
+        stencils.fdtd_2d_kernel(c["tsteps"], ex, ey, hz, _dev(arrays[f"{name}/fict"]))
+        for k, v in (("ex", ex), ("ey", ey), ("hz", hz)):
+            assert bits_equal(_host(v), arrays[f"{name}/{k}_out"]), (name, k)
+        n += 1
+    assert n >= 20
+
+
 def test_reference_initializer_presets(golden):
     seen = 0
     for c in golden[0]["cases"]:
         if c.get("init") != "reference":
             continue
-        if c["bench"] == "hdiff":
+        if c["bench"] == "fdtd_2d":
+            ex, ey, hz, fict = workloads.init_fdtd_2d(c["TMAX"], c["NX"], c["NY"],
+                                                      np.dtype(c["dtype"]).type)
+            dev = [_dev(x) for x in (ex, ey, hz, fict)]
+            stencils.fdtd_2d_kernel(c["tsteps"], *dev)
+            assert [_sha(_host(x)) for x in dev[:3]] == [c["sha_ex_out"], c["sha_ey_out"],
+                                                         c["sha_hz_out"]], c["name"]
+        elif c["bench"] == "hdiff":
             inf, out, coeff = workloads.init_hdiff(*c["shape"])
             o = _dev(out)
             stencils.hdiff(_dev(inf), o, _dev(coeff))
             assert _sha(_host(o)) == c["sha_out"], c["name"]
         else:
-            init = workloads.init_jacobi_2d if c["bench"] == "jacobi_2d" else workloads.init_heat_3d
-            A, B = init(c["N"], np.dtype(c["dtype"]).type)
+            A, B = INITS[c["bench"]](c["N"], np.dtype(c["dtype"]).type)
             dA, dB = _dev(A), _dev(B)
             KERNELS[c["bench"]](c["tsteps"], dA, dB)
             assert _sha(_host(dA)) == c["sha_A_out"], c["name"]
             assert _sha(_host(dB)) == c["sha_B_out"], c["name"]
         seen += 1
-    assert seen == 5
+    assert seen == 9
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_jacobi_1d_paper_size_vs_oracle(dtype):
+    A, B = workloads.uniform_pair((32000,), dtype, seed=15)
+    dA, dB = _dev(A), _dev(B)
+    stencils.jacobi_1d_kernel(4000, dA, dB)
+    cref.jacobi_1d_kernel(4000, A, B)
+    assert bits_equal(_host(dA), A) and bits_equal(_host(dB), B)
+    for n, T in ((3, 5), (1026, 17), (2049, 34), (5000, 3)):
+        A, B = workloads.uniform_pair((n,), dtype, seed=n)
+        dA, dB = _dev(A), _dev(B)
+        stencils.jacobi_1d_kernel(T, dA, dB)
+        cref.jacobi_1d_kernel(T, A, B)
+        assert bits_equal(_host(dA), A) and bits_equal(_host(dB), B), (n, T)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_fdtd_paper_size_vs_oracle(dtype):
+    ex, ey, hz, fict = workloads.init_fdtd_2d(500, 1000, 1200, dtype)
+    rng = np.random.default_rng(16)
+    ex, ey, hz = (rng.random(ex.shape).astype(dtype) for _ in range(3))
+    dev = [_dev(x) for x in (ex, ey, hz, fict)]
+    stencils.fdtd_2d_kernel(500, *dev)
+    cref.fdtd_2d_kernel(500, ex, ey, hz, fict)
+    for d, h in zip(dev[:3], (ex, ey, hz)):
+        assert bits_equal(_host(d), h), first_diff(_host(d), h)
+
+
+def test_fdtd_rejects_short_fict():
+    ex = torch.zeros((4, 5), dtype=torch.float64, device=DEV)
+    with pytest.raises(IndexError):
+        stencils.fdtd_2d_kernel(3, ex, ex.clone(), ex.clone(), torch.zeros(2, dtype=torch.float64,
+                                                                             device=DEV))
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
@@ -360,3 +418,45 @@ def test_heat_kernel_variants_bit_exact(rows, cvt, hw):
     finally:
         for k, v in zip(keys, old):
             _lib.set_config(k, v)
+
+
+@pytest.mark.parametrize("hw_warps", [0, 1, 3, 8])
+def test_jacobi_hw_warp_mix_bit_exact(hw_warps):
+    from npbench_gb300 import _lib
+    old = _lib.set_config(_lib.NPBGB_CFG_JACOBI_HW_WARPS, hw_warps)
+    try:
+        for field in ("uniform", "mixed"):
+            shape = (200, 1100)
+            A, B = (workloads.uniform_pair(shape, np.float64, seed=hw_warps) if field == "uniform"
+                    else (_mixed_range_field(shape, 60), _mixed_range_field(shape, 61)))
+            ra, rb = A.copy(), B.copy()
+            cref.jacobi_2d_kernel(6, ra, rb)
+            dA, dB = _dev(A), _dev(B)
+            stencils.jacobi_2d_kernel(6, dA, dB)
+            assert bits_equal(_host(dA), ra) and bits_equal(_host(dB), rb), (hw_warps, field)
+    finally:
+        _lib.set_config(_lib.NPBGB_CFG_JACOBI_HW_WARPS, old)
+
+
+@pytest.mark.parametrize("bench,shape,tsteps", [("jacobi_2d", (1000, 1000), 10),
+                                                ("jacobi_2d", (1000, 1000), 100),
+                                                ("heat_3d", (256, 256, 256), 10),
+                                                ("heat_3d", (256, 256, 256), 100)])
+def test_fp32_form_error_against_fp64(bench, shape, tsteps):
+    """The float32 form: max-abs and relative-L2 error against the float64 run (<= 1e-5)."""
+    if bench == "jacobi_2d":
+        A, B = workloads.uniform_pair(shape, np.float64, seed=70)
+        kern = stencils.jacobi_2d_kernel
+    else:
+        A, B = workloads.uniform_heat(shape, np.float64, seed=71)
+        kern = stencils.heat_3d_kernel
+    d64 = (_dev(A), _dev(B))
+    d32 = (_dev(A.astype(np.float32)), _dev(B.astype(np.float32)))
+    kern(tsteps, *d64)
+    kern(tsteps, *d32)
+    ref = d64[0]
+    diff = d32[0].double() - ref
+    max_abs = float(diff.abs().max())
+    rel_l2 = float(diff.norm() / ref.norm())
+    print(f"\nfp32-vs-fp64 {bench} {shape} TSTEPS={tsteps}: max_abs={max_abs:.3e} rel_l2={rel_l2:.3e}")
+    assert rel_l2 <= 1e-5 and max_abs < 1e-4

@@ -50,7 +50,9 @@ assert type(f).__name__ == "GB300Framework"
 assert f.version().startswith("npbgb ")
 for name, fn, mod in [("jacobi_2d", "kernel", "npbench.benchmarks.polybench.jacobi_2d.jacobi_2d_gb300"),
                       ("heat_3d", "kernel", "npbench.benchmarks.polybench.heat_3d.heat_3d_gb300"),
-                      ("hdiff", "hdiff", "npbench.benchmarks.weather_stencils.hdiff.hdiff_gb300")]:
+                      ("hdiff", "hdiff", "npbench.benchmarks.weather_stencils.hdiff.hdiff_gb300"),
+                      ("jacobi_1d", "kernel", "npbench.benchmarks.polybench.jacobi_1d.jacobi_1d_gb300"),
+                      ("fdtd_2d", "kernel", "npbench.benchmarks.polybench.fdtd_2d.fdtd_2d_gb300")]:
     b = Benchmark(name)
     impl, label = f.implementations(b)[0]
     assert impl.__module__ == mod and impl.__name__ == fn and label == "default", impl
@@ -76,7 +78,7 @@ def test_install_is_idempotent(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("bench", ["jacobi_2d", "heat_3d", "hdiff"])
+@pytest.mark.parametrize("bench", ["jacobi_2d", "heat_3d", "hdiff", "jacobi_1d", "fdtd_2d"])
 def test_harness_runs_and_validates_plugin(tmp_path, bench):
     if not os.path.isdir(os.path.join(BUILT_TREE, "npbench", "infrastructure")):
         pytest.skip("baseline/_ref/npbench was not built")

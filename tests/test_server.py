@@ -64,8 +64,8 @@ def _requests(n, seed):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("direct_cells", [1 << 20, 600])
-def test_served_mix_equals_alone(direct_cells):
+@pytest.mark.parametrize("direct_cells,round_updates", [(1 << 20, 2e9), (600, 2e4)])
+def test_served_mix_equals_alone(direct_cells, round_updates):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -74,7 +74,8 @@ def test_served_mix_equals_alone(direct_cells):
     reqs = _requests(40, seed=3)
     budget = max(r.nbytes for r in reqs) * 3  # small: forces waiting for memory
     futures = []
-    with StencilServer(hbm_budget_bytes=budget, quantum=6, direct_cells=direct_cells) as srv:
+    with StencilServer(hbm_budget_bytes=budget, quantum=6, direct_cells=direct_cells,
+                       round_updates=round_updates) as srv:
         def client(part):
             for r in part:
                 futures.append((r, srv.submit(r)))
