@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--workload", default="heat3d",
-                    choices=["heat3d", "jacobi2d", "hdiff", "batch", "serve"],
+                    choices=["heat3d", "jacobi2d", "hdiff", "batch", "serve", "jacobi1d", "fdtd2d"],
                     help="heat3d (default): Heat-3D 256^3; jacobi2d: Jacobi-2D 1000^2 float64, "
                          "TSTEPS=100; hdiff: 256x256x160 float64, one call per step; batch: "
                          "4096 mixed Jacobi-2D grids in one persistent launch; serve: "
@@ -450,6 +450,89 @@ def run_hdiff(args):
         gpu_launches=args.steps, clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
 
 
+def run_jacobi1d(args):
+    """Jacobi-1D at NPBench's paper preset (N=32000, TSTEPS=4000), float64."""
+    import torch
+    from npbench_gb300 import stencils, workloads
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    n, T = 32000, 4000
+    A0, B0 = workloads.init_jacobi_1d(n)
+    pA, pB = torch.from_numpy(A0).to(dev), torch.from_numpy(B0).to(dev)
+    A, B = torch.empty_like(pA), torch.empty_like(pB)
+
+    def reset():
+        A.copy_(pA)
+        B.copy_(pB)
+
+    with ClockSampler(0) as clk:
+        ms = _timed_steps(torch, dev, stream, lambda: stencils.jacobi_1d_kernel(T, A, B), reset,
+                          args.steps, args.warmup)
+    ups = 2 * (T - 1) * (n - 2)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import stencils_np
+        a, b = A0.copy(), B0.copy()
+        t0 = time.perf_counter()
+        stencils_np.jacobi_1d_kernel(201, a, b)
+        dt = time.perf_counter() - t0
+        cpu = {"value": 400 * (n - 2) / dt, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"TSTEPS=201 (400 half-sweeps) on the same array, {dt:.2f} s"}
+    peak, kind = measured_peaks()
+    ach = 16.0 * ups / (ms / args.steps * 1e-3) / 1e9
+    print(json.dumps(_base_line(
+        args, ups * args.steps / (ms * 1e-3), ms / args.steps, "f64",
+        "jacobi_1d N=32000 float64, TSTEPS=4000 (paper preset, reference initialize)",
+        {"n": n, "TSTEPS": T, "l2": "256 KB arrays are L2-resident"},
+        roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                  "peak_kind": kind, "traffic": None,
+                  "note": "16 B per update; 32 half-sweeps per launch run in shared memory, "
+                          "so the binary64 pipe, not HBM, bounds it"},
+        gpu_launches=(2 * (T - 1) + 31) // 32 * args.steps, clocks=clk.summary(),
+        cpu_baseline=cpu)), flush=True)
+
+
+def run_fdtd2d(args):
+    """FDTD-2D at NPBench's paper preset (TMAX=500, 1000 x 1200), float64."""
+    import torch
+    from npbench_gb300 import stencils, workloads
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    T, nx, ny = 500, 1000, 1200
+    host = workloads.init_fdtd_2d(T, nx, ny)
+    pristine = [torch.from_numpy(x).to(dev) for x in host]
+    work = [x.clone() for x in pristine]
+
+    def reset():
+        for w, p in zip(work[:3], pristine[:3]):
+            w.copy_(p)
+
+    with ClockSampler(0) as clk:
+        ms = _timed_steps(torch, dev, stream, lambda: stencils.fdtd_2d_kernel(T, *work), reset,
+                          args.steps, args.warmup)
+    cells = T * nx * ny  # cell-steps (each updates ex, ey and hz)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import stencils_np
+        ex, ey, hz, fict = (x.copy() for x in host)
+        t0 = time.perf_counter()
+        stencils_np.fdtd_2d_kernel(20, ex, ey, hz, fict)
+        dt = time.perf_counter() - t0
+        cpu = {"value": 20 * nx * ny / dt, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"TMAX=20 on the same fields, {dt:.2f} s"}
+    peak, kind = measured_peaks()
+    ach = 48.0 * cells / (ms / args.steps * 1e-3) / 1e9
+    print(json.dumps(_base_line(
+        args, cells * args.steps / (ms * 1e-3), ms / args.steps, "f64",
+        "fdtd_2d 1000x1200 float64, TMAX=500 (paper preset, reference initialize)",
+        {"shape": [nx, ny], "TMAX": T, "unit_note": "value counts cell-steps per second",
+         "l2": "the three 9.6 MB fields are L2-resident"},
+        roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                  "peak_kind": kind, "traffic": None,
+                  "note": "48 B per cell-step (ex, ey, hz read and written once)"},
+        gpu_launches=2 * T * args.steps, clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
+
+
 def run_batch(args):
     """4096 independent Jacobi-2D grids (sides log-uniform in [64, 2048], half float32 and
     half float64, TSTEPS uniform in [10, 500]) in one persistent launch per step."""
@@ -559,7 +642,7 @@ def main():
         run_gb300(args, world, rank, local)
     elif rank == 0:
         {"jacobi2d": run_jacobi2d, "hdiff": run_hdiff, "batch": run_batch,
-         "serve": run_serve}[args.workload](args)
+         "serve": run_serve, "jacobi1d": run_jacobi1d, "fdtd2d": run_fdtd2d}[args.workload](args)
 
 
 if __name__ == "__main__":

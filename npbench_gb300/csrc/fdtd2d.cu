@@ -7,7 +7,9 @@
 //   hz[i, j] -= 0.7 * (((ex[i, j+1] - ex[i, j]) + ey[i+1, j]) - ey[i, j])   i < nx-1, j < ny-1
 // The ey and ex updates read only hz, so one launch does both (and the row-0
 // source); the hz update reads the new ex and ey and is a second launch.
-// Every operator is one correctly rounded IEEE operation.
+// Every operator is one correctly rounded IEEE operation; the binary64
+// products by 0.5, which are exact, are done as exponent decrements on the
+// integer pipe (GB300's binary64 pipe is the bound).
 #include "npbgb_common.cuh"
 
 namespace npbgb {
@@ -15,11 +17,23 @@ namespace {
 
 constexpr int kBX = 32, kBY = 8;
 
+// 0.5 * x without the binary64 pipe: halving is exact (an exponent decrement)
+// for normal x whose halving stays normal; zero, subnormal, inf and NaN take
+// the literal multiply, kept out of line so it is not predicated into the
+// common path.
+__device__ __noinline__ double half_literal(double x) { return mul_rn(0.5, x); }
+__device__ __forceinline__ double half_of(double x) {
+  const uint64_t b = static_cast<uint64_t>(__double_as_longlong(x));
+  const uint32_t e = static_cast<uint32_t>(b >> 52) & 0x7ffu;
+  if (e >= 2u && e <= 2046u) return __longlong_as_double(static_cast<long long>(b - (1ull << 52)));
+  return half_literal(x);
+}
+__device__ __forceinline__ float half_of(float x) { return mul_rn(0.5f, x); }
+
 template <typename T>
 __global__ void __launch_bounds__(kBX * kBY)
 fdtd_e(T* __restrict__ ex, T* __restrict__ ey, const T* __restrict__ hz, const T* __restrict__ fict,
        int64_t nx, int64_t ny, int t) {
-  const T half = T(0.5);
   const int64_t j = int64_t(blockIdx.x) * kBX + threadIdx.x;
   if (j >= ny) return;
   for (int64_t i = int64_t(blockIdx.y) * kBY + threadIdx.y; i < nx; i += int64_t(gridDim.y) * kBY) {
@@ -28,8 +42,8 @@ fdtd_e(T* __restrict__ ex, T* __restrict__ ey, const T* __restrict__ hz, const T
     if (i == 0)
       ey[o] = fict[t];
     else
-      ey[o] = sub_rn(ey[o], mul_rn(half, sub_rn(h, hz[o - ny])));
-    if (j >= 1) ex[o] = sub_rn(ex[o], mul_rn(half, sub_rn(h, hz[o - 1])));
+      ey[o] = sub_rn(ey[o], half_of(sub_rn(h, hz[o - ny])));
+    if (j >= 1) ex[o] = sub_rn(ex[o], half_of(sub_rn(h, hz[o - 1])));
   }
 }
 

@@ -7,7 +7,8 @@
 // The arrays are small (NPBench's presets go up to 34000 points), so a plain
 // one-launch-per-half-sweep loop is bound by launch latency.  Instead each
 // launch performs kSteps half-sweeps with temporal blocking: a CTA stages its
-// segment of kW points plus kSteps halo points on each side into shared
+// segment of kW points (128 to 1024, chosen per array so that the CTAs
+// cover the SMs) plus kSteps halo points on each side into shared
 // memory, runs the half-sweeps there (the valid region shrinks by one point
 // per side and half-sweep, so every kept value is computed exactly as the
 // reference computes it), and writes back its segment of both arrays: A
@@ -20,13 +21,14 @@ namespace npbgb {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kW = 1024;              // segment written per CTA
 constexpr int kSteps = 32;            // half-sweeps per launch (even)
-constexpr int kSpan = kW + 2 * kSteps;  // staged points per CTA
 
-template <typename T>
+// kW: points written per CTA; chosen per array so that the segments cover the
+// SMs (the arithmetic is bound by the small binary64 pipe, so idle SMs cost).
+template <typename T, int kW>
 __global__ void __launch_bounds__(kThreads)
 jacobi1d_block(T* __restrict__ a, T* __restrict__ b, int64_t n, int steps) {
+  constexpr int kSpan = kW + 2 * kSteps;  // staged points per CTA
   __shared__ T buf[2][kSpan];
   const T k = T(0.33333);
   const int64_t seg = int64_t(blockIdx.x) * kW;       // first written point - 1 (interior starts at 1)
@@ -60,19 +62,29 @@ jacobi1d_block(T* __restrict__ a, T* __restrict__ b, int64_t n, int steps) {
   }
 }
 
-template <typename T>
-int32_t run(T* a, T* b, int64_t n, int32_t tsteps, cudaStream_t st) {
-  if (tsteps <= 1 || n < 3) return NPBGB_OK;
+template <typename T, int kW>
+int32_t run_w(T* a, T* b, int64_t n, int32_t tsteps, cudaStream_t st) {
   const int64_t blocks = cdiv(n - 2, kW);
   if (blocks > 0x7fffffff) return set_error(NPBGB_ERR_ARG, "jacobi1d: extent too large");
   int64_t left = 2 * int64_t(tsteps - 1);  // half-sweeps, even
   while (left > 0) {
     const int s = int(left < kSteps ? left : kSteps);
-    jacobi1d_block<T><<<unsigned(blocks), kThreads, 0, st>>>(a, b, n, s);
+    jacobi1d_block<T, kW><<<unsigned(blocks), kThreads, 0, st>>>(a, b, n, s);
     left -= s;
   }
   NPBGB_CHECK_LAUNCH("jacobi1d_block");
   return NPBGB_OK;
+}
+
+template <typename T>
+int32_t run(T* a, T* b, int64_t n, int32_t tsteps, cudaStream_t st) {
+  if (tsteps <= 1 || n < 3) return NPBGB_OK;
+  // Widest segment that still gives every SM a CTA.
+  const int64_t per_sm = cdiv(n - 2, sm_count());
+  if (per_sm <= 128) return run_w<T, 128>(a, b, n, tsteps, st);
+  if (per_sm <= 256) return run_w<T, 256>(a, b, n, tsteps, st);
+  if (per_sm <= 512) return run_w<T, 512>(a, b, n, tsteps, st);
+  return run_w<T, 1024>(a, b, n, tsteps, st);
 }
 
 }  // namespace
