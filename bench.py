@@ -59,11 +59,13 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--workload", default="heat3d",
-                    choices=["heat3d", "jacobi2d", "hdiff", "batch", "serve", "jacobi1d", "fdtd2d"],
+                    choices=["heat3d", "jacobi2d", "hdiff", "batch", "serve", "jacobi1d", "fdtd2d",
+                             "vadv"],
                     help="heat3d (default): Heat-3D 256^3; jacobi2d: Jacobi-2D 1000^2 float64, "
                          "TSTEPS=100; hdiff: 256x256x160 float64, one call per step; batch: "
                          "4096 mixed Jacobi-2D grids in one persistent launch; serve: "
-                         "Poisson-arrival mixed solves through the continuous-batching server")
+                         "Poisson-arrival mixed solves through the continuous-batching server; "
+                         "jacobi1d / fdtd2d / vadv: NPBench paper presets")
     ap.add_argument("--batch-grids", type=int, default=4096)
     ap.add_argument("--compare", action="store_true",
                     help="batch/serve: also time the per-grid / sequential comparator")
@@ -492,6 +494,51 @@ def run_jacobi1d(args):
         cpu_baseline=cpu)), flush=True)
 
 
+def run_vadv(args):
+    """vadv 256x256x160 float64 (paper preset, reference initialize), one call per step."""
+    import torch
+    from npbench_gb300 import stencils, workloads
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    I, J, K = 256, 256, 160
+    dtr, us0, u, w, up, ut = workloads.init_vadv(I, J, K)
+    pristine = torch.from_numpy(us0).to(dev)
+    dUs = pristine.clone()
+    dU, dW, dUp, dUt = (torch.from_numpy(x).to(dev) for x in (u, w, up, ut))
+
+    def reset():
+        dUs.copy_(pristine)
+
+    with ClockSampler(0) as clk:
+        ms = _timed_steps(torch, dev, stream,
+                          lambda: stencils.vadv(dUs, dU, dW, dUp, dUt, dtr), reset,
+                          args.steps, args.warmup)
+    ms_step = ms / args.steps
+    pts = I * J * K
+    # read utens_stage, u_stage, u_pos, utens and wcon once, write utens_stage once
+    alg = 8.0 * (5 * I * J * K + (I + 1) * J * K)
+    peak, kind = measured_peaks()
+    ach = alg / (ms_step * 1e-3) / 1e9
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import stencils_np
+        o = us0.copy()
+        t0 = time.perf_counter()
+        stencils_np.vadv(o, u, w, up, ut, dtr)
+        dt = time.perf_counter() - t0
+        cpu = {"value": pts / dt, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"1 call on the same 256x256x160 input, {dt:.2f} s"}
+    print(json.dumps(_base_line(
+        args, pts * args.steps / (ms * 1e-3), ms_step, "f64",
+        "vadv 256x256x160 float64 (paper preset, reference initialize), one call per step",
+        {"shape": [I, J, K], "l2": "420 MB of inputs+output, larger than L2"},
+        unit_note="value counts output points per second",
+        roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                  "peak_kind": kind, "traffic": ncu_traffic("vadv_f64_256"),
+                  "alg_bytes_per_launch": alg},
+        gpu_launches=args.steps, clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
+
+
 def run_fdtd2d(args):
     """FDTD-2D at NPBench's paper preset (TMAX=500, 1000 x 1200), float64."""
     import torch
@@ -642,7 +689,7 @@ def main():
         run_gb300(args, world, rank, local)
     elif rank == 0:
         {"jacobi2d": run_jacobi2d, "hdiff": run_hdiff, "batch": run_batch,
-         "serve": run_serve, "jacobi1d": run_jacobi1d, "fdtd2d": run_fdtd2d}[args.workload](args)
+         "serve": run_serve, "jacobi1d": run_jacobi1d, "fdtd2d": run_fdtd2d, "vadv": run_vadv}[args.workload](args)
 
 
 if __name__ == "__main__":

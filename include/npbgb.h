@@ -162,6 +162,23 @@ NPBGB_API int32_t npbgb_jacobi1d(void* A, void* B, int64_t n, int32_t tsteps, in
 NPBGB_API int32_t npbgb_fdtd2d(void* ex, void* ey, void* hz, const void* fict, int64_t fict_len,
                                int64_t nx, int64_t ny, int32_t tmax, int32_t dtype, void* stream);
 
+/* Vertical advection, a tridiagonal (Thomas) solve along K per (i, j) column,
+ *   vadv(utens_stage, u_stage, wcon, u_pos, utens, dtr_stage)
+ *                               weather_stencils/vadv/vadv_numpy.py:9-78
+ * utens_stage, u_stage, u_pos, utens are (I, J, K) and wcon is (I+1, J, K);
+ * K is contiguous.  Writes all of utens_stage (the only output; its values are
+ * also read).  dtype must be NPBGB_F64.  K < 2 is NPBGB_ERR_ARG (the reference
+ * raises IndexError: it reads level 1 unconditionally).  The solve keeps one
+ * coefficient per point in a device workspace of npbgb_vadv_workspace_bytes()
+ * bytes (8*(K-1)*I*J); pass it, or NULL to have the call allocate and free it
+ * stream-ordered (cudaMallocAsync / cudaFreeAsync on `stream`).  A caller that
+ * passes a workspace must not use it concurrently for another call. */
+NPBGB_API int64_t npbgb_vadv_workspace_bytes(int64_t I, int64_t J, int64_t K);
+NPBGB_API int32_t npbgb_vadv(void* utens_stage, const void* u_stage, const void* wcon,
+                             const void* u_pos, const void* utens, double dtr_stage, int64_t I,
+                             int64_t J, int64_t K, int32_t dtype, void* workspace,
+                             int64_t workspace_bytes, void* stream);
+
 /* Batches: many independent grids advanced by one persistent launch.
  *
  * npbgb_batch_create plans a batch of Jacobi-2D and Heat-3D grids: each grid

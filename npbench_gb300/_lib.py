@@ -64,6 +64,9 @@ SIGNATURES = {
     "npbgb_hdiff": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i32, _vp]),
     "npbgb_jacobi1d": (_i32, [_vp, _vp, _i64, _i32, _i32, _vp]),
     "npbgb_fdtd2d": (_i32, [_vp, _vp, _vp, _vp, _i64, _i64, _i64, _i32, _i32, _vp]),
+    "npbgb_vadv_workspace_bytes": (_i64, [_i64, _i64, _i64]),
+    "npbgb_vadv": (_i32, [_vp, _vp, _vp, _vp, _vp, ctypes.c_double, _i64, _i64, _i64, _i32, _vp,
+                          _i64, _vp]),
 }
 
 _lock = threading.Lock()

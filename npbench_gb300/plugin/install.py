@@ -13,6 +13,7 @@ Adds, under NPBENCH_ROOT (the directory holding ``framework_info/``,
 * ``npbench/benchmarks/weather_stencils/hdiff/hdiff_gb300.py``
 * ``npbench/benchmarks/polybench/jacobi_1d/jacobi_1d_gb300.py``
 * ``npbench/benchmarks/polybench/fdtd_2d/fdtd_2d_gb300.py``
+* ``npbench/benchmarks/weather_stencils/vadv/vadv_gb300.py``
 
 and appends ``from .gb300_framework import *`` to
 ``npbench/infrastructure/__init__.py`` (once).  ``--copy-from`` first copies a
@@ -34,6 +35,7 @@ FILES = [
     "benchmarks/weather_stencils/hdiff/hdiff_gb300.py",
     "benchmarks/polybench/jacobi_1d/jacobi_1d_gb300.py",
     "benchmarks/polybench/fdtd_2d/fdtd_2d_gb300.py",
+    "benchmarks/weather_stencils/vadv/vadv_gb300.py",
 ]
 IMPORT_LINE = "from .gb300_framework import *\n"
 

@@ -14,6 +14,7 @@ heat_f32   Heat-3D 256^3 float32, TSTEPS=3                heat3d_tma, -s 2
 jacobi_f64 Jacobi-2D 4096^2 float64, TSTEPS=3             jacobi2d_strip, -s 2
 jacobi_f32 Jacobi-2D 4096^2 float32, TSTEPS=3             jacobi2d_strip, -s 2
 hdiff      hdiff 256x256x160 float64, 3 calls             hdiff_tile, -s 1
+vadv       vadv 256x256x160 float64, 3 calls              vadv_columns, -s 1
 batch      256 mixed Jacobi-2D grids, 2 launches          batch_persistent, -s 1
 ========== ============================================== ===================
 """
@@ -42,6 +43,11 @@ def run(case):
         x, y, z = (torch.from_numpy(t).to(dev) for t in (inf, out, co))
         for _ in range(3):
             stencils.hdiff(x, y, z)
+    elif case == "vadv":
+        dtr, us, u, w, up, ut = workloads.init_vadv(256, 256, 160)
+        a, b, c, d, e = (torch.from_numpy(t).to(dev) for t in (us, u, w, up, ut))
+        for _ in range(3):
+            stencils.vadv(a, b, c, d, e, dtr)
     elif case == "batch":
         from npbench_gb300.batch import Batch
         specs = workloads.batch_jacobi_specs(256, seed=0, tsteps=(10, 40))

@@ -7,6 +7,8 @@ These are drop-ins for the reference NumPy kernels:
 * ``hdiff(in_field, out_field, coeff)`` -- weather_stencils/hdiff/hdiff_numpy.py:5
 * ``jacobi_1d_kernel(TSTEPS, A, B)``   -- polybench/jacobi_1d/jacobi_1d_numpy.py:4
 * ``fdtd_2d_kernel(TMAX, ex, ey, hz, _fict_)`` -- polybench/fdtd_2d/fdtd_2d_numpy.py:4
+* ``vadv(utens_stage, u_stage, wcon, u_pos, utens, dtr_stage)`` --
+  weather_stencils/vadv/vadv_numpy.py:9
 
 Arguments are updated in place and nothing is returned, as in the reference.
 They may be
@@ -17,7 +19,7 @@ They may be
   updated there and copied back into the same NumPy arrays before returning.
 
 Results are bit-identical to the reference NumPy kernels for float64 and
-float32 (hdiff: float64 only).  Errors raise ``TypeError`` (dtype),
+float32 (hdiff and vadv: float64 only).  Errors raise ``TypeError`` (dtype),
 ``ValueError`` (shape, device, aliasing) or ``npbench_gb300.NpbgbError``
 (a status from the library).  There is no CPU fallback: without a CUDA device
 or without libnpbgb.so these functions raise.
@@ -26,7 +28,8 @@ import numpy as np
 
 from . import _lib
 
-__all__ = ["jacobi_2d_kernel", "heat_3d_kernel", "hdiff", "jacobi_1d_kernel", "fdtd_2d_kernel"]
+__all__ = ["jacobi_2d_kernel", "heat_3d_kernel", "hdiff", "jacobi_1d_kernel", "fdtd_2d_kernel",
+           "vadv"]
 
 
 def _torch():
@@ -199,4 +202,40 @@ def fdtd_2d_kernel(TMAX, ex, ey, hz, _fict_):
                               int(_fict_.shape[0]), int(ex.shape[0]), int(ex.shape[1]), T, code,
                               view.stream)
         _lib.check(st, "fdtd_2d")
+        view.finish()
+
+
+def vadv(utens_stage, u_stage, wcon, u_pos, utens, dtr_stage):
+    """``vadv(utens_stage, u_stage, wcon, u_pos, utens, dtr_stage)`` of
+    weather_stencils/vadv/vadv_numpy.py:9-78; writes ``utens_stage``.
+
+    The solve's coefficient workspace (8*(K-1)*I*J bytes) is taken from
+    PyTorch's caching allocator on the call's stream.  K < 2 raises
+    IndexError, as the reference does.
+    """
+    I, J, K = (int(s) for s in utens_stage.shape)
+    for n, a in (("u_stage", u_stage), ("u_pos", u_pos), ("utens", utens)):
+        if tuple(a.shape) != (I, J, K):
+            raise ValueError(f"vadv: {n} shape {tuple(a.shape)}, expected {(I, J, K)}")
+    if tuple(wcon.shape) != (I + 1, J, K):
+        raise ValueError(f"vadv: wcon shape {tuple(wcon.shape)}, expected {(I + 1, J, K)}")
+    for n, a in (("u_stage", u_stage), ("wcon", wcon), ("u_pos", u_pos), ("utens", utens)):
+        if a.dtype != utens_stage.dtype:
+            raise TypeError(f"vadv: {n} dtype {a.dtype} differs from utens_stage "
+                            f"{utens_stage.dtype}")
+        if _shares_memory(a, utens_stage):
+            raise ValueError(f"vadv: {n} shares memory with utens_stage")
+    code = _dtype_code(utens_stage.dtype, allowed=(np.float64,))
+    if K < 2:
+        raise IndexError(f"vadv: K = {K}; the solve reads level 1")
+    lib = _lib.load()
+    torch = _torch()
+    view = _DeviceView((utens_stage, u_stage, wcon, u_pos, utens),
+                       (True, False, False, False, False))
+    with torch.cuda.device(view.device):
+        nbytes = int(lib.npbgb_vadv_workspace_bytes(I, J, K))
+        ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=view.device)
+        st = lib.npbgb_vadv(view.ptr(0), view.ptr(1), view.ptr(2), view.ptr(3), view.ptr(4),
+                            float(dtr_stage), I, J, K, code, ws.data_ptr(), nbytes, view.stream)
+        _lib.check(st, "vadv")
         view.finish()

@@ -7,6 +7,9 @@
 * ``init_hdiff(I, J, K)`` restates weather_stencils/hdiff/hdiff.py:6-15:
   ``default_rng(42)`` draws ``in_field (I+4,J+4,K)``, ``out_field (I,J,K)``,
   ``coeff (I,J,K)`` in that order.
+* ``init_vadv(I, J, K)`` restates weather_stencils/vadv/vadv.py:6-19:
+  ``dtr_stage = 3/20`` and ``default_rng(42)`` draws ``utens_stage``,
+  ``u_stage``, ``wcon (I+1,J,K)``, ``u_pos``, ``utens`` in that order.
 * ``uniform_pair`` / ``uniform_heat`` draw U[0,1) fields from
   ``numpy.random.default_rng(seed)`` (float32 forms are casts of the float64
   draw, so both precisions see the same field).
@@ -22,6 +25,8 @@ PRESETS = {
               "L": {"I": 384, "J": 384, "K": 160}, "paper": {"I": 256, "J": 256, "K": 160}},
     "jacobi_1d": {"S": {"TSTEPS": 800, "N": 3200}, "M": {"TSTEPS": 3000, "N": 12000},
                   "L": {"TSTEPS": 8500, "N": 34000}, "paper": {"TSTEPS": 4000, "N": 32000}},
+    "vadv": {"S": {"I": 60, "J": 60, "K": 40}, "M": {"I": 112, "J": 112, "K": 80},
+             "L": {"I": 180, "J": 180, "K": 160}, "paper": {"I": 256, "J": 256, "K": 160}},
     "fdtd_2d": {"S": {"TMAX": 20, "NX": 200, "NY": 220}, "M": {"TMAX": 60, "NX": 400, "NY": 450},
                 "L": {"TMAX": 150, "NX": 800, "NY": 900},
                 "paper": {"TMAX": 500, "NX": 1000, "NY": 1200}},
@@ -62,6 +67,18 @@ def init_hdiff(I, J, K):
     out_field = rng.random((I, J, K))
     coeff = rng.random((I, J, K))
     return in_field, out_field, coeff
+
+
+def init_vadv(I, J, K):
+    """Returns (dtr_stage, utens_stage, u_stage, wcon, u_pos, utens)."""
+    rng = np.random.default_rng(42)
+    dtr_stage = 3. / 20.
+    utens_stage = rng.random((I, J, K))
+    u_stage = rng.random((I, J, K))
+    wcon = rng.random((I + 1, J, K))
+    u_pos = rng.random((I, J, K))
+    utens = rng.random((I, J, K))
+    return dtr_stage, utens_stage, u_stage, wcon, u_pos, utens
 
 
 def uniform_pair(shape, dtype=np.float64, seed=0):

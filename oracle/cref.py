@@ -9,6 +9,8 @@ with the same call shapes as the reference kernels:
 * ``hdiff(in_field, out_field, coeff)`` -- weather_stencils/hdiff/hdiff_numpy.py:5
 * ``jacobi_1d_kernel(TSTEPS, A, B)``   -- polybench/jacobi_1d/jacobi_1d_numpy.py:4
 * ``fdtd_2d_kernel(TMAX, ex, ey, hz, _fict_)`` -- polybench/fdtd_2d/fdtd_2d_numpy.py:4
+* ``vadv(utens_stage, u_stage, wcon, u_pos, utens, dtr_stage)`` --
+  weather_stencils/vadv/vadv_numpy.py:9
 """
 import ctypes
 import os
@@ -41,6 +43,7 @@ def _bind(lib):
     for sfx in ("f64", "f32"):
         getattr(lib, "oracle_jacobi1d_" + sfx).argtypes = [vp, vp, i64, i32]
         getattr(lib, "oracle_fdtd2d_" + sfx).argtypes = [vp, vp, vp, vp, i64, i64, i32]
+    lib.oracle_vadv_f64.argtypes = [vp, vp, vp, vp, vp, ctypes.c_double, i64, i64, i64]
     return lib
 
 
@@ -108,3 +111,15 @@ def fdtd_2d_kernel(TMAX, ex, ey, hz, _fict_):
         raise ValueError("_fict_ shorter than TMAX")
     getattr(lib(), "oracle_fdtd2d_" + sfx)(_p(ex), _p(ey), _p(hz), _p(_fict_), ex.shape[0],
                                           ex.shape[1], int(TMAX))
+
+
+def vadv(utens_stage, u_stage, wcon, u_pos, utens, dtr_stage):
+    if _sfx(utens_stage, u_stage, wcon, u_pos, utens) != "f64":
+        raise TypeError("vadv oracle is float64 only")
+    I, J, K = utens_stage.shape
+    if wcon.shape != (I + 1, J, K) or any(a.shape != (I, J, K) for a in (u_stage, u_pos, utens)):
+        raise ValueError("vadv shapes: wcon (I+1, J, K), the others (I, J, K)")
+    if K < 2:
+        raise IndexError(f"vadv needs K >= 2 (reads level 1), got K={K}")
+    lib().oracle_vadv_f64(_p(utens_stage), _p(u_stage), _p(wcon), _p(u_pos), _p(utens),
+                          float(dtr_stage), I, J, K)

@@ -10,6 +10,9 @@
  *   heat_3d    polybench/heat_3d/heat_3d_numpy.py:6-20
  *              dst = ((ti + tj) + tk) + c,  tx = 0.125 * ((nx - 2*c) + px)
  *   hdiff      weather_stencils/hdiff/hdiff_numpy.py:5-29
+ *   jacobi_1d  polybench/jacobi_1d/jacobi_1d_numpy.py:4-8
+ *   fdtd_2d    polybench/fdtd_2d/fdtd_2d_numpy.py:4-11
+ *   vadv       weather_stencils/vadv/vadv_numpy.py:9-78
  *
  * so results are bit-identical to the reference.  Each half-sweep is a
  * parallel loop over the slow axis (OpenMP when built with -fopenmp); the
@@ -20,6 +23,7 @@
  */
 #include <stddef.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #define DEF_JACOBI(T, SUFFIX, K02)                                              \
   static void jacobi_half_##SUFFIX(const T* src, T* dst, int64_t ny,            \
@@ -180,3 +184,76 @@ DEF_JACOBI1D(float, f32, 0.33333f)
   }
 DEF_FDTD(double, f64, 0.5, 0.7)
 DEF_FDTD(float, f32, 0.5f, 0.7f)
+
+/* vadv: weather_stencils/vadv/vadv_numpy.py:9-78, float64, arrays (I, J, K) with
+ * K contiguous and wcon (I+1, J, K).  One (i, j) column at a time: forward
+ * elimination over k = 0..K-1, then back substitution into utens_stage.  The
+ * operations and their order per level are those of the reference:
+ *   w_k = wcon[i+1,j,k] + wcon[i,j,k];  gcv = 0.25*w_{k+1};  gav = -0.25*w_k
+ *   cs = ccol_k = gcv*0.5;  as = acol = gav*0.5
+ *   bcol = (dtr - acol) - ccol_k
+ *   corr = (-as)*(u[k-1]-u[k]) - cs*(u[k+1]-u[k])
+ *   dcol_k = ((dtr*u_pos[k] + utens[k]) + utens_stage[k]) + corr
+ *   divided = 1.0 / (bcol - ccol_{k-1}*acol)
+ *   ccol_k = ccol_k*divided;  dcol_k = (dcol_k - dcol_{k-1}*acol)*divided
+ * with the one-sided forms at k = 0 and k = K-1, and
+ *   data = dcol_k - ccol_k*data;  utens_stage[k] = dtr*(data - u_pos[k]).
+ * Requires K >= 2 (the Python wrapper raises IndexError otherwise). */
+void oracle_vadv_f64(double* us, const double* u, const double* wcon, const double* up,
+                     const double* ut, double dtr, int64_t I, int64_t J, int64_t K) {
+  if (K < 2) return;
+  _Pragma("omp parallel for schedule(static)")
+  for (int64_t i = 0; i < I; ++i) {
+    double* ccol = (double*)malloc(sizeof(double) * (size_t)K * 2);
+    double* dcol = ccol + K;
+    for (int64_t j = 0; j < J; ++j) {
+      const int64_t c = (i * J + j) * K;
+      const double* wl = wcon + c;               /* wcon[i, j, :]   */
+      const double* wh = wcon + c + J * K;       /* wcon[i+1, j, :] */
+      const double* uu = u + c;
+      double* s = us + c;
+      for (int64_t k = 0; k < K; ++k) {
+        double acol = 0.0, as = 0.0, cs = 0.0, bcol, corr;
+        if (k + 1 < K) {
+          const double gcv = 0.25 * (wh[k + 1] + wl[k + 1]);
+          cs = gcv * 0.5;
+          ccol[k] = gcv * 0.5;
+        }
+        if (k > 0) {
+          const double gav = -0.25 * (wh[k] + wl[k]);
+          as = gav * 0.5;
+          acol = gav * 0.5;
+        }
+        if (k == 0) {
+          bcol = dtr - ccol[k];
+          corr = (-cs) * (uu[1] - uu[0]);
+        } else if (k < K - 1) {
+          bcol = (dtr - acol) - ccol[k];
+          corr = (-as) * (uu[k - 1] - uu[k]) - cs * (uu[k + 1] - uu[k]);
+        } else {
+          bcol = dtr - acol;
+          corr = (-as) * (uu[k - 1] - uu[k]);
+        }
+        double d = dtr * up[c + k] + ut[c + k];
+        d = d + s[k];
+        d = d + corr;
+        if (k == 0) {
+          const double divided = 1.0 / bcol;
+          ccol[k] = ccol[k] * divided;
+          dcol[k] = d * divided;
+        } else {
+          const double divided = 1.0 / (bcol - ccol[k - 1] * acol);
+          if (k < K - 1) ccol[k] = ccol[k] * divided;
+          dcol[k] = (d - dcol[k - 1] * acol) * divided;
+        }
+      }
+      double data = dcol[K - 1];
+      s[K - 1] = dtr * (data - up[c + K - 1]);
+      for (int64_t k = K - 2; k >= 0; --k) {
+        data = dcol[k] - ccol[k] * data;
+        s[k] = dtr * (data - up[c + k]);
+      }
+    }
+    free(ccol);
+  }
+}

@@ -17,11 +17,12 @@ Evaluation orders restated here:
   ``dst = ((ti + tj) + tk) + c`` with
   ``tx = 0.125 * ((next_x - 2.0 * c) + prev_x)``.
 * hdiff, weather_stencils/hdiff/hdiff_numpy.py:5-29 -- see ``hdiff``.
+* vadv, weather_stencils/vadv/vadv_numpy.py:9-78 -- see ``vadv``.
 """
 import numpy as np
 
 __all__ = ["jacobi_2d_kernel", "heat_3d_kernel", "hdiff", "jacobi_2d_half_sweep",
-           "heat_3d_half_sweep", "jacobi_1d_kernel", "fdtd_2d_kernel"]
+           "heat_3d_half_sweep", "jacobi_1d_kernel", "fdtd_2d_kernel", "vadv"]
 
 
 def jacobi_2d_half_sweep(src, dst):
@@ -157,3 +158,83 @@ def fdtd_2d_kernel(TMAX, ex, ey, hz, _fict_):
         np.subtract(d, ey[:-1, :-1], out=d)
         np.multiply(c07, d, out=d)
         np.subtract(hz[:-1, :-1], d, out=hz[:-1, :-1])
+
+
+def vadv(utens_stage, u_stage, wcon, u_pos, utens, dtr_stage):
+    """``vadv(utens_stage, u_stage, wcon, u_pos, utens, dtr_stage)`` of
+    weather_stencils/vadv/vadv_numpy.py:9-78 (float64; K contiguous).
+
+    A tridiagonal (Thomas) solve along K for every (i, j) column, written into
+    ``utens_stage``.  With ``w_k = wcon[i+1, j, k] + wcon[i, j, k]`` the
+    reference forms ``gcv = 0.25*w_{k+1}``, ``gav = -0.25*w_k`` and their
+    halves (BET_M = BET_P = 0.5), then per level k, in this order:
+
+    * ``bcol = (dtr - acol) - ccol_k`` (no ``acol`` at k = 0, no ``ccol_k`` at
+      k = K-1);
+    * ``corr = (-as)*(u[k-1] - u[k]) - cs*(u[k+1] - u[k])`` (one-sided at the
+      ends);
+    * ``dcol_k = ((dtr*u_pos[k] + utens[k]) + utens_stage[k]) + corr``;
+    * ``divided = 1.0 / (bcol - ccol_{k-1}*acol)``; ``ccol_k *= divided``;
+      ``dcol_k = (dcol_k - dcol_{k-1}*acol) * divided``;
+
+    then back substitution ``data = dcol_k - ccol_k*data`` from K-2 down to 0
+    (``data = dcol_{K-1}`` at the top) with
+    ``utens_stage[k] = dtr*(data - u_pos[k])``.  K < 2 raises IndexError, as
+    the reference does (it reads level 1 unconditionally).
+    """
+    I, J, K = utens_stage.shape
+    if K < 2:
+        raise IndexError(f"vadv needs K >= 2 (reads level 1), got K={K}")
+    dtr = float(dtr_stage)
+    ccol = np.empty((I, J, K))
+    dcol = np.empty((I, J, K))
+
+    def wsum(k):
+        return np.add(wcon[1:, :, k], wcon[:-1, :, k])
+
+    def dfirst(k, corr):
+        d = np.multiply(dtr, u_pos[:, :, k])
+        np.add(d, utens[:, :, k], out=d)
+        np.add(d, utens_stage[:, :, k], out=d)
+        np.add(d, corr, out=d)
+        return d
+
+    for k in range(K):
+        if k + 1 < K:
+            gcv = np.multiply(0.25, wsum(k + 1))
+            cs = np.multiply(gcv, 0.5)
+            ccol[:, :, k] = np.multiply(gcv, 0.5)
+        if k > 0:
+            gav = np.multiply(-0.25, wsum(k))
+            as_ = np.multiply(gav, 0.5)
+            acol = np.multiply(gav, 0.5)
+        # bcol and the correction term
+        if k == 0:
+            bcol = np.subtract(dtr, ccol[:, :, k])
+            corr = np.multiply(np.negative(cs), np.subtract(u_stage[:, :, 1], u_stage[:, :, 0]))
+        elif k < K - 1:
+            bcol = np.subtract(np.subtract(dtr, acol), ccol[:, :, k])
+            lo = np.multiply(np.negative(as_), np.subtract(u_stage[:, :, k - 1], u_stage[:, :, k]))
+            hi = np.multiply(cs, np.subtract(u_stage[:, :, k + 1], u_stage[:, :, k]))
+            corr = np.subtract(lo, hi)
+        else:
+            bcol = np.subtract(dtr, acol)
+            corr = np.multiply(np.negative(as_), np.subtract(u_stage[:, :, k - 1], u_stage[:, :, k]))
+        dcol[:, :, k] = dfirst(k, corr)
+        # forward elimination
+        if k == 0:
+            divided = np.divide(1.0, bcol)
+            np.multiply(ccol[:, :, k], divided, out=ccol[:, :, k])
+            np.multiply(dcol[:, :, k], divided, out=dcol[:, :, k])
+        else:
+            divided = np.divide(1.0, np.subtract(bcol, np.multiply(ccol[:, :, k - 1], acol)))
+            if k < K - 1:
+                np.multiply(ccol[:, :, k], divided, out=ccol[:, :, k])
+            t = np.subtract(dcol[:, :, k], np.multiply(dcol[:, :, k - 1], acol))
+            np.multiply(t, divided, out=dcol[:, :, k])
+
+    data = dcol[:, :, K - 1].copy()
+    utens_stage[:, :, K - 1] = np.multiply(dtr, np.subtract(data, u_pos[:, :, K - 1]))
+    for k in range(K - 2, -1, -1):
+        data = np.subtract(dcol[:, :, k], np.multiply(ccol[:, :, k], data))
+        utens_stage[:, :, k] = np.multiply(dtr, np.subtract(data, u_pos[:, :, k]))

@@ -9,6 +9,9 @@ It imports the reference's own NumPy kernels
 * ``npbench.benchmarks.polybench.jacobi_2d.jacobi_2d_numpy.kernel``
 * ``npbench.benchmarks.polybench.heat_3d.heat_3d_numpy.kernel``
 * ``npbench.benchmarks.weather_stencils.hdiff.hdiff_numpy.hdiff``
+* ``npbench.benchmarks.polybench.jacobi_1d.jacobi_1d_numpy.kernel``
+* ``npbench.benchmarks.polybench.fdtd_2d.fdtd_2d_numpy.kernel``
+* ``npbench.benchmarks.weather_stencils.vadv.vadv_numpy.vadv``
 
 and their ``initialize`` functions, runs them on seeded inputs, and writes
 
@@ -59,6 +62,7 @@ def main():
     from npbench.benchmarks.weather_stencils.hdiff import hdiff_numpy, hdiff
     from npbench.benchmarks.polybench.jacobi_1d import jacobi_1d_numpy, jacobi_1d
     from npbench.benchmarks.polybench.fdtd_2d import fdtd_2d_numpy, fdtd_2d
+    from npbench.benchmarks.weather_stencils.vadv import vadv_numpy, vadv
 
     arrays, cases = {}, []
     rng = np.random.default_rng(20211)
@@ -179,6 +183,80 @@ def main():
         ex, ey, hz, fict = fdtd_2d.initialize(20, 200, 220, dt)
         add_fdtd_case(f"fdtd_2d/{dt.__name__}/presetS", 20, ex, ey, hz, fict, store=False,
                       init="reference", TMAX=20, NX=200, NY=220)
+
+    # vadv (float64; K >= 2).  Its own generator, so the cases above keep their draws.
+    vrng = np.random.default_rng(20212)
+
+    def add_vadv_case(name, us, u, w, up, ut, dtr, store=True, **meta):
+        out = us.copy()
+        vadv_numpy.vadv(out, u, w, up, ut, dtr)
+        case = dict(name=name, bench="vadv", dtype="float64", shape=list(us.shape),
+                    dtr_stage=float(dtr), **meta)
+        if store:
+            for k, v in (("utens_stage_in", us), ("u_stage", u), ("wcon", w), ("u_pos", up),
+                         ("utens", ut), ("utens_stage_out", out)):
+                arrays[f"{name}/{k}"] = v
+        else:
+            case.update(sha_in=sha(us), sha_out=sha(out))
+        cases.append(case)
+
+    for (I, J, K) in [(1, 1, 2), (1, 1, 3), (2, 3, 2), (3, 2, 5), (0, 3, 4), (3, 0, 4),
+                      (5, 4, 17), (7, 9, 33), (16, 8, 40)]:
+        for dtr in (3.0 / 20.0, 0.7):
+            us, u, up, ut = (vrng.random((I, J, K)) for _ in range(4))
+            w = vrng.random((I + 1, J, K))
+            add_vadv_case(f"vadv/float64/{I}x{J}x{K}/dtr{dtr:g}", us, u, w, up, ut, dtr)
+    # Full special pool (NaN and inf spread along the columns).
+    us, u, up, ut = (special_values(vrng, (6, 7, 9), np.float64) for _ in range(4))
+    w = special_values(vrng, (7, 7, 9), np.float64)
+    add_vadv_case("vadv/float64/special", us, u, w, up, ut, 0.15, special=True)
+    # Finite edge values: signed zeros, subnormal and tiny wcon sums, exact cancellations,
+    # negatives and repeated u levels (zero differences).
+    us, u, up, ut = (vrng.random((5, 6, 12)) for _ in range(4))
+    w = vrng.random((6, 6, 12))
+    flat = w.reshape(-1)
+    pool = np.array([0.0, -0.0, 5e-324, -2.5e-320, 2.0 ** -1021, 2.0 ** -1019, 2.0 ** -1018,
+                     -0.5, 1e-300])
+    idx = vrng.choice(flat.size, size=flat.size // 3, replace=False)
+    flat[idx] = pool[vrng.integers(0, pool.size, size=idx.size)]
+    w[1:4, :, 3] = -w[0:3, :, 3]          # w sums of exactly zero
+    u[:, :, 5] = u[:, :, 4]               # zero differences
+    u[:, ::2, 7] = -0.0
+    u[:, 1::2, 6] = 0.0
+    us[0, 0, :] = -us[0, 0, :]
+    add_vadv_case("vadv/float64/edge", us, u, w, up, ut, 0.15, special=True)
+    # Signed zeros through the whole solve: u constant along K (zero differences),
+    # or alternating +0/-0; with u_pos = +0, utens = utens_stage = -0 and a
+    # negative dtr_stage, the sign of each zero difference reaches the output
+    # (a solver that takes -(previous product) for (-as)*(u[k-1] - u[k]) without
+    # IEEE's rule for zero differences gets a third of these outputs wrong).
+    for K in (8, 6):
+        I, J = 3, 4
+        us, u, up, ut = (vrng.random((I, J, K)) for _ in range(4))
+        w = vrng.random((I + 1, J, K))
+        u[0, :, :] = 0.5
+        u[1, 0, :] = 0.0
+        u[1, 1, :] = -0.0
+        u[1, 2, :] = np.where(np.arange(K) % 2 == 0, 0.0, -0.0)
+        u[1, 3, :] = np.where(np.arange(K) % 2 == 0, -0.0, 0.0)
+        up[0:2] = 0.0
+        ut[0:2] = -0.0
+        us[0:2] = -0.0
+        add_vadv_case(f"vadv/float64/zeros/K{K}", us, u, w, up, ut, -0.15, special=True)
+    # Preset S with the reference initializer (default_rng(42)).
+    dtr, us, u, w, up, ut = vadv.initialize(60, 60, 40)
+    add_vadv_case("vadv/float64/presetS", us, u, w, up, ut, dtr, store=False, init="reference",
+                  I=60, J=60, K=40)
+    # K < 2: the reference raises IndexError (it reads level 1 unconditionally).
+    for K in (0, 1):
+        z = np.zeros((2, 3, K))
+        try:
+            vadv_numpy.vadv(z.copy(), z, np.zeros((3, 3, K)), z, z, 0.15)
+            raised = None
+        except Exception as e:  # noqa: BLE001 - record what the reference raises
+            raised = type(e).__name__
+        cases.append(dict(name=f"vadv/float64/K{K}", bench="vadv", dtype="float64",
+                          shape=[2, 3, K], dtr_stage=0.15, raises=raised))
 
     np.savez_compressed(os.path.join(HERE, "cases.npz"), **arrays)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:

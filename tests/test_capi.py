@@ -59,6 +59,23 @@ def test_argument_errors_are_status_codes_not_crashes():
     assert b"alias" in lib.npbgb_last_error()
     assert lib.npbgb_heat3d(ctypes.c_void_p(4096), ctypes.c_void_p(8192), 8, 8, 8, 3, 7,
                             None) == _lib.NPBGB_ERR_DTYPE
+    assert lib.npbgb_vadv(None, None, None, None, None, 0.15, 4, 4, 4, _lib.NPBGB_F32, None, 0,
+                          None) == _lib.NPBGB_ERR_DTYPE
+    assert lib.npbgb_vadv(None, None, None, None, None, 0.15, 4, 4, 1, _lib.NPBGB_F64, None, 0,
+                          None) == _lib.NPBGB_ERR_ARG
+    assert b"level 1" in lib.npbgb_last_error()
+    assert lib.npbgb_vadv(None, None, None, None, None, 0.15, 4, 4, 4, _lib.NPBGB_F64, None, 0,
+                          None) == _lib.NPBGB_ERR_ARG
+    assert b"null" in lib.npbgb_last_error()
+    p = [ctypes.c_void_p(4096 * (i + 1)) for i in range(5)]
+    assert lib.npbgb_vadv(p[0], p[1], p[2], p[3], p[0], 0.15, 4, 4, 4, _lib.NPBGB_F64, None, 0,
+                          None) == _lib.NPBGB_ERR_ARG
+    assert b"alias" in lib.npbgb_last_error()
+    assert lib.npbgb_vadv(*p, 0.15, 4, 4, 4, _lib.NPBGB_F64, ctypes.c_void_p(65536), 8,
+                          None) == _lib.NPBGB_ERR_ARG
+    assert b"workspace" in lib.npbgb_last_error()
+    assert lib.npbgb_vadv_workspace_bytes(256, 256, 160) == 8 * 159 * 256 * 256
+    assert lib.npbgb_vadv_workspace_bytes(4, 4, 1) == 0
 
 
 def test_noop_sizes_return_ok_without_touching_memory():
@@ -68,6 +85,8 @@ def test_noop_sizes_return_ok_without_touching_memory():
     assert lib.npbgb_jacobi2d(None, None, 2, 100, 50, _lib.NPBGB_F32, None) == _lib.NPBGB_OK
     assert lib.npbgb_heat3d(None, None, 100, 2, 100, 50, _lib.NPBGB_F64, None) == _lib.NPBGB_OK
     assert lib.npbgb_hdiff(None, None, None, 0, 5, 5, _lib.NPBGB_F64, None) == _lib.NPBGB_OK
+    assert lib.npbgb_vadv(None, None, None, None, None, 0.15, 0, 5, 5, _lib.NPBGB_F64, None, 0,
+                          None) == _lib.NPBGB_OK
 
 
 def test_python_errors_mirror_reference_behaviour():
@@ -87,6 +106,17 @@ def test_python_errors_mirror_reference_behaviour():
         stencils.jacobi_2d_kernel(3, a, a)
     with pytest.raises(ValueError):
         stencils.heat_3d_kernel(3, np.zeros((4, 4)), np.zeros((4, 4)))
+    z = np.zeros((3, 4, 5))
+    with pytest.raises(ValueError):
+        stencils.vadv(z.copy(), z, np.zeros((3, 4, 5)), z, z, 0.15)   # wcon must be (I+1, J, K)
+    with pytest.raises(TypeError):
+        stencils.vadv(z.astype(np.float32), z.astype(np.float32), np.zeros((4, 4, 5), np.float32),
+                      z.astype(np.float32), z.astype(np.float32), 0.15)
+    with pytest.raises(ValueError):
+        stencils.vadv(z, z, np.zeros((4, 4, 5)), z.copy(), z.copy(), 0.15)  # output aliases input
+    z1 = np.zeros((3, 4, 1))
+    with pytest.raises(IndexError):
+        stencils.vadv(z1.copy(), z1, np.zeros((4, 4, 1)), z1, z1, 0.15)
 
 
 def test_missing_library_fails_loudly(monkeypatch, tmp_path):

@@ -78,6 +78,28 @@ def test_fdtd_golden(golden, which):
 
 
 @pytest.mark.parametrize("which", sorted(ORACLES))
+def test_vadv_golden(golden, which):
+    _, arrays = golden
+    n = 0
+    with np.errstate(all="ignore"):
+        for c in _cases(golden, "vadv"):
+            name = c["name"]
+            if "raises" in c:
+                I, J, K = c["shape"]
+                z = np.zeros((I, J, K))
+                with pytest.raises(IndexError):
+                    ORACLES[which].vadv(z.copy(), z, np.zeros((I + 1, J, K)), z, z, c["dtr_stage"])
+                continue
+            us = arrays[f"{name}/utens_stage_in"].copy()
+            ORACLES[which].vadv(us, *(arrays[f"{name}/{k}"] for k in
+                                      ("u_stage", "wcon", "u_pos", "utens")), c["dtr_stage"])
+            exp = arrays[f"{name}/utens_stage_out"]
+            assert bits_equal(us, exp), (name, first_diff(us, exp))
+            n += 1
+    assert n >= 20
+
+
+@pytest.mark.parametrize("which", sorted(ORACLES))
 def test_reference_initializer_presets(golden, which):
     """Preset S with the reference's own initializers, checked by SHA-256."""
     o = ORACLES[which]
@@ -91,6 +113,13 @@ def test_reference_initializer_presets(golden, which):
             o.fdtd_2d_kernel(c["tsteps"], ex, ey, hz, fict)
             assert (_sha(ex), _sha(ey), _sha(hz)) == (c["sha_ex_out"], c["sha_ey_out"],
                                                       c["sha_hz_out"]), c["name"]
+            seen += 1
+            continue
+        if c["bench"] == "vadv":
+            dtr, us, u, w, up, ut = workloads.init_vadv(c["I"], c["J"], c["K"])
+            assert _sha(us) == c["sha_in"] and dtr == c["dtr_stage"], c["name"]
+            o.vadv(us, u, w, up, ut, dtr)
+            assert _sha(us) == c["sha_out"], c["name"]
             seen += 1
             continue
         if c["bench"] == "jacobi_1d":
@@ -114,7 +143,7 @@ def test_reference_initializer_presets(golden, which):
         kern(c["tsteps"], A, B)
         assert _sha(A) == c["sha_A_out"] and _sha(B) == c["sha_B_out"], c["name"]
         seen += 1
-    assert seen == 9
+    assert seen == 10
 
 
 def test_oracles_agree_on_random_nonsquare():

@@ -3,8 +3,9 @@
 * every stored golden case (reference NumPy outputs) -- bit for bit;
 * preset S with the reference initializers -- SHA-256 of the outputs;
 * seeded U[0,1) grids at the full benchmark sizes (Jacobi-2D 1000^2 x 100
-  steps, Heat-3D 256^3 x 100 steps in float64 and float32, hdiff
-  256x256x160) against the C oracle -- bit for bit;
+  steps, Heat-3D 256^3 x 100 steps in float64 and float32, hdiff and vadv
+  256x256x160, Jacobi-1D and FDTD-2D paper presets) against the C oracle --
+  bit for bit;
 * host NumPy arrays through the same entry points (copy in, copy back).
 
 Bit-exact means identical bit patterns, except that any NaN matches any NaN.
@@ -94,6 +95,72 @@ def test_golden_fdtd_bit_exact(golden):
     assert n >= 20
 
 
+def _vadv_args(arrays, name):
+    return [_dev(arrays[f"{name}/{k}"]) for k in ("u_stage", "wcon", "u_pos", "utens")]
+
+
+def test_golden_vadv_bit_exact(golden):
+    manifest, arrays = golden
+    n = 0
+    for c in manifest["cases"]:
+        if c["bench"] != "vadv" or "init" in c:
+            continue
+        name = c["name"]
+        if "raises" in c:
+            I, J, K = c["shape"]
+            z = torch.zeros((I, J, K), dtype=torch.float64, device=DEV)
+            with pytest.raises(IndexError):
+                stencils.vadv(z.clone(), z, torch.zeros((I + 1, J, K), dtype=torch.float64,
+                                                        device=DEV), z, z, c["dtr_stage"])
+            continue
+        us = _dev(arrays[f"{name}/utens_stage_in"])
+        stencils.vadv(us, *_vadv_args(arrays, name), c["dtr_stage"])
+        o, exp = _host(us), arrays[f"{name}/utens_stage_out"]
+        assert bits_equal(o, exp), (name, first_diff(o, exp))
+        n += 1
+    assert n >= 20
+
+
+def test_vadv_library_allocated_workspace(golden):
+    """workspace = NULL: the call allocates and frees its workspace stream-ordered."""
+    from npbench_gb300 import _lib
+    _, arrays = golden
+    name = "vadv/float64/16x8x40/dtr0.7"
+    us = _dev(arrays[f"{name}/utens_stage_in"])
+    u, w, up, ut = _vadv_args(arrays, name)
+    lib = _lib.load()
+    st = lib.npbgb_vadv(us.data_ptr(), u.data_ptr(), w.data_ptr(), up.data_ptr(), ut.data_ptr(),
+                        0.7, 16, 8, 40, _lib.NPBGB_F64, None, 0,
+                        torch.cuda.current_stream(DEV).cuda_stream)
+    _lib.check(st, "vadv")
+    assert bits_equal(_host(us), arrays[f"{name}/utens_stage_out"])
+
+
+def test_vadv_paper_size_vs_oracle():
+    rng = np.random.default_rng(17)
+    I, J, K = 256, 256, 160
+    us, u, up, ut = (rng.random((I, J, K)) for _ in range(4))
+    w = rng.random((I + 1, J, K))
+    d = _dev(us)
+    stencils.vadv(d, _dev(u), _dev(w), _dev(up), _dev(ut), 3.0 / 20.0)
+    cref.vadv(us, u, w, up, ut, 3.0 / 20.0)
+    o = _host(d)
+    assert bits_equal(o, us), first_diff(o, us)
+
+
+@pytest.mark.parametrize("IJK", [(1, 1, 2), (3, 5, 2), (7, 3, 3), (65, 1, 9), (33, 31, 7),
+                                 (2, 700, 5)])
+def test_vadv_ragged_shapes(IJK):
+    I, J, K = IJK
+    rng = np.random.default_rng(I * 10000 + J * 100 + K)
+    us, u, up, ut = (rng.random((I, J, K)) for _ in range(4))
+    w = rng.random((I + 1, J, K))
+    d = _dev(us)
+    stencils.vadv(d, _dev(u), _dev(w), _dev(up), _dev(ut), 0.15)
+    cref.vadv(us, u, w, up, ut, 0.15)
+    assert bits_equal(_host(d), us), IJK
+
+
 def test_reference_initializer_presets(golden):
     seen = 0
     for c in golden[0]["cases"]:
@@ -111,6 +178,11 @@ def test_reference_initializer_presets(golden):
             o = _dev(out)
             stencils.hdiff(_dev(inf), o, _dev(coeff))
             assert _sha(_host(o)) == c["sha_out"], c["name"]
+        elif c["bench"] == "vadv":
+            dtr, us, u, w, up, ut = workloads.init_vadv(c["I"], c["J"], c["K"])
+            d = _dev(us)
+            stencils.vadv(d, _dev(u), _dev(w), _dev(up), _dev(ut), dtr)
+            assert _sha(_host(d)) == c["sha_out"], c["name"]
         else:
             A, B = INITS[c["bench"]](c["N"], np.dtype(c["dtype"]).type)
             dA, dB = _dev(A), _dev(B)
@@ -118,7 +190,7 @@ def test_reference_initializer_presets(golden):
             assert _sha(_host(dA)) == c["sha_A_out"], c["name"]
             assert _sha(_host(dB)) == c["sha_B_out"], c["name"]
         seen += 1
-    assert seen == 9
+    assert seen == 10
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
@@ -128,7 +200,8 @@ def test_jacobi_1d_paper_size_vs_oracle(dtype):
     stencils.jacobi_1d_kernel(4000, dA, dB)
     cref.jacobi_1d_kernel(4000, A, B)
     assert bits_equal(_host(dA), A) and bits_equal(_host(dB), B)
-    for n, T in ((3, 5), (1026, 17), (2049, 34), (5000, 3)):
+    # Sizes that select each segment width (128, 256, 512, 1024 points per CTA).
+    for n, T in ((3, 5), (1026, 17), (2049, 34), (5000, 3), (50000, 40), (400000, 9)):
         A, B = workloads.uniform_pair((n,), dtype, seed=n)
         dA, dB = _dev(A), _dev(B)
         stencils.jacobi_1d_kernel(T, dA, dB)

@@ -52,7 +52,8 @@ for name, fn, mod in [("jacobi_2d", "kernel", "npbench.benchmarks.polybench.jaco
                       ("heat_3d", "kernel", "npbench.benchmarks.polybench.heat_3d.heat_3d_gb300"),
                       ("hdiff", "hdiff", "npbench.benchmarks.weather_stencils.hdiff.hdiff_gb300"),
                       ("jacobi_1d", "kernel", "npbench.benchmarks.polybench.jacobi_1d.jacobi_1d_gb300"),
-                      ("fdtd_2d", "kernel", "npbench.benchmarks.polybench.fdtd_2d.fdtd_2d_gb300")]:
+                      ("fdtd_2d", "kernel", "npbench.benchmarks.polybench.fdtd_2d.fdtd_2d_gb300"),
+                      ("vadv", "vadv", "npbench.benchmarks.weather_stencils.vadv.vadv_gb300")]:
     b = Benchmark(name)
     impl, label = f.implementations(b)[0]
     assert impl.__module__ == mod and impl.__name__ == fn and label == "default", impl
@@ -78,10 +79,14 @@ def test_install_is_idempotent(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("bench", ["jacobi_2d", "heat_3d", "hdiff", "jacobi_1d", "fdtd_2d"])
+@pytest.mark.parametrize("bench", ["jacobi_2d", "heat_3d", "hdiff", "jacobi_1d", "fdtd_2d",
+                                   "vadv"])
 def test_harness_runs_and_validates_plugin(tmp_path, bench):
     if not os.path.isdir(os.path.join(BUILT_TREE, "npbench", "infrastructure")):
         pytest.skip("baseline/_ref/npbench was not built")
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
     import shutil
     tree = str(tmp_path / "npbench")
     shutil.copytree(BUILT_TREE, tree)
