@@ -179,6 +179,45 @@ NPBGB_API int32_t npbgb_vadv(void* utens_stage, const void* u_stage, const void*
                              int64_t J, int64_t K, int32_t dtype, void* workspace,
                              int64_t workspace_bytes, void* stream);
 
+/* Lid-driven cavity flow, the whole time loop of
+ *   cavity_flow(nx, ny, nt, nit, u, v, dt, dx, dy, p, rho, nu)
+ *                               cavity_flow/cavity_flow_numpy.py:41-82
+ * u, v, p are (ny, nx) and updated in place.  Per time step: build_up_b, nit
+ * pressure iterations with the reference's boundary statements, the momentum
+ * updates and the walls, every operation rounded as NumPy rounds it (the
+ * scalars dx**2 etc. are formed with the C library's pow, as Python's float
+ * power is).  One cooperative persistent launch runs all nt steps.
+ * dtype must be NPBGB_F64.  With nt >= 1, ny or nx below 1, or below 2 when
+ * nit >= 1, is NPBGB_ERR_ARG (the reference raises IndexError).  Grids of 3 x 3
+ * and more need a workspace of npbgb_cavity_flow_workspace_bytes(ny, nx)
+ * (four fields and the band counters); pass it, or NULL to have the call
+ * allocate and free it stream-ordered.  Bounded waits: a band that sees no
+ * progress from its neighbours for two seconds records an error reported by
+ * npbgb_device_status. */
+NPBGB_API int64_t npbgb_cavity_flow_workspace_bytes(int64_t ny, int64_t nx);
+NPBGB_API int32_t npbgb_cavity_flow(void* u, void* v, void* p, int64_t ny, int64_t nx, int32_t nt,
+                                    int32_t nit, double dt, double dx, double dy, double rho,
+                                    double nu, int32_t dtype, void* workspace,
+                                    int64_t workspace_bytes, void* stream);
+
+/* Channel flow, the whole convergence loop of
+ *   channel_flow(nit, u, v, dt, dx, dy, p, rho, nu, F)
+ *                               channel_flow/channel_flow_numpy.py:69-152
+ * u, v, p are (ny, nx), periodic in x, updated in place; the loop runs while
+ * (sum(u) - sum(un)) / sum(u) > .001, the sums being np.sum's (+0.0 plus
+ * NumPy's pairwise summation) bit for bit, so the step count matches the
+ * reference's.  *steps (if not NULL; the call then synchronizes `stream`)
+ * receives it, negated if max_steps steps ran without converging.  dtype must
+ * be NPBGB_F64.  nx < 2, ny < 1, or ny < 2 with nit >= 1 is NPBGB_ERR_ARG (the
+ * reference raises IndexError).  Workspace: npbgb_channel_flow_workspace_bytes
+ * (ny, nx) bytes, or NULL for a stream-ordered allocation inside the call. */
+NPBGB_API int64_t npbgb_channel_flow_workspace_bytes(int64_t ny, int64_t nx);
+NPBGB_API int32_t npbgb_channel_flow(void* u, void* v, void* p, int64_t ny, int64_t nx,
+                                     int32_t nit, double dt, double dx, double dy, double rho,
+                                     double nu, double F, int64_t max_steps, int32_t dtype,
+                                     void* workspace, int64_t workspace_bytes, int64_t* steps,
+                                     void* stream);
+
 /* Batches: many independent grids advanced by one persistent launch.
  *
  * npbgb_batch_create plans a batch of Jacobi-2D and Heat-3D grids: each grid

@@ -65,6 +65,13 @@ SIGNATURES = {
     "npbgb_jacobi1d": (_i32, [_vp, _vp, _i64, _i32, _i32, _vp]),
     "npbgb_fdtd2d": (_i32, [_vp, _vp, _vp, _vp, _i64, _i64, _i64, _i32, _i32, _vp]),
     "npbgb_vadv_workspace_bytes": (_i64, [_i64, _i64, _i64]),
+    "npbgb_cavity_flow_workspace_bytes": (_i64, [_i64, _i64]),
+    "npbgb_channel_flow_workspace_bytes": (_i64, [_i64, _i64]),
+    "npbgb_channel_flow": (_i32, [_vp, _vp, _vp, _i64, _i64, _i32] + [ctypes.c_double] * 6 +
+                           [_i64, _i32, _vp, _i64, ctypes.POINTER(ctypes.c_int64), _vp]),
+    "npbgb_cavity_flow": (_i32, [_vp, _vp, _vp, _i64, _i64, _i32, _i32, ctypes.c_double,
+                                 ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                 ctypes.c_double, _i32, _vp, _i64, _vp]),
     "npbgb_vadv": (_i32, [_vp, _vp, _vp, _vp, _vp, ctypes.c_double, _i64, _i64, _i64, _i32, _vp,
                           _i64, _vp]),
 }

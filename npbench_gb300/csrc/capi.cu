@@ -23,6 +23,7 @@ int64_t g_cfg_jacobi_chunk = 0;
 
 uint32_t take_heat_device_error();
 uint32_t take_batch_device_error();
+uint32_t take_cfd_device_error();
 int32_t launch_wait_timeout_selftest(uint64_t limit_ns, cudaStream_t st);
 
 int32_t set_error(int32_t code, const char* fmt, ...) {
@@ -162,10 +163,12 @@ int32_t npbgb_device_status(void* stream) {
   if (e != cudaSuccess) return cuda_status(e, "device status");
   const uint32_t h = take_heat_device_error();
   const uint32_t bt = take_batch_device_error();
-  if (h == 0xffffffffu || bt == 0xffffffffu)
+  const uint32_t cf = take_cfd_device_error();
+  if (h == 0xffffffffu || bt == 0xffffffffu || cf == 0xffffffffu)
     return set_error(NPBGB_ERR_CUDA, "reading the device error words");
   if (h) return set_error(NPBGB_ERR_TIMEOUT, "a bounded device wait gave up (heat3d)");
   if (bt) return set_error(NPBGB_ERR_TIMEOUT, "a batch CTA made no progress within its limit");
+  if (cf) return set_error(NPBGB_ERR_TIMEOUT, "a cavity_flow band waited on its neighbours past its limit");
   return NPBGB_OK;
 }
 

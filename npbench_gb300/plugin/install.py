@@ -14,6 +14,8 @@ Adds, under NPBENCH_ROOT (the directory holding ``framework_info/``,
 * ``npbench/benchmarks/polybench/jacobi_1d/jacobi_1d_gb300.py``
 * ``npbench/benchmarks/polybench/fdtd_2d/fdtd_2d_gb300.py``
 * ``npbench/benchmarks/weather_stencils/vadv/vadv_gb300.py``
+* ``npbench/benchmarks/cavity_flow/cavity_flow_gb300.py``
+* ``npbench/benchmarks/channel_flow/channel_flow_gb300.py``
 
 and appends ``from .gb300_framework import *`` to
 ``npbench/infrastructure/__init__.py`` (once).  ``--copy-from`` first copies a
@@ -36,6 +38,8 @@ FILES = [
     "benchmarks/polybench/jacobi_1d/jacobi_1d_gb300.py",
     "benchmarks/polybench/fdtd_2d/fdtd_2d_gb300.py",
     "benchmarks/weather_stencils/vadv/vadv_gb300.py",
+    "benchmarks/cavity_flow/cavity_flow_gb300.py",
+    "benchmarks/channel_flow/channel_flow_gb300.py",
 ]
 IMPORT_LINE = "from .gb300_framework import *\n"
 

@@ -15,6 +15,7 @@ jacobi_f64 Jacobi-2D 4096^2 float64, TSTEPS=3             jacobi2d_strip, -s 2
 jacobi_f32 Jacobi-2D 4096^2 float32, TSTEPS=3             jacobi2d_strip, -s 2
 hdiff      hdiff 256x256x160 float64, 3 calls             hdiff_tile, -s 1
 vadv       vadv 256x256x160 float64, 3 calls              vadv_columns, -s 1
+cavity     cavity_flow 101x101, nt=20, nit=50, 2 calls    cavity_bands, -s 1
 batch      256 mixed Jacobi-2D grids, 2 launches          batch_persistent, -s 1
 ========== ============================================== ===================
 """
@@ -48,6 +49,11 @@ def run(case):
         a, b, c, d, e = (torch.from_numpy(t).to(dev) for t in (us, u, w, up, ut))
         for _ in range(3):
             stencils.vadv(a, b, c, d, e, dtr)
+    elif case == "cavity":
+        u, v, p, dx, dy, dt = workloads.init_cavity_flow(101, 101)
+        a, b, c = (torch.from_numpy(t).to(dev) for t in (u, v, p))
+        for _ in range(2):
+            stencils.cavity_flow(101, 101, 20, 50, a, b, dt, dx, dy, c, 1.0, 0.1)
     elif case == "batch":
         from npbench_gb300.batch import Batch
         specs = workloads.batch_jacobi_specs(256, seed=0, tsteps=(10, 40))

@@ -9,6 +9,10 @@ These are drop-ins for the reference NumPy kernels:
 * ``fdtd_2d_kernel(TMAX, ex, ey, hz, _fict_)`` -- polybench/fdtd_2d/fdtd_2d_numpy.py:4
 * ``vadv(utens_stage, u_stage, wcon, u_pos, utens, dtr_stage)`` --
   weather_stencils/vadv/vadv_numpy.py:9
+* ``cavity_flow(nx, ny, nt, nit, u, v, dt, dx, dy, p, rho, nu)`` --
+  cavity_flow/cavity_flow_numpy.py:41
+* ``channel_flow(nit, u, v, dt, dx, dy, p, rho, nu, F)`` --
+  channel_flow/channel_flow_numpy.py:69 (returns the step count)
 
 Arguments are updated in place and nothing is returned, as in the reference.
 They may be
@@ -19,7 +23,7 @@ They may be
   updated there and copied back into the same NumPy arrays before returning.
 
 Results are bit-identical to the reference NumPy kernels for float64 and
-float32 (hdiff and vadv: float64 only).  Errors raise ``TypeError`` (dtype),
+float32 (hdiff, vadv, cavity_flow and channel_flow: float64 only).  Errors raise ``TypeError`` (dtype),
 ``ValueError`` (shape, device, aliasing) or ``npbench_gb300.NpbgbError``
 (a status from the library).  There is no CPU fallback: without a CUDA device
 or without libnpbgb.so these functions raise.
@@ -29,7 +33,7 @@ import numpy as np
 from . import _lib
 
 __all__ = ["jacobi_2d_kernel", "heat_3d_kernel", "hdiff", "jacobi_1d_kernel", "fdtd_2d_kernel",
-           "vadv"]
+           "vadv", "cavity_flow", "channel_flow"]
 
 
 def _torch():
@@ -239,3 +243,80 @@ def vadv(utens_stage, u_stage, wcon, u_pos, utens, dtr_stage):
                             float(dtr_stage), I, J, K, code, ws.data_ptr(), nbytes, view.stream)
         _lib.check(st, "vadv")
         view.finish()
+
+
+def cavity_flow(nx, ny, nt, nit, u, v, dt, dx, dy, p, rho, nu):
+    """``cavity_flow(nx, ny, nt, nit, u, v, dt, dx, dy, p, rho, nu)`` of
+    cavity_flow/cavity_flow_numpy.py:41-82; updates u, v and p in place.
+
+    The whole time loop is one persistent launch; its workspace (four fields
+    and the band counters) comes from PyTorch's caching allocator.  Sizes the
+    reference's boundary statements cannot index raise IndexError, as there.
+    """
+    ny, nx, nt, nit = int(ny), int(nx), int(nt), int(nit)
+    _check_same((u, v, p), ("u", "v", "p"))
+    if tuple(u.shape) != (ny, nx):
+        raise ValueError(f"cavity_flow: arrays are {tuple(u.shape)}, expected (ny, nx) = "
+                         f"{(ny, nx)}")
+    code = _dtype_code(u.dtype, allowed=(np.float64,))
+    for x, y, a, b in (("u", "v", u, v), ("u", "p", u, p), ("v", "p", v, p)):
+        if _shares_memory(a, b):
+            raise ValueError(f"cavity_flow: {x} and {y} share memory")
+    if nt > 0 and (ny < 1 or nx < 1 or (nit > 0 and (ny < 2 or nx < 2))):
+        raise IndexError(f"cavity_flow: a ({ny}, {nx}) grid is too small for the boundary "
+                         "statements")
+    if nt < 0 or nit < 0:
+        raise ValueError("cavity_flow: negative nt or nit")
+    lib = _lib.load()
+    torch = _torch()
+    view = _DeviceView((u, v, p), (True, True, True))
+    with torch.cuda.device(view.device):
+        nbytes = int(lib.npbgb_cavity_flow_workspace_bytes(ny, nx))
+        ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=view.device)
+        st = lib.npbgb_cavity_flow(view.ptr(0), view.ptr(1), view.ptr(2), ny, nx, nt, nit,
+                                   float(dt), float(dx), float(dy), float(rho), float(nu), code,
+                                   ws.data_ptr(), nbytes, view.stream)
+        _lib.check(st, "cavity_flow")
+        view.finish()
+
+
+def channel_flow(nit, u, v, dt, dx, dy, p, rho, nu, F, max_steps=1_000_000):
+    """``channel_flow(nit, u, v, dt, dx, dy, p, rho, nu, F)`` of
+    channel_flow/channel_flow_numpy.py:69-152; updates u, v, p in place and
+    returns the step count, which matches the reference's because its
+    convergence sums are np.sum's bit for bit.
+
+    ``max_steps`` bounds the loop (the reference's has no bound); reaching it
+    without convergence raises RuntimeError, with u, v, p left at that step.
+    """
+    import ctypes
+    nit = int(nit)
+    _check_same((u, v, p), ("u", "v", "p"))
+    if len(u.shape) != 2:
+        raise ValueError(f"channel_flow: expected 2-D arrays, got shape {tuple(u.shape)}")
+    ny, nx = (int(x) for x in u.shape)
+    code = _dtype_code(u.dtype, allowed=(np.float64,))
+    for x, y, a, b in (("u", "v", u, v), ("u", "p", u, p), ("v", "p", v, p)):
+        if _shares_memory(a, b):
+            raise ValueError(f"channel_flow: {x} and {y} share memory")
+    if nx < 2 or ny < 1 or (nit > 0 and ny < 2):
+        raise IndexError(f"channel_flow: a ({ny}, {nx}) grid is too small for the boundary "
+                         "statements")
+    if nit < 0 or int(max_steps) < 1:
+        raise ValueError("channel_flow: negative nit or max_steps < 1")
+    lib = _lib.load()
+    torch = _torch()
+    view = _DeviceView((u, v, p), (True, True, True))
+    steps = ctypes.c_int64(0)
+    with torch.cuda.device(view.device):
+        nbytes = int(lib.npbgb_channel_flow_workspace_bytes(ny, nx))
+        ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=view.device)
+        st = lib.npbgb_channel_flow(view.ptr(0), view.ptr(1), view.ptr(2), ny, nx, nit,
+                                    float(dt), float(dx), float(dy), float(rho), float(nu),
+                                    float(F), int(max_steps), code, ws.data_ptr(), nbytes,
+                                    ctypes.byref(steps), view.stream)
+        _lib.check(st, "channel_flow")
+        view.finish()
+    if steps.value < 0:
+        raise RuntimeError(f"channel_flow: no convergence within {max_steps} steps")
+    return int(steps.value)

@@ -10,6 +10,11 @@
 * ``init_vadv(I, J, K)`` restates weather_stencils/vadv/vadv.py:6-19:
   ``dtr_stage = 3/20`` and ``default_rng(42)`` draws ``utens_stage``,
   ``u_stage``, ``wcon (I+1,J,K)``, ``u_pos``, ``utens`` in that order.
+* ``init_cavity_flow(ny, nx)`` restates cavity_flow/cavity_flow.py:6-13:
+  zero u, v, p and ``dx = 2/(nx-1)``, ``dy = 2/(ny-1)``,
+  ``dt = .1/((nx-1)*(ny-1))``.
+* ``init_channel_flow(ny, nx)`` restates channel_flow/channel_flow.py:6-13
+  (as cavity_flow's, but p = 1).
 * ``uniform_pair`` / ``uniform_heat`` draw U[0,1) fields from
   ``numpy.random.default_rng(seed)`` (float32 forms are casts of the float64
   draw, so both precisions see the same field).
@@ -25,6 +30,16 @@ PRESETS = {
               "L": {"I": 384, "J": 384, "K": 160}, "paper": {"I": 256, "J": 256, "K": 160}},
     "jacobi_1d": {"S": {"TSTEPS": 800, "N": 3200}, "M": {"TSTEPS": 3000, "N": 12000},
                   "L": {"TSTEPS": 8500, "N": 34000}, "paper": {"TSTEPS": 4000, "N": 32000}},
+    "cavity_flow": {"S": {"ny": 61, "nx": 61, "nt": 25, "nit": 5, "rho": 1.0, "nu": 0.1},
+                    "M": {"ny": 121, "nx": 121, "nt": 50, "nit": 10, "rho": 1.0, "nu": 0.1},
+                    "L": {"ny": 201, "nx": 201, "nt": 100, "nit": 20, "rho": 1.0, "nu": 0.1},
+                    "paper": {"ny": 101, "nx": 101, "nt": 700, "nit": 50, "rho": 1.0,
+                              "nu": 0.1}},
+    "channel_flow": {"S": {"ny": 61, "nx": 61, "nit": 5, "rho": 1.0, "nu": 0.1, "F": 1.0},
+                     "M": {"ny": 121, "nx": 121, "nit": 10, "rho": 1.0, "nu": 0.1, "F": 1.0},
+                     "L": {"ny": 201, "nx": 201, "nit": 20, "rho": 1.0, "nu": 0.1, "F": 1.0},
+                     "paper": {"ny": 101, "nx": 101, "nit": 50, "rho": 1.0, "nu": 0.1,
+                               "F": 1.0}},
     "vadv": {"S": {"I": 60, "J": 60, "K": 40}, "M": {"I": 112, "J": 112, "K": 80},
              "L": {"I": 180, "J": 180, "K": 160}, "paper": {"I": 256, "J": 256, "K": 160}},
     "fdtd_2d": {"S": {"TMAX": 20, "NX": 200, "NY": 220}, "M": {"TMAX": 60, "NX": 400, "NY": 450},
@@ -79,6 +94,28 @@ def init_vadv(I, J, K):
     u_pos = rng.random((I, J, K))
     utens = rng.random((I, J, K))
     return dtr_stage, utens_stage, u_stage, wcon, u_pos, utens
+
+
+def init_cavity_flow(ny, nx):
+    """Returns (u, v, p, dx, dy, dt)."""
+    u = np.zeros((ny, nx), dtype=np.float64)
+    v = np.zeros((ny, nx), dtype=np.float64)
+    p = np.zeros((ny, nx), dtype=np.float64)
+    dx = 2 / (nx - 1)
+    dy = 2 / (ny - 1)
+    dt = .1 / ((nx - 1) * (ny - 1))
+    return u, v, p, dx, dy, dt
+
+
+def init_channel_flow(ny, nx):
+    """channel_flow/channel_flow.py:6-13: u = v = 0, p = 1; returns (u, v, p, dx, dy, dt)."""
+    u = np.zeros((ny, nx), dtype=np.float64)
+    v = np.zeros((ny, nx), dtype=np.float64)
+    p = np.ones((ny, nx), dtype=np.float64)
+    dx = 2 / (nx - 1)
+    dy = 2 / (ny - 1)
+    dt = .1 / ((nx - 1) * (ny - 1))
+    return u, v, p, dx, dy, dt
 
 
 def uniform_pair(shape, dtype=np.float64, seed=0):

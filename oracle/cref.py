@@ -11,6 +11,11 @@ with the same call shapes as the reference kernels:
 * ``fdtd_2d_kernel(TMAX, ex, ey, hz, _fict_)`` -- polybench/fdtd_2d/fdtd_2d_numpy.py:4
 * ``vadv(utens_stage, u_stage, wcon, u_pos, utens, dtr_stage)`` --
   weather_stencils/vadv/vadv_numpy.py:9
+* ``cavity_flow(nx, ny, nt, nit, u, v, dt, dx, dy, p, rho, nu)`` --
+  cavity_flow/cavity_flow_numpy.py:41
+* ``channel_flow(nit, u, v, dt, dx, dy, p, rho, nu, F)`` --
+  channel_flow/channel_flow_numpy.py:69 (returns the step count)
+* ``numpy_sum(a)`` -- ``np.sum`` of a contiguous float64 array
 """
 import ctypes
 import os
@@ -44,6 +49,12 @@ def _bind(lib):
         getattr(lib, "oracle_jacobi1d_" + sfx).argtypes = [vp, vp, i64, i32]
         getattr(lib, "oracle_fdtd2d_" + sfx).argtypes = [vp, vp, vp, vp, i64, i64, i32]
     lib.oracle_vadv_f64.argtypes = [vp, vp, vp, vp, vp, ctypes.c_double, i64, i64, i64]
+    d = ctypes.c_double
+    lib.oracle_cavity_flow_f64.argtypes = [vp, vp, vp, i64, i64, i32, i32, d, d, d, d, d, vp]
+    lib.oracle_channel_flow_f64.argtypes = [vp, vp, vp, i64, i64, i32, d, d, d, d, d, d, vp, i64]
+    lib.oracle_channel_flow_f64.restype = i64
+    lib.oracle_numpy_sum_f64.argtypes = [vp, i64]
+    lib.oracle_numpy_sum_f64.restype = d
     return lib
 
 
@@ -123,3 +134,44 @@ def vadv(utens_stage, u_stage, wcon, u_pos, utens, dtr_stage):
         raise IndexError(f"vadv needs K >= 2 (reads level 1), got K={K}")
     lib().oracle_vadv_f64(_p(utens_stage), _p(u_stage), _p(wcon), _p(u_pos), _p(utens),
                           float(dtr_stage), I, J, K)
+
+
+_CFD_KEYS = ("two_dx", "two_dy", "inv_dt", "dx2", "dy2", "pD", "pC", "k1u", "k1v", "k2", "k3")
+
+
+def cavity_flow(nx, ny, nt, nit, u, v, dt, dx, dy, p, rho, nu):
+    from .stencils_np import cfd_constants
+    if _sfx(u, v, p) != "f64":
+        raise TypeError("cavity_flow oracle is float64 only")
+    if u.shape != (ny, nx) or v.shape != (ny, nx) or p.shape != (ny, nx):
+        raise ValueError("cavity_flow arrays must be (ny, nx)")
+    if int(nt) > 0 and int(nit) > 0 and (ny < 2 or nx < 2):
+        raise IndexError("cavity_flow: the pressure boundaries need ny >= 2 and nx >= 2")
+    k = cfd_constants(dt, dx, dy, rho)
+    kc = np.array([k[n] for n in _CFD_KEYS], dtype=np.float64)
+    lib().oracle_cavity_flow_f64(_p(u), _p(v), _p(p), ny, nx, int(nt), int(nit), float(dt),
+                                 float(dx), float(dy), float(rho), float(nu), _p(kc))
+
+
+def numpy_sum(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return lib().oracle_numpy_sum_f64(_p(a), a.size)
+
+
+def channel_flow(nit, u, v, dt, dx, dy, p, rho, nu, F, max_steps=10**7):
+    from .stencils_np import cfd_constants
+    if _sfx(u, v, p) != "f64":
+        raise TypeError("channel_flow oracle is float64 only")
+    ny, nx = u.shape
+    if v.shape != (ny, nx) or p.shape != (ny, nx):
+        raise ValueError("channel_flow arrays must share one (ny, nx) shape")
+    if ny < 1 or (int(nit) > 0 and ny < 2) or nx < 2:
+        raise IndexError("channel_flow: the boundary statements need ny >= 2 and nx >= 2")
+    k = cfd_constants(dt, dx, dy, rho)
+    kc = np.array([k[n] for n in _CFD_KEYS], dtype=np.float64)
+    steps = lib().oracle_channel_flow_f64(_p(u), _p(v), _p(p), ny, nx, int(nit), float(dt),
+                                          float(dx), float(dy), float(rho), float(nu),
+                                          float(F * dt), _p(kc), int(max_steps))
+    if steps < 0:
+        raise RuntimeError(f"channel_flow did not converge in {max_steps} steps")
+    return int(steps)

@@ -13,6 +13,8 @@
  *   jacobi_1d  polybench/jacobi_1d/jacobi_1d_numpy.py:4-8
  *   fdtd_2d    polybench/fdtd_2d/fdtd_2d_numpy.py:4-11
  *   vadv       weather_stencils/vadv/vadv_numpy.py:9-78
+ *   cavity_flow  cavity_flow/cavity_flow_numpy.py:13-82
+ *   channel_flow channel_flow/channel_flow_numpy.py:13-152
  *
  * so results are bit-identical to the reference.  Each half-sweep is a
  * parallel loop over the slow axis (OpenMP when built with -fopenmp); the
@@ -256,4 +258,208 @@ void oracle_vadv_f64(double* us, const double* u, const double* wcon, const doub
     }
     free(ccol);
   }
+}
+
+/* cavity_flow: cavity_flow/cavity_flow_numpy.py:13-82, float64, arrays (ny, nx).
+ * kc holds the scalars the reference forms in Python (its dx**2 is the C
+ * library's pow, not always dx*dx), in this order:
+ *   two_dx, two_dy, inv_dt, dx2, dy2, pD = 2*(dx2+dy2), pC = dx2*dy2/pD,
+ *   k1u = dt/(2*rho*dx), k1v = dt/(2*rho*dy), k2 = dt/dx2, k3 = dt/dy2.
+ * Per time step: b from u, v; nit pressure iterations with the reference's
+ * four boundary statements in order; u and v from copies un, vn; walls. */
+enum { KC_TWO_DX, KC_TWO_DY, KC_INV_DT, KC_DX2, KC_DY2, KC_PD, KC_PC, KC_K1U, KC_K1V, KC_K2,
+       KC_K3 };
+
+static double cfd_comp(const double* f, const double* un, const double* vn, double pdiff,
+                       int64_t i, int64_t j, int64_t nx, double dt, double dx, double dy,
+                       double nu, double k1, const double* kc) {
+  const int64_t o = i * nx + j;
+  const double fc = f[o];
+  const double a = ((un[o] * dt) / dx) * (fc - f[o - 1]);
+  const double b = ((vn[o] * dt) / dy) * (fc - f[o - nx]);
+  double out = fc - a;
+  out = out - b;
+  out = out - k1 * pdiff;
+  const double two_f = 2.0 * fc;
+  const double d1 = kc[KC_K2] * ((f[o + 1] - two_f) + f[o - 1]);
+  const double d2 = kc[KC_K3] * ((f[o + nx] - two_f) + f[o - nx]);
+  return out + nu * (d1 + d2);
+}
+
+void oracle_cavity_flow_f64(double* u, double* v, double* p, int64_t ny, int64_t nx, int32_t nt,
+                            int32_t nit, double dt, double dx, double dy, double rho, double nu,
+                            const double* kc) {
+  const size_t n = (size_t)(ny * nx);
+  double* un = (double*)malloc(sizeof(double) * n * 4 + 1);
+  double* vn = un + n;
+  double* pn = vn + n;
+  double* b = pn + n;
+  for (size_t q = 0; q < n; ++q) b[q] = 0.0;
+  for (int32_t t = 0; t < nt; ++t) {
+    for (size_t q = 0; q < n; ++q) { un[q] = u[q]; vn[q] = v[q]; }
+    /* build_up_b */
+    for (int64_t i = 1; i < ny - 1; ++i)
+      for (int64_t j = 1; j < nx - 1; ++j) {
+        const int64_t o = i * nx + j;
+        const double x1 = (u[o + 1] - u[o - 1]) / kc[KC_TWO_DX];
+        const double x2 = (v[o + nx] - v[o - nx]) / kc[KC_TWO_DY];
+        double r = kc[KC_INV_DT] * (x1 + x2);
+        r = r - x1 * x1;
+        double z = (u[o + nx] - u[o - nx]) / kc[KC_TWO_DY];
+        z = z * (v[o + 1] - v[o - 1]);
+        z = z / kc[KC_TWO_DX];
+        r = r - 2.0 * z;
+        r = r - x2 * x2;
+        b[o] = rho * r;
+      }
+    /* pressure_poisson */
+    for (int32_t q = 0; q < nit; ++q) {
+      for (size_t m = 0; m < n; ++m) pn[m] = p[m];
+      for (int64_t i = 1; i < ny - 1; ++i)
+        for (int64_t j = 1; j < nx - 1; ++j) {
+          const int64_t o = i * nx + j;
+          double s = (pn[o + 1] + pn[o - 1]) * kc[KC_DY2];
+          s = s + (pn[o + nx] + pn[o - nx]) * kc[KC_DX2];
+          s = s / kc[KC_PD];
+          p[o] = s - kc[KC_PC] * b[o];
+        }
+      if (nx >= 2)
+        for (int64_t i = 0; i < ny; ++i) p[i * nx + nx - 1] = p[i * nx + nx - 2];
+      if (ny >= 2)
+        for (int64_t j = 0; j < nx; ++j) p[j] = p[nx + j];
+      if (nx >= 2)
+        for (int64_t i = 0; i < ny; ++i) p[i * nx] = p[i * nx + 1];
+      for (int64_t j = 0; j < nx; ++j) p[(ny - 1) * nx + j] = 0.0;
+    }
+    /* velocities from un, vn and the new p */
+    for (int64_t i = 1; i < ny - 1; ++i)
+      for (int64_t j = 1; j < nx - 1; ++j) {
+        const int64_t o = i * nx + j;
+        u[o] = cfd_comp(un, un, vn, p[o + 1] - p[o - 1], i, j, nx, dt, dx, dy, nu, kc[KC_K1U], kc);
+        v[o] = cfd_comp(vn, un, vn, p[o + nx] - p[o - nx], i, j, nx, dt, dx, dy, nu, kc[KC_K1V], kc);
+      }
+    for (int64_t j = 0; j < nx; ++j) u[j] = 0.0;
+    for (int64_t i = 0; i < ny; ++i) u[i * nx] = 0.0;
+    for (int64_t i = 0; i < ny; ++i) u[i * nx + nx - 1] = 0.0;
+    for (int64_t j = 0; j < nx; ++j) u[(ny - 1) * nx + j] = 1.0;
+    for (int64_t j = 0; j < nx; ++j) v[j] = 0.0;
+    for (int64_t j = 0; j < nx; ++j) v[(ny - 1) * nx + j] = 0.0;
+    for (int64_t i = 0; i < ny; ++i) v[i * nx] = 0.0;
+    for (int64_t i = 0; i < ny; ++i) v[i * nx + nx - 1] = 0.0;
+  }
+  free(un);
+}
+
+/* NumPy's sum of a contiguous float64 array (np.sum / np.add.reduce): the
+ * output starts at +0.0 and receives the pairwise sum of all n elements.  The
+ * pairwise sum (NumPy's pairwise_sum for doubles) adds fewer than 8 elements in
+ * order from 0.0; up to 128 with 8 running partial sums r[0..7] over
+ * consecutive groups of 8, combined as ((r0+r1)+(r2+r3))+((r4+r5)+(r6+r7)),
+ * then the remainder in order; above 128 it splits at n2 = n/2 rounded down to
+ * a multiple of 8 and adds the two halves' sums. */
+double oracle_pairwise_sum_f64(const double* a, int64_t n) {
+  if (n < 8) {
+    double res = 0.0;
+    for (int64_t i = 0; i < n; ++i) res = res + a[i];
+    return res;
+  }
+  if (n <= 128) {
+    double r[8];
+    int64_t i;
+    for (int j = 0; j < 8; ++j) r[j] = a[j];
+    for (i = 8; i < n - (n % 8); i += 8)
+      for (int j = 0; j < 8; ++j) r[j] = r[j] + a[i + j];
+    double res = ((r[0] + r[1]) + (r[2] + r[3])) + ((r[4] + r[5]) + (r[6] + r[7]));
+    for (; i < n; ++i) res = res + a[i];
+    return res;
+  }
+  int64_t n2 = n / 2;
+  n2 -= n2 % 8;
+  return oracle_pairwise_sum_f64(a, n2) + oracle_pairwise_sum_f64(a + n2, n - n2);
+}
+
+double oracle_numpy_sum_f64(const double* a, int64_t n) {
+  return 0.0 + oracle_pairwise_sum_f64(a, n);
+}
+
+/* channel_flow: the cavity_flow arithmetic with periodic columns (the east
+ * neighbour of column nx-1 is column 0, the west neighbour of column 0 is
+ * column nx-1), u += F*dt (Fdt), pressure walls p[-1] = p[-2] then p[0] = p[1],
+ * velocity walls u = v = 0 on rows 0 and -1, looping while
+ * (sum(u) - sum(un)) / sum(u) > .001.  Returns the step count, or -1 if
+ * max_steps steps did not converge. */
+static inline int64_t wrapc(int64_t j, int64_t nx) { return j < 0 ? j + nx : (j >= nx ? j - nx : j); }
+
+int64_t oracle_channel_flow_f64(double* u, double* v, double* p, int64_t ny, int64_t nx,
+                                int32_t nit, double dt, double dx, double dy, double rho,
+                                double nu, double Fdt, const double* kc, int64_t max_steps) {
+  const size_t n = (size_t)(ny * nx);
+  double* un = (double*)malloc(sizeof(double) * n * 4 + 1);
+  double* vn = un + n;
+  double* pn = vn + n;
+  double* b = pn + n;
+  int64_t steps = 0;
+  double udiff = 1.0;
+  while (udiff > .001) {
+    if (steps >= max_steps) { steps = -1; break; }
+    for (size_t q = 0; q < n; ++q) { un[q] = u[q]; vn[q] = v[q]; b[q] = 0.0; }
+    for (int64_t i = 1; i < ny - 1; ++i)
+      for (int64_t j = 0; j < nx; ++j) {
+        const int64_t o = i * nx, je = wrapc(j + 1, nx), jw = wrapc(j - 1, nx);
+        const double x1 = (u[o + je] - u[o + jw]) / kc[KC_TWO_DX];
+        const double x2 = (v[o + nx + j] - v[o - nx + j]) / kc[KC_TWO_DY];
+        double r = kc[KC_INV_DT] * (x1 + x2);
+        r = r - x1 * x1;
+        double z = (u[o + nx + j] - u[o - nx + j]) / kc[KC_TWO_DY];
+        z = z * (v[o + je] - v[o + jw]);
+        z = z / kc[KC_TWO_DX];
+        r = r - 2.0 * z;
+        r = r - x2 * x2;
+        b[o + j] = rho * r;
+      }
+    for (int32_t q = 0; q < nit; ++q) {
+      for (size_t m = 0; m < n; ++m) pn[m] = p[m];
+      for (int64_t i = 1; i < ny - 1; ++i)
+        for (int64_t j = 0; j < nx; ++j) {
+          const int64_t o = i * nx;
+          double t = (pn[o + wrapc(j + 1, nx)] + pn[o + wrapc(j - 1, nx)]) * kc[KC_DY2];
+          t = t + (pn[o + nx + j] + pn[o - nx + j]) * kc[KC_DX2];
+          t = t / kc[KC_PD];
+          p[o + j] = t - kc[KC_PC] * b[o + j];
+        }
+      for (int64_t j = 0; j < nx; ++j) p[(ny - 1) * nx + j] = p[(ny - 2) * nx + j];
+      for (int64_t j = 0; j < nx; ++j) p[j] = p[nx + j];
+    }
+    for (int64_t i = 1; i < ny - 1; ++i)
+      for (int64_t j = 0; j < nx; ++j) {
+        const int64_t o = i * nx, je = wrapc(j + 1, nx), jw = wrapc(j - 1, nx);
+        const double uc = un[o + j], vc = vn[o + j];
+        const double cu = (uc * dt) / dx, cv = (vc * dt) / dy;
+        double ou = uc - cu * (uc - un[o + jw]);
+        ou = ou - cv * (uc - un[o - nx + j]);
+        ou = ou - kc[KC_K1U] * (p[o + je] - p[o + jw]);
+        double d1 = kc[KC_K2] * ((un[o + je] - 2.0 * uc) + un[o + jw]);
+        double d2 = kc[KC_K3] * ((un[o + nx + j] - 2.0 * uc) + un[o - nx + j]);
+        ou = ou + nu * (d1 + d2);
+        u[o + j] = ou + Fdt;
+        double ov = vc - cu * (vc - vn[o + jw]);
+        ov = ov - cv * (vc - vn[o - nx + j]);
+        ov = ov - kc[KC_K1V] * (p[o + nx + j] - p[o - nx + j]);
+        d1 = kc[KC_K2] * ((vn[o + je] - 2.0 * vc) + vn[o + jw]);
+        d2 = kc[KC_K3] * ((vn[o + nx + j] - 2.0 * vc) + vn[o - nx + j]);
+        v[o + j] = ov + nu * (d1 + d2);
+      }
+    for (int64_t j = 0; j < nx; ++j) {
+      u[j] = 0.0;
+      u[(ny - 1) * nx + j] = 0.0;
+      v[j] = 0.0;
+      v[(ny - 1) * nx + j] = 0.0;
+    }
+    const double su = oracle_numpy_sum_f64(u, (int64_t)n);
+    const double sun = oracle_numpy_sum_f64(un, (int64_t)n);
+    udiff = (su - sun) / su;
+    ++steps;
+  }
+  free(un);
+  return steps;
 }

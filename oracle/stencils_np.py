@@ -18,11 +18,14 @@ Evaluation orders restated here:
   ``tx = 0.125 * ((next_x - 2.0 * c) + prev_x)``.
 * hdiff, weather_stencils/hdiff/hdiff_numpy.py:5-29 -- see ``hdiff``.
 * vadv, weather_stencils/vadv/vadv_numpy.py:9-78 -- see ``vadv``.
+* cavity_flow, cavity_flow/cavity_flow_numpy.py:13-82 -- see ``cavity_flow``.
+* channel_flow, channel_flow/channel_flow_numpy.py:13-152 -- see ``channel_flow``.
 """
 import numpy as np
 
 __all__ = ["jacobi_2d_kernel", "heat_3d_kernel", "hdiff", "jacobi_2d_half_sweep",
-           "heat_3d_half_sweep", "jacobi_1d_kernel", "fdtd_2d_kernel", "vadv"]
+           "heat_3d_half_sweep", "jacobi_1d_kernel", "fdtd_2d_kernel", "vadv",
+           "cavity_flow", "cfd_constants", "channel_flow"]
 
 
 def jacobi_2d_half_sweep(src, dst):
@@ -238,3 +241,203 @@ def vadv(utens_stage, u_stage, wcon, u_pos, utens, dtr_stage):
     for k in range(K - 2, -1, -1):
         data = np.subtract(dcol[:, :, k], np.multiply(ccol[:, :, k], data))
         utens_stage[:, :, k] = np.multiply(dtr, np.subtract(data, u_pos[:, :, k]))
+
+
+def cfd_constants(dt, dx, dy, rho):
+    """The scalars cavity_flow_numpy.py forms with Python float arithmetic.
+
+    ``dx**2`` is Python's float power, i.e. the C library's ``pow(dx, 2.0)``,
+    which is not always the correctly rounded ``dx*dx``; every user of these
+    constants must take them from ``pow`` as well.
+    """
+    dx2, dy2 = dx ** 2, dy ** 2
+    return {
+        "two_dx": 2 * dx, "two_dy": 2 * dy, "inv_dt": 1 / dt,       # build_up_b, :15-21
+        "dx2": dx2, "dy2": dy2,                                     # pressure_poisson, :30-33
+        "pD": 2 * (dx2 + dy2), "pC": dx2 * dy2 / (2 * (dx2 + dy2)),
+        "k1u": dt / (2 * rho * dx), "k1v": dt / (2 * rho * dy),     # the u/v updates, :53-74
+        "k2": dt / dx2, "k3": dt / dy2,
+    }
+
+
+def cavity_flow(nx, ny, nt, nit, u, v, dt, dx, dy, p, rho, nu):
+    """``cavity_flow(nx, ny, nt, nit, u, v, dt, dx, dy, p, rho, nu)`` of
+    cavity_flow/cavity_flow_numpy.py:41-82 (float64; u, v, p updated in place).
+
+    Per time step, in the reference's order:
+
+    * ``build_up_b`` (:13-21) on the interior, with x1 = (u_e - u_w)/(2dx),
+      x2 = (v_s - v_n)/(2dy), z = (((u_s - u_n)/(2dy))*(v_e - v_w))/(2dx):
+      ``b = rho*((((1/dt)*(x1 + x2) - x1**2) - 2*z) - x2**2)``;
+    * ``pressure_poisson`` (:24-38), nit times: the interior
+      ``(((p_e + p_w)*dy**2 + (p_s + p_n)*dx**2) / (2*(dx**2 + dy**2))) - c*b``
+      from the previous iterate, then ``p[:, -1] = p[:, -2]``,
+      ``p[0, :] = p[1, :]``, ``p[:, 0] = p[:, 1]``, ``p[-1, :] = 0``;
+    * the u and v updates (:53-74) from copies un, vn and the new p, then the
+      walls (:75-82): u = 0 on three sides and 1 on the lid (row -1), v = 0.
+
+    Here ``_e/_w`` are columns j+1/j-1 and ``_s/_n`` rows i+1/i-1.
+    """
+    k = cfd_constants(dt, dx, dy, rho)
+    b = np.zeros((ny, nx))
+    for _ in range(nt):
+        un = u.copy()
+        vn = v.copy()
+        _cfd_build_up_b(b, rho, u, v, k)
+        _cfd_pressure_poisson(nit, p, b, k)
+        _cfd_velocity(u, v, un, vn, p, dt, dx, dy, nu, k)
+        u[0, :] = 0
+        u[:, 0] = 0
+        u[:, -1] = 0
+        u[-1, :] = 1
+        v[0, :] = 0
+        v[-1, :] = 0
+        v[:, 0] = 0
+        v[:, -1] = 0
+
+
+def _cfd_build_up_b(b, rho, u, v, k):
+    x1 = np.divide(np.subtract(u[1:-1, 2:], u[1:-1, 0:-2]), k["two_dx"])
+    x2 = np.divide(np.subtract(v[2:, 1:-1], v[0:-2, 1:-1]), k["two_dy"])
+    r = np.multiply(k["inv_dt"], np.add(x1, x2))
+    np.subtract(r, np.multiply(x1, x1), out=r)
+    z = np.divide(np.subtract(u[2:, 1:-1], u[0:-2, 1:-1]), k["two_dy"])
+    np.multiply(z, np.subtract(v[1:-1, 2:], v[1:-1, 0:-2]), out=z)
+    np.divide(z, k["two_dx"], out=z)
+    np.subtract(r, np.multiply(2, z), out=r)
+    np.subtract(r, np.multiply(x2, x2), out=r)
+    b[1:-1, 1:-1] = np.multiply(rho, r)
+
+
+def _cfd_pressure_poisson(nit, p, b, k):
+    cb = np.multiply(k["pC"], b[1:-1, 1:-1])
+    for _ in range(nit):
+        pn = p.copy()
+        t = np.multiply(np.add(pn[1:-1, 2:], pn[1:-1, 0:-2]), k["dy2"])
+        np.add(t, np.multiply(np.add(pn[2:, 1:-1], pn[0:-2, 1:-1]), k["dx2"]), out=t)
+        np.divide(t, k["pD"], out=t)
+        p[1:-1, 1:-1] = np.subtract(t, cb)
+        p[:, -1] = p[:, -2]
+        p[0, :] = p[1, :]
+        p[:, 0] = p[:, 1]
+        p[-1, :] = 0
+
+
+def _cfd_component(c, f, p_diff, dt, dx, dy, nu, k1, k):
+    """(((f - ((ua*dt)/dx)*(f - f_w)) - ((vn*dt)/dy)*(f - f_n)) - k1*p_diff)
+    + nu*(k2*((f_e - 2f) + f_w) + k3*((f_s - 2f) + f_n)) on the interior, where
+    ``c`` is the (un, vn) pair and ``f`` the advected field."""
+    un, vn = c
+    fc = f[1:-1, 1:-1]
+    a = np.multiply(np.divide(np.multiply(un[1:-1, 1:-1], dt), dx),
+                    np.subtract(fc, f[1:-1, 0:-2]))
+    bb = np.multiply(np.divide(np.multiply(vn[1:-1, 1:-1], dt), dy),
+                     np.subtract(fc, f[0:-2, 1:-1]))
+    out = np.subtract(fc, a)
+    np.subtract(out, bb, out=out)
+    np.subtract(out, np.multiply(k1, p_diff), out=out)
+    two_f = np.multiply(2, fc)
+    d1 = np.multiply(k["k2"], np.add(np.subtract(f[1:-1, 2:], two_f), f[1:-1, 0:-2]))
+    d2 = np.multiply(k["k3"], np.add(np.subtract(f[2:, 1:-1], two_f), f[0:-2, 1:-1]))
+    np.add(out, np.multiply(nu, np.add(d1, d2)), out=out)
+    return out
+
+
+def _cfd_velocity(u, v, un, vn, p, dt, dx, dy, nu, k):
+    u[1:-1, 1:-1] = _cfd_component((un, vn), un, np.subtract(p[1:-1, 2:], p[1:-1, 0:-2]),
+                                   dt, dx, dy, nu, k["k1u"], k)
+    v[1:-1, 1:-1] = _cfd_component((un, vn), vn, np.subtract(p[2:, 1:-1], p[0:-2, 1:-1]),
+                                   dt, dx, dy, nu, k["k1v"], k)
+
+
+def _wrap_cols(f):
+    """(east, west) neighbours of every column with periodic wrap in x."""
+    return np.roll(f, -1, axis=1), np.roll(f, 1, axis=1)
+
+
+def channel_flow(nit, u, v, dt, dx, dy, p, rho, nu, F):
+    """``channel_flow(nit, u, v, dt, dx, dy, p, rho, nu, F)`` of
+    channel_flow/channel_flow_numpy.py:69-152; returns the step count.
+
+    The cavity_flow arithmetic with a periodic x direction: build_up_b (:13-39),
+    the pressure iterations (:42-66) and the u/v updates (:80-143) evaluate the
+    same expressions at every column, the neighbours of columns 0 and -1
+    wrapping around; the pressure walls copy row -2 to row -1, then row 1 to
+    row 0; u gains ``+ F*dt`` and the walls zero rows 0 and -1 of u and v.
+    The loop runs while ``(sum(u) - sum(un)) / sum(u) > .001`` (``np.sum``,
+    NumPy's pairwise summation).
+    """
+    ny, nx = u.shape
+    # The reference indexes column -2 (channel_flow_numpy.py:24), row -2 of p
+    # (:65, when nit >= 1) and row 0 (:144): IndexError below these sizes.
+    if nx < 2 or ny < 1 or (nit > 0 and ny < 2):
+        raise IndexError(f"channel_flow: a ({ny}, {nx}) grid is too small for the boundaries")
+    k = cfd_constants(dt, dx, dy, rho)
+    Fdt = F * dt
+    udiff = 1
+    stepcount = 0
+    while udiff > .001:
+        un = u.copy()
+        vn = v.copy()
+        b = np.zeros_like(u)
+        _chan_build_up_b(b, rho, u, v, k)
+        _chan_pressure(nit, p, b, k)
+        _chan_velocity(u, v, un, vn, p, dt, dx, dy, nu, Fdt, k)
+        u[0, :] = 0
+        u[-1, :] = 0
+        v[0, :] = 0
+        v[-1, :] = 0
+        udiff = (np.sum(u) - np.sum(un)) / np.sum(u)
+        stepcount += 1
+    return stepcount
+
+
+def _chan_build_up_b(b, rho, u, v, k):
+    ue, uw = _wrap_cols(u)
+    ve, vw = _wrap_cols(v)
+    x1 = np.divide(np.subtract(ue[1:-1], uw[1:-1]), k["two_dx"])
+    x2 = np.divide(np.subtract(v[2:], v[0:-2]), k["two_dy"])
+    r = np.multiply(k["inv_dt"], np.add(x1, x2))
+    np.subtract(r, np.multiply(x1, x1), out=r)
+    z = np.divide(np.subtract(u[2:], u[0:-2]), k["two_dy"])
+    np.multiply(z, np.subtract(ve[1:-1], vw[1:-1]), out=z)
+    np.divide(z, k["two_dx"], out=z)
+    np.subtract(r, np.multiply(2, z), out=r)
+    np.subtract(r, np.multiply(x2, x2), out=r)
+    b[1:-1, :] = np.multiply(rho, r)
+
+
+def _chan_pressure(nit, p, b, k):
+    cb = np.multiply(k["pC"], b[1:-1])
+    for _ in range(nit):
+        pn = p.copy()
+        pe, pw = _wrap_cols(pn)
+        t = np.multiply(np.add(pe[1:-1], pw[1:-1]), k["dy2"])
+        np.add(t, np.multiply(np.add(pn[2:], pn[0:-2]), k["dx2"]), out=t)
+        np.divide(t, k["pD"], out=t)
+        p[1:-1, :] = np.subtract(t, cb)
+        p[-1, :] = p[-2, :]
+        p[0, :] = p[1, :]
+
+
+def _chan_component(un, vn, f, p_diff, dt, dx, dy, nu, k1, k):
+    fe, fw = _wrap_cols(f)
+    fc = f[1:-1]
+    a = np.multiply(np.divide(np.multiply(un[1:-1], dt), dx), np.subtract(fc, fw[1:-1]))
+    bb = np.multiply(np.divide(np.multiply(vn[1:-1], dt), dy), np.subtract(fc, f[0:-2]))
+    out = np.subtract(fc, a)
+    np.subtract(out, bb, out=out)
+    np.subtract(out, np.multiply(k1, p_diff), out=out)
+    two_f = np.multiply(2, fc)
+    d1 = np.multiply(k["k2"], np.add(np.subtract(fe[1:-1], two_f), fw[1:-1]))
+    d2 = np.multiply(k["k3"], np.add(np.subtract(f[2:], two_f), f[0:-2]))
+    np.add(out, np.multiply(nu, np.add(d1, d2)), out=out)
+    return out
+
+
+def _chan_velocity(u, v, un, vn, p, dt, dx, dy, nu, Fdt, k):
+    pe, pw = _wrap_cols(p)
+    nu_ = _chan_component(un, vn, un, np.subtract(pe[1:-1], pw[1:-1]), dt, dx, dy, nu, k["k1u"], k)
+    u[1:-1, :] = np.add(nu_, Fdt)
+    v[1:-1, :] = _chan_component(un, vn, vn, np.subtract(p[2:], p[0:-2]), dt, dx, dy, nu,
+                                 k["k1v"], k)

@@ -12,6 +12,8 @@ It imports the reference's own NumPy kernels
 * ``npbench.benchmarks.polybench.jacobi_1d.jacobi_1d_numpy.kernel``
 * ``npbench.benchmarks.polybench.fdtd_2d.fdtd_2d_numpy.kernel``
 * ``npbench.benchmarks.weather_stencils.vadv.vadv_numpy.vadv``
+* ``npbench.benchmarks.cavity_flow.cavity_flow_numpy.cavity_flow``
+* ``npbench.benchmarks.channel_flow.channel_flow_numpy.channel_flow``
 
 and their ``initialize`` functions, runs them on seeded inputs, and writes
 
@@ -63,6 +65,8 @@ def main():
     from npbench.benchmarks.polybench.jacobi_1d import jacobi_1d_numpy, jacobi_1d
     from npbench.benchmarks.polybench.fdtd_2d import fdtd_2d_numpy, fdtd_2d
     from npbench.benchmarks.weather_stencils.vadv import vadv_numpy, vadv
+    from npbench.benchmarks.cavity_flow import cavity_flow_numpy, cavity_flow
+    from npbench.benchmarks.channel_flow import channel_flow_numpy, channel_flow
 
     arrays, cases = {}, []
     rng = np.random.default_rng(20211)
@@ -257,6 +261,91 @@ def main():
             raised = type(e).__name__
         cases.append(dict(name=f"vadv/float64/K{K}", bench="vadv", dtype="float64",
                           shape=[2, 3, K], dtr_stage=0.15, raises=raised))
+
+    # cavity_flow (float64): reference initialize (zeros) and random fields.
+    crng = np.random.default_rng(20213)
+
+    def add_cfd_case(name, ny, nx, nt, nit, u, v, p, rho=1.0, nu=0.1, store=True, **meta):
+        _, _, _, dx, dy, dt = cavity_flow.initialize(ny, nx)
+        a, b, c = u.copy(), v.copy(), p.copy()
+        cavity_flow_numpy.cavity_flow(nx, ny, nt, nit, a, b, dt, dx, dy, c, rho, nu)
+        case = dict(name=name, bench="cavity_flow", dtype="float64", shape=[ny, nx], nt=nt,
+                    nit=nit, rho=rho, nu=nu, dx=dx, dy=dy, dt=dt, **meta)
+        if store:
+            for k, val in (("u_in", u), ("v_in", v), ("p_in", p), ("u_out", a), ("v_out", b),
+                           ("p_out", c)):
+                arrays[f"{name}/{k}"] = val
+        else:
+            case.update(sha_u=sha(a), sha_v=sha(b), sha_p=sha(c))
+        cases.append(case)
+
+    for (ny, nx, nt, nit) in [(2, 2, 2, 2), (2, 5, 3, 2), (5, 2, 3, 2), (3, 3, 2, 3), (5, 7, 3, 2),
+                              (12, 9, 4, 3), (31, 33, 6, 5), (40, 17, 3, 4), (9, 70, 2, 1),
+                              (6, 6, 0, 3), (6, 6, 2, 0)]:
+        u0, v0, p0, _, _, _ = cavity_flow.initialize(ny, nx)
+        add_cfd_case(f"cavity_flow/float64/{ny}x{nx}/nt{nt}/nit{nit}/init", ny, nx, nt, nit,
+                     u0, v0, p0)
+        u0, v0, p0 = (crng.random((ny, nx)) for _ in range(3))
+        add_cfd_case(f"cavity_flow/float64/{ny}x{nx}/nt{nt}/nit{nit}/rand", ny, nx, nt, nit,
+                     u0, v0, p0, rho=1.3, nu=0.07)
+    u0, v0, p0 = (special_values(crng, (8, 9), np.float64) for _ in range(3))
+    add_cfd_case("cavity_flow/float64/special", 8, 9, 3, 2, u0, v0, p0, special=True)
+    u0, v0, p0, _, _, _ = cavity_flow.initialize(61, 61)
+    add_cfd_case("cavity_flow/float64/presetS", 61, 61, 25, 5, u0, v0, p0, store=False,
+                 init="reference")
+    # ny or nx below 2: the reference's pressure boundary statements raise IndexError.
+    for (ny, nx) in [(1, 5), (5, 1)]:
+        u0, v0, p0 = (np.zeros((ny, nx)) for _ in range(3))
+        try:
+            cavity_flow_numpy.cavity_flow(nx, ny, 1, 1, u0, v0, 0.01, 0.5, 0.5, p0, 1.0, 0.1)
+            raised = None
+        except Exception as e:  # noqa: BLE001 - record what the reference raises
+            raised = type(e).__name__
+        cases.append(dict(name=f"cavity_flow/float64/{ny}x{nx}/raises", bench="cavity_flow",
+                          dtype="float64", shape=[ny, nx], nt=1, nit=1, raises=raised))
+
+    # channel_flow (float64): the step count is part of each case.
+    hrng = np.random.default_rng(20214)
+
+    def add_chan_case(name, ny, nx, nit, u, v, p, rho=1.0, nu=0.1, F=1.0, store=True, **meta):
+        _, _, _, dx, dy, dt = channel_flow.initialize(ny, nx)
+        a, b, c = u.copy(), v.copy(), p.copy()
+        steps = channel_flow_numpy.channel_flow(nit, a, b, dt, dx, dy, c, rho, nu, F)
+        case = dict(name=name, bench="channel_flow", dtype="float64", shape=[ny, nx], nit=nit,
+                    rho=rho, nu=nu, F=F, dx=dx, dy=dy, dt=dt, steps=int(steps), **meta)
+        if store:
+            for k, val in (("u_in", u), ("v_in", v), ("p_in", p), ("u_out", a), ("v_out", b),
+                           ("p_out", c)):
+                arrays[f"{name}/{k}"] = val
+        else:
+            case.update(sha_u=sha(a), sha_v=sha(b), sha_p=sha(c))
+        cases.append(case)
+
+    for (ny, nx, nit) in [(2, 2, 1), (2, 5, 2), (3, 2, 2), (5, 7, 2), (12, 9, 3), (31, 33, 5),
+                          (4, 40, 1), (9, 12, 0)]:
+        u0, v0, p0, _, _, _ = channel_flow.initialize(ny, nx)
+        add_chan_case(f"channel_flow/float64/{ny}x{nx}/nit{nit}/init", ny, nx, nit, u0, v0, p0)
+    # random pressure, other physical constants
+    u0, v0, _, _, _, _ = channel_flow.initialize(9, 12)
+    add_chan_case("channel_flow/float64/9x12/nit3/randp", 9, 12, 3, u0, v0, hrng.random((9, 12)),
+                  rho=1.2, nu=0.05, F=0.5)
+    # two rows, negative sum(u): the first udiff is +inf, so a second step runs
+    add_chan_case("channel_flow/float64/2x6/nit1/negu", 2, 6, 1, -hrng.random((2, 6)),
+                  hrng.random((2, 6)), hrng.random((2, 6)))
+    u0, v0, p0 = (special_values(hrng, (6, 8), np.float64) for _ in range(3))
+    add_chan_case("channel_flow/float64/special", 6, 8, 2, u0, v0, p0, special=True)
+    u0, v0, p0, _, _, _ = channel_flow.initialize(61, 61)
+    add_chan_case("channel_flow/float64/presetS", 61, 61, 5, u0, v0, p0, store=False,
+                  init="reference")
+    for (ny, nx, nit) in [(5, 1, 0), (1, 5, 1)]:
+        u0, v0, p0 = (np.zeros((ny, nx)) for _ in range(3))
+        try:
+            channel_flow_numpy.channel_flow(nit, u0, v0, 0.01, 0.5, 0.5, p0, 1.0, 0.1, 1.0)
+            raised = None
+        except Exception as e:  # noqa: BLE001 - record what the reference raises
+            raised = type(e).__name__
+        cases.append(dict(name=f"channel_flow/float64/{ny}x{nx}/raises", bench="channel_flow",
+                          dtype="float64", shape=[ny, nx], nit=nit, raises=raised))
 
     np.savez_compressed(os.path.join(HERE, "cases.npz"), **arrays)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:

@@ -99,6 +99,73 @@ def test_vadv_golden(golden, which):
     assert n >= 20
 
 
+def cfd_case_args(arrays, c, copy=True):
+    """(nx, ny, nt, nit, u, v, dt, dx, dy, p, rho, nu) for a stored cavity_flow case."""
+    name = c["name"]
+    u, v, p = (arrays[f"{name}/{k}_in"] for k in ("u", "v", "p"))
+    if copy:
+        u, v, p = u.copy(), v.copy(), p.copy()
+    ny, nx = c["shape"]
+    return (nx, ny, c["nt"], c["nit"], u, v, c["dt"], c["dx"], c["dy"], p, c["rho"], c["nu"])
+
+
+@pytest.mark.parametrize("which", sorted(ORACLES))
+def test_cavity_flow_golden(golden, which):
+    _, arrays = golden
+    n = 0
+    with np.errstate(all="ignore"):
+        for c in _cases(golden, "cavity_flow"):
+            name = c["name"]
+            if "raises" in c:
+                ny, nx = c["shape"]
+                z = [np.zeros((ny, nx)) for _ in range(3)]
+                with pytest.raises(IndexError):
+                    ORACLES[which].cavity_flow(nx, ny, 1, 1, z[0], z[1], 0.01, 0.5, 0.5, z[2],
+                                               1.0, 0.1)
+                continue
+            args = cfd_case_args(arrays, c)
+            ORACLES[which].cavity_flow(*args)
+            for k, got in (("u", args[4]), ("v", args[5]), ("p", args[9])):
+                exp = arrays[f"{name}/{k}_out"]
+                assert bits_equal(got, exp), (name, k, first_diff(got, exp))
+            n += 1
+    assert n >= 20
+
+
+@pytest.mark.parametrize("which", sorted(ORACLES))
+def test_channel_flow_golden(golden, which):
+    _, arrays = golden
+    n = 0
+    with np.errstate(all="ignore"):
+        for c in _cases(golden, "channel_flow"):
+            name = c["name"]
+            if "raises" in c:
+                ny, nx = c["shape"]
+                z = [np.zeros((ny, nx)) for _ in range(3)]
+                with pytest.raises(IndexError):
+                    ORACLES[which].channel_flow(c["nit"], z[0], z[1], 0.01, 0.5, 0.5, z[2], 1.0,
+                                                0.1, 1.0)
+                continue
+            u, v, p = (arrays[f"{name}/{k}_in"].copy() for k in ("u", "v", "p"))
+            steps = ORACLES[which].channel_flow(c["nit"], u, v, c["dt"], c["dx"], c["dy"], p,
+                                                c["rho"], c["nu"], c["F"])
+            assert steps == c["steps"], name
+            for k, got in (("u", u), ("v", v), ("p", p)):
+                exp = arrays[f"{name}/{k}_out"]
+                assert bits_equal(got, exp), (name, k, first_diff(got, exp))
+            n += 1
+    assert n >= 10
+
+
+def test_c_pairwise_sum_is_numpy_sum():
+    """The C restatement of np.sum (+0.0 plus NumPy's pairwise summation)."""
+    rng = np.random.default_rng(11)
+    for n in list(range(0, 260)) + [1000, 4097, 8193, 10201, 40401]:
+        a = rng.standard_normal(n) * np.exp(rng.standard_normal(n) * 6)
+        assert cref.numpy_sum(a) == np.sum(a), n
+    assert np.signbit(np.sum(np.full(9, -0.0))) == np.signbit(cref.numpy_sum(np.full(9, -0.0)))
+
+
 @pytest.mark.parametrize("which", sorted(ORACLES))
 def test_reference_initializer_presets(golden, which):
     """Preset S with the reference's own initializers, checked by SHA-256."""
@@ -113,6 +180,23 @@ def test_reference_initializer_presets(golden, which):
             o.fdtd_2d_kernel(c["tsteps"], ex, ey, hz, fict)
             assert (_sha(ex), _sha(ey), _sha(hz)) == (c["sha_ex_out"], c["sha_ey_out"],
                                                       c["sha_hz_out"]), c["name"]
+            seen += 1
+            continue
+        if c["bench"] == "channel_flow":
+            ny, nx = c["shape"]
+            u, v, p, dx, dy, dt = workloads.init_channel_flow(ny, nx)
+            assert (dx, dy, dt) == (c["dx"], c["dy"], c["dt"]), c["name"]
+            steps = o.channel_flow(c["nit"], u, v, dt, dx, dy, p, c["rho"], c["nu"], c["F"])
+            assert steps == c["steps"], c["name"]
+            assert (_sha(u), _sha(v), _sha(p)) == (c["sha_u"], c["sha_v"], c["sha_p"]), c["name"]
+            seen += 1
+            continue
+        if c["bench"] == "cavity_flow":
+            ny, nx = c["shape"]
+            u, v, p, dx, dy, dt = workloads.init_cavity_flow(ny, nx)
+            assert (dx, dy, dt) == (c["dx"], c["dy"], c["dt"]), c["name"]
+            o.cavity_flow(nx, ny, c["nt"], c["nit"], u, v, dt, dx, dy, p, c["rho"], c["nu"])
+            assert (_sha(u), _sha(v), _sha(p)) == (c["sha_u"], c["sha_v"], c["sha_p"]), c["name"]
             seen += 1
             continue
         if c["bench"] == "vadv":
@@ -143,7 +227,7 @@ def test_reference_initializer_presets(golden, which):
         kern(c["tsteps"], A, B)
         assert _sha(A) == c["sha_A_out"] and _sha(B) == c["sha_B_out"], c["name"]
         seen += 1
-    assert seen == 10
+    assert seen == 12
 
 
 def test_oracles_agree_on_random_nonsquare():

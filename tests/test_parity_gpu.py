@@ -161,6 +161,117 @@ def test_vadv_ragged_shapes(IJK):
     assert bits_equal(_host(d), us), IJK
 
 
+def _cfd_args(arrays, c):
+    name = c["name"]
+    u, v, p = (_dev(arrays[f"{name}/{k}_in"]) for k in ("u", "v", "p"))
+    ny, nx = c["shape"]
+    return (nx, ny, c["nt"], c["nit"], u, v, c["dt"], c["dx"], c["dy"], p, c["rho"], c["nu"])
+
+
+def test_golden_cavity_flow_bit_exact(golden):
+    manifest, arrays = golden
+    n = 0
+    for c in manifest["cases"]:
+        if c["bench"] != "cavity_flow" or "init" in c:
+            continue
+        name = c["name"]
+        if "raises" in c:
+            ny, nx = c["shape"]
+            z = [torch.zeros((ny, nx), dtype=torch.float64, device=DEV) for _ in range(3)]
+            with pytest.raises(IndexError):
+                stencils.cavity_flow(nx, ny, 1, 1, z[0], z[1], 0.01, 0.5, 0.5, z[2], 1.0, 0.1)
+            continue
+        args = _cfd_args(arrays, c)
+        stencils.cavity_flow(*args)
+        for k, t in (("u", args[4]), ("v", args[5]), ("p", args[9])):
+            got, exp = _host(t), arrays[f"{name}/{k}_out"]
+            assert bits_equal(got, exp), (name, k, first_diff(got, exp))
+        n += 1
+    assert n >= 20
+
+
+@pytest.mark.parametrize("shape,nt,nit", [((101, 101), 700, 50), ((400, 37), 5, 7),
+                                          ((3, 300), 4, 3), ((161, 5), 6, 9)])
+def test_cavity_flow_vs_oracle(shape, nt, nit):
+    """The paper preset (one persistent launch for 700 steps of 50 pressure
+    iterations) and band splits with several rows per band, from random fields."""
+    ny, nx = shape
+    rng = np.random.default_rng(ny * 1000 + nx)
+    u, v, p = (rng.random(shape) for _ in range(3))
+    dx, dy, dt = 2 / (nx - 1), 2 / (ny - 1), .1 / ((nx - 1) * (ny - 1))
+    dev = [_dev(x) for x in (u, v, p)]
+    stencils.cavity_flow(nx, ny, nt, nit, dev[0], dev[1], dt, dx, dy, dev[2], 1.0, 0.1)
+    cref.cavity_flow(nx, ny, nt, nit, u, v, dt, dx, dy, p, 1.0, 0.1)
+    for d, h, k in zip(dev, (u, v, p), "uvp"):
+        got = _host(d)
+        assert bits_equal(got, h), (shape, k, first_diff(got, h))
+
+
+def test_cavity_flow_library_allocated_workspace(golden):
+    """workspace = NULL: the call allocates and frees its workspace stream-ordered."""
+    from npbench_gb300 import _lib
+    manifest, arrays = golden
+    c = next(c for c in manifest["cases"] if c["name"] == "cavity_flow/float64/31x33/nt6/nit5/rand")
+    nx, ny, nt, nit, u, v, dt, dx, dy, p, rho, nu = _cfd_args(arrays, c)
+    lib = _lib.load()
+    st = lib.npbgb_cavity_flow(u.data_ptr(), v.data_ptr(), p.data_ptr(), ny, nx, nt, nit, dt, dx,
+                               dy, rho, nu, _lib.NPBGB_F64, None, 0,
+                               torch.cuda.current_stream(DEV).cuda_stream)
+    _lib.check(st, "cavity_flow")
+    assert lib.npbgb_device_status(None) == _lib.NPBGB_OK
+    for k, t in (("u", u), ("v", v), ("p", p)):
+        assert bits_equal(_host(t), arrays[f"{c['name']}/{k}_out"]), k
+
+
+def test_golden_channel_flow_bit_exact(golden):
+    manifest, arrays = golden
+    n = 0
+    for c in manifest["cases"]:
+        if c["bench"] != "channel_flow" or "init" in c:
+            continue
+        name = c["name"]
+        if "raises" in c:
+            ny, nx = c["shape"]
+            z = [torch.zeros((ny, nx), dtype=torch.float64, device=DEV) for _ in range(3)]
+            with pytest.raises(IndexError):
+                stencils.channel_flow(c["nit"], z[0], z[1], 0.01, 0.5, 0.5, z[2], 1.0, 0.1, 1.0)
+            continue
+        u, v, p = (_dev(arrays[f"{name}/{k}_in"]) for k in ("u", "v", "p"))
+        steps = stencils.channel_flow(c["nit"], u, v, c["dt"], c["dx"], c["dy"], p, c["rho"],
+                                      c["nu"], c["F"])
+        assert steps == c["steps"], (name, steps)
+        for k, t in (("u", u), ("v", v), ("p", p)):
+            got, exp = _host(t), arrays[f"{name}/{k}_out"]
+            assert bits_equal(got, exp), (name, k, first_diff(got, exp))
+        n += 1
+    assert n >= 10
+
+
+@pytest.mark.parametrize("shape,nit", [((101, 101), 50), ((400, 37), 3), ((161, 2), 4)])
+def test_channel_flow_vs_oracle(shape, nit):
+    """The paper preset (989 steps of 50 pressure iterations in one launch) and
+    band splits with several rows per band, from the reference's initial state."""
+    ny, nx = shape
+    u, v, p, dx, dy, dt = workloads.init_channel_flow(ny, nx)
+    dev = [_dev(x) for x in (u, v, p)]
+    s_gpu = stencils.channel_flow(nit, dev[0], dev[1], dt, dx, dy, dev[2], 1.0, 0.1, 1.0)
+    s_ref = cref.channel_flow(nit, u, v, dt, dx, dy, p, 1.0, 0.1, 1.0)
+    assert s_gpu == s_ref
+    for d, h, k in zip(dev, (u, v, p), "uvp"):
+        got = _host(d)
+        assert bits_equal(got, h), (shape, k, first_diff(got, h))
+
+
+def test_channel_flow_step_cap():
+    """max_steps bounds the loop: RuntimeError, with the state after that many steps."""
+    u, v, p, dx, dy, dt = workloads.init_channel_flow(12, 9)
+    dev = [_dev(x) for x in (u, v, p)]
+    with pytest.raises(RuntimeError):
+        stencils.channel_flow(3, dev[0], dev[1], dt, dx, dy, dev[2], 1.0, 0.1, 1.0, max_steps=17)
+    from npbench_gb300 import _lib
+    assert _lib.load().npbgb_device_status(None) == _lib.NPBGB_OK
+
+
 def test_reference_initializer_presets(golden):
     seen = 0
     for c in golden[0]["cases"]:
@@ -178,6 +289,21 @@ def test_reference_initializer_presets(golden):
             o = _dev(out)
             stencils.hdiff(_dev(inf), o, _dev(coeff))
             assert _sha(_host(o)) == c["sha_out"], c["name"]
+        elif c["bench"] == "channel_flow":
+            ny, nx = c["shape"]
+            u, v, p, dx, dy, dt = workloads.init_channel_flow(ny, nx)
+            dev = [_dev(x) for x in (u, v, p)]
+            steps = stencils.channel_flow(c["nit"], dev[0], dev[1], dt, dx, dy, dev[2], c["rho"],
+                                          c["nu"], c["F"])
+            assert steps == c["steps"], c["name"]
+            assert [_sha(_host(x)) for x in dev] == [c["sha_u"], c["sha_v"], c["sha_p"]], c["name"]
+        elif c["bench"] == "cavity_flow":
+            ny, nx = c["shape"]
+            u, v, p, dx, dy, dt = workloads.init_cavity_flow(ny, nx)
+            dev = [_dev(x) for x in (u, v, p)]
+            stencils.cavity_flow(nx, ny, c["nt"], c["nit"], dev[0], dev[1], dt, dx, dy, dev[2],
+                                 c["rho"], c["nu"])
+            assert [_sha(_host(x)) for x in dev] == [c["sha_u"], c["sha_v"], c["sha_p"]], c["name"]
         elif c["bench"] == "vadv":
             dtr, us, u, w, up, ut = workloads.init_vadv(c["I"], c["J"], c["K"])
             d = _dev(us)
@@ -190,7 +316,7 @@ def test_reference_initializer_presets(golden):
             assert _sha(_host(dA)) == c["sha_A_out"], c["name"]
             assert _sha(_host(dB)) == c["sha_B_out"], c["name"]
         seen += 1
-    assert seen == 10
+    assert seen == 12
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])

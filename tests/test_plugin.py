@@ -53,7 +53,11 @@ for name, fn, mod in [("jacobi_2d", "kernel", "npbench.benchmarks.polybench.jaco
                       ("hdiff", "hdiff", "npbench.benchmarks.weather_stencils.hdiff.hdiff_gb300"),
                       ("jacobi_1d", "kernel", "npbench.benchmarks.polybench.jacobi_1d.jacobi_1d_gb300"),
                       ("fdtd_2d", "kernel", "npbench.benchmarks.polybench.fdtd_2d.fdtd_2d_gb300"),
-                      ("vadv", "vadv", "npbench.benchmarks.weather_stencils.vadv.vadv_gb300")]:
+                      ("vadv", "vadv", "npbench.benchmarks.weather_stencils.vadv.vadv_gb300"),
+                      ("cavity_flow", "cavity_flow",
+                       "npbench.benchmarks.cavity_flow.cavity_flow_gb300"),
+                      ("channel_flow", "channel_flow",
+                       "npbench.benchmarks.channel_flow.channel_flow_gb300")]:
     b = Benchmark(name)
     impl, label = f.implementations(b)[0]
     assert impl.__module__ == mod and impl.__name__ == fn and label == "default", impl
@@ -80,7 +84,7 @@ def test_install_is_idempotent(tmp_path):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("bench", ["jacobi_2d", "heat_3d", "hdiff", "jacobi_1d", "fdtd_2d",
-                                   "vadv"])
+                                   "vadv", "cavity_flow", "channel_flow"])
 def test_harness_runs_and_validates_plugin(tmp_path, bench):
     if not os.path.isdir(os.path.join(BUILT_TREE, "npbench", "infrastructure")):
         pytest.skip("baseline/_ref/npbench was not built")
