@@ -6,7 +6,9 @@
   synchronisation (framework.py:140-162, cupy_framework.py:32-58).
 * GPU: the harness's ``Test.run`` executes each stencil benchmark at preset S
   through the plugin, validates it against the harness's own NumPy run
-  (test.py:103-126) and reports SUCCESS.  It uses the NPBench tree that
+  (test.py:103-126), reports SUCCESS and writes its timings into the
+  harness's ``npbench.db`` (test.py:133-163); ``run_benchmark.py`` does the
+  same end to end, line counts included (run_benchmark.py:1-59).  It uses the NPBench tree that
   ``__graft_entry__.build()`` installs into baseline/_ref/npbench, and is
   skipped where that tree was never built.
 """
@@ -107,3 +109,42 @@ print("HARNESS-DONE")
     assert r.returncode == 0 and "HARNESS-DONE" in r.stdout, out
     assert "validation: SUCCESS" in r.stdout, out
     assert "did not validate" not in out, out
+    rows = _results(tree)
+    assert len(rows) == 2 and all(v == 1 and t > 0 for _, _, v, t in rows), rows
+    assert {fw for _, fw, _, _ in rows} == {"gb300"}, rows
+
+
+def _results(tree):
+    import sqlite3
+    with sqlite3.connect(os.path.join(tree, "npbench.db")) as con:
+        return con.execute("SELECT benchmark, framework, validated, time FROM results").fetchall()
+
+
+@pytest.mark.gpu
+def test_run_benchmark_writes_results_db(tmp_path):
+    """NPBench's own command line with -f gb300: validated timings land in npbench.db."""
+    if not os.path.isdir(os.path.join(BUILT_TREE, "npbench", "infrastructure")):
+        pytest.skip("baseline/_ref/npbench was not built")
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import shutil
+    import sqlite3
+    tree = str(tmp_path / "npbench")
+    shutil.copytree(BUILT_TREE, tree)
+    env = dict(os.environ)
+    env["PYTHONPATH"] = os.pathsep.join([tree, ROOT, STUBS, env.get("PYTHONPATH", "")])
+    env["PYTHONDONTWRITEBYTECODE"] = "1"
+    r = subprocess.run([sys.executable, "run_benchmark.py", "-b", "heat_3d", "-f", "gb300", "-p",
+                        "S", "-r", "3"], cwd=tree, env=env, capture_output=True, text=True,
+                       timeout=600)
+    out = r.stdout + r.stderr
+    assert r.returncode == 0, out
+    assert "validation: SUCCESS" in r.stdout, out
+    rows = _results(tree)
+    assert len(rows) == 3, rows
+    assert all(b == "heat3d" or b == "heat_3d" for b, _, _, _ in rows), rows
+    assert all(fw == "gb300" and v == 1 and t > 0 for _, fw, v, t in rows), rows
+    with sqlite3.connect(os.path.join(tree, "npbench.db")) as con:
+        lc = con.execute("SELECT framework, count FROM lcounts").fetchall()
+    assert any(fw == "gb300" and n > 0 for fw, n in lc), lc
