@@ -65,6 +65,9 @@ extern "C" {
                                        fixed-point warps; -1 (default) = 1 */
 #define NPBGB_CFG_BATCH_CTAS_PER_SM 9 /* persistent batch kernel: 2 or 3 (default)
                                          CTAs per SM (read when a batch is planned) */
+#define NPBGB_CFG_PDL 10              /* 1 (default): the per-half-sweep launches of the
+                                         time loops use programmatic dependent launch;
+                                         0: plain stream order */
 
 /* Grid kinds for batches. */
 #define NPBGB_KIND_JACOBI2D 0

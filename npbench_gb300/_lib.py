@@ -28,6 +28,7 @@ NPBGB_CFG_HEAT_HW_ROWS = 6
 NPBGB_CFG_F64_CVT = 7
 NPBGB_CFG_JACOBI_HW_WARPS = 8
 NPBGB_CFG_BATCH_CTAS_PER_SM = 9
+NPBGB_CFG_PDL = 10
 
 NPBGB_KIND_JACOBI2D = 0
 NPBGB_KIND_HEAT3D = 1

@@ -34,6 +34,7 @@ template <typename T>
 __global__ void __launch_bounds__(kBX * kBY)
 fdtd_e(T* __restrict__ ex, T* __restrict__ ey, const T* __restrict__ hz, const T* __restrict__ fict,
        int64_t nx, int64_t ny, int t) {
+  pdl_begin();
   const int64_t j = int64_t(blockIdx.x) * kBX + threadIdx.x;
   if (j >= ny) return;
   for (int64_t i = int64_t(blockIdx.y) * kBY + threadIdx.y; i < nx; i += int64_t(gridDim.y) * kBY) {
@@ -50,6 +51,7 @@ fdtd_e(T* __restrict__ ex, T* __restrict__ ey, const T* __restrict__ hz, const T
 template <typename T>
 __global__ void __launch_bounds__(kBX * kBY)
 fdtd_h(const T* __restrict__ ex, const T* __restrict__ ey, T* __restrict__ hz, int64_t nx, int64_t ny) {
+  pdl_begin();
   const T c07 = T(0.7);
   const int64_t j = int64_t(blockIdx.x) * kBX + threadIdx.x;
   if (j >= ny - 1) return;
@@ -70,12 +72,13 @@ int32_t run(T* ex, T* ey, T* hz, const T* fict, int64_t nx, int64_t ny, int32_t 
   if (gx > 0x7fffffff) return set_error(NPBGB_ERR_ARG, "fdtd2d: extent too large");
   const dim3 grid{unsigned(gx), unsigned(gy0 > 65535 ? 65535 : gy0)};
   const dim3 block{unsigned(kBX), unsigned(kBY)};
-  for (int32_t t = 0; t < tmax; ++t) {
-    fdtd_e<T><<<grid, block, 0, st>>>(ex, ey, hz, fict, nx, ny, t);
-    if (nx > 1 && ny > 1) fdtd_h<T><<<grid, block, 0, st>>>(ex, ey, hz, nx, ny);
+  cudaError_t e = cudaSuccess;
+  for (int32_t t = 0; t < tmax && e == cudaSuccess; ++t) {
+    e = launch_chained(fdtd_e<T>, grid, block, 0, st, ex, ey, hz, fict, nx, ny, t);
+    if (e == cudaSuccess && nx > 1 && ny > 1)
+      e = launch_chained(fdtd_h<T>, grid, block, 0, st, ex, ey, hz, nx, ny);
   }
-  NPBGB_CHECK_LAUNCH("fdtd2d");
-  return NPBGB_OK;
+  return cuda_status(e, "fdtd2d");
 }
 
 }  // namespace

@@ -97,6 +97,7 @@ __global__ void __launch_bounds__(kThreads)
 heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ src,
            T* __restrict__ dst, int64_t n0, int64_t n1, int64_t n2, int chunk, int hw_rows,
            uint32_t one) {
+  pdl_begin();
   using G = TmaGeom<T, R>;
   using S = typename std::conditional<FX, int64_t, T>::type;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -209,6 +210,7 @@ template <typename T, bool FX>
 __global__ void __launch_bounds__(kThreads)
 heat3d_ldg(const T* __restrict__ src, T* __restrict__ dst, int64_t n0, int64_t n1, int64_t n2,
            int chunk) {
+  pdl_begin();
   __shared__ hcore::PlaneBuf<T, FX> plane;
   const int64_t k0 = 1 + int64_t(blockIdx.x) * kTK, j0 = 1 + int64_t(blockIdx.y) * kTJ;
   const int64_t ib = 1 + int64_t(blockIdx.z) * chunk;
@@ -254,12 +256,16 @@ int32_t launch_tma(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tstep
   const dim3 grid{unsigned(gx), unsigned(gy), unsigned(gz)};
   int hw = g_cfg_heat_hw_rows >= 0 ? int(g_cfg_heat_hw_rows) : (FX ? 2 : 0);
   if (hw > G::TJ) hw = G::TJ;
-  for (int32_t t = 1; t < tsteps; ++t) {
-    heat3d_tma<T, FX, R, CVT><<<grid, kThreads, smem, st>>>(map_a, a, b, n0, n1, n2, chunk, hw, 1u);
-    heat3d_tma<T, FX, R, CVT><<<grid, kThreads, smem, st>>>(map_b, b, a, n0, n1, n2, chunk, hw, 1u);
+  const dim3 block{unsigned(kThreads)};
+  cudaError_t e = cudaSuccess;
+  for (int32_t t = 1; t < tsteps && e == cudaSuccess; ++t) {
+    e = launch_chained(heat3d_tma<T, FX, R, CVT>, grid, block, smem, st, map_a, a, b, n0, n1, n2,
+                       chunk, hw, 1u);
+    if (e == cudaSuccess)
+      e = launch_chained(heat3d_tma<T, FX, R, CVT>, grid, block, smem, st, map_b, b, a, n0, n1,
+                         n2, chunk, hw, 1u);
   }
-  NPBGB_CHECK_LAUNCH("heat3d_tma");
-  return NPBGB_OK;
+  return cuda_status(e, "heat3d_tma");
 }
 
 template <typename T, bool FX>
@@ -272,12 +278,14 @@ int32_t launch_ldg(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tstep
   if (gy > 65535 || gz > 65535 || gx > 0x7fffffff)
     return set_error(NPBGB_ERR_ARG, "heat3d: extent too large");
   const dim3 grid{unsigned(gx), unsigned(gy), unsigned(gz)};
-  for (int32_t t = 1; t < tsteps; ++t) {
-    heat3d_ldg<T, FX><<<grid, kThreads, 0, st>>>(a, b, n0, n1, n2, chunk);
-    heat3d_ldg<T, FX><<<grid, kThreads, 0, st>>>(b, a, n0, n1, n2, chunk);
+  const dim3 block{unsigned(kThreads)};
+  cudaError_t e = cudaSuccess;
+  for (int32_t t = 1; t < tsteps && e == cudaSuccess; ++t) {
+    e = launch_chained(heat3d_ldg<T, FX>, grid, block, 0, st, a, b, n0, n1, n2, chunk);
+    if (e == cudaSuccess)
+      e = launch_chained(heat3d_ldg<T, FX>, grid, block, 0, st, b, a, n0, n1, n2, chunk);
   }
-  NPBGB_CHECK_LAUNCH("heat3d_ldg");
-  return NPBGB_OK;
+  return cuda_status(e, "heat3d_ldg");
 }
 
 template <typename T, bool FX>

@@ -28,6 +28,7 @@ constexpr int kSteps = 32;            // half-sweeps per launch (even)
 template <typename T, int kW>
 __global__ void __launch_bounds__(kThreads)
 jacobi1d_block(T* __restrict__ a, T* __restrict__ b, int64_t n, int steps) {
+  pdl_begin();
   constexpr int kSpan = kW + 2 * kSteps;  // staged points per CTA
   __shared__ T buf[2][kSpan];
   const T k = T(0.33333);
@@ -67,13 +68,14 @@ int32_t run_w(T* a, T* b, int64_t n, int32_t tsteps, cudaStream_t st) {
   const int64_t blocks = cdiv(n - 2, kW);
   if (blocks > 0x7fffffff) return set_error(NPBGB_ERR_ARG, "jacobi1d: extent too large");
   int64_t left = 2 * int64_t(tsteps - 1);  // half-sweeps, even
-  while (left > 0) {
+  cudaError_t e = cudaSuccess;
+  while (left > 0 && e == cudaSuccess) {
     const int s = int(left < kSteps ? left : kSteps);
-    jacobi1d_block<T, kW><<<unsigned(blocks), kThreads, 0, st>>>(a, b, n, s);
+    e = launch_chained(jacobi1d_block<T, kW>, dim3{unsigned(blocks)}, dim3{unsigned(kThreads)}, 0,
+                       st, a, b, n, s);
     left -= s;
   }
-  NPBGB_CHECK_LAUNCH("jacobi1d_block");
-  return NPBGB_OK;
+  return cuda_status(e, "jacobi1d_block");
 }
 
 template <typename T>

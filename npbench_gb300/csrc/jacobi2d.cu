@@ -34,6 +34,7 @@ template <typename T, bool FX>
 __global__ void __launch_bounds__(32 * kWarps)
 jacobi2d_strip(const T* __restrict__ src, T* __restrict__ dst, int64_t ny, int64_t nx, int chunk,
                int hw_warps, uint32_t one) {
+  pdl_begin();
   const int warp = threadIdx.x >> 5;
   const int64_t k0 = 1 + (int64_t(blockIdx.x) * kWarps + warp) * 32;
   if (k0 >= nx - 1) return;  // whole strip outside the interior (warp-uniform)
@@ -67,12 +68,14 @@ int32_t run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st)
   if (gx > 0x7fffffff || gy > 65535) return set_error(NPBGB_ERR_ARG, "jacobi2d: extent too large");
   const dim3 grid{unsigned(gx), unsigned(gy)};
   const int hw = int(g_cfg_jacobi_hw_warps >= 0 ? g_cfg_jacobi_hw_warps : 1);
-  for (int32_t t = 1; t < tsteps; ++t) {
-    jacobi2d_strip<T, FX><<<grid, 32 * kWarps, 0, st>>>(a, b, ny, nx, chunk, hw, 1u);
-    jacobi2d_strip<T, FX><<<grid, 32 * kWarps, 0, st>>>(b, a, ny, nx, chunk, hw, 1u);
+  const dim3 block{32u * kWarps};
+  cudaError_t e = cudaSuccess;
+  for (int32_t t = 1; t < tsteps && e == cudaSuccess; ++t) {
+    e = launch_chained(jacobi2d_strip<T, FX>, grid, block, 0, st, a, b, ny, nx, chunk, hw, 1u);
+    if (e == cudaSuccess)
+      e = launch_chained(jacobi2d_strip<T, FX>, grid, block, 0, st, b, a, ny, nx, chunk, hw, 1u);
   }
-  NPBGB_CHECK_LAUNCH("jacobi2d_strip");
-  return NPBGB_OK;
+  return cuda_status(e, "jacobi2d_strip");
 }
 
 }  // namespace

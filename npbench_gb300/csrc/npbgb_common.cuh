@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <utility>
 
 #include "../../include/npbgb.h"
 
@@ -47,5 +48,37 @@ __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+
+// Programmatic dependent launch (griddepcontrol, sm_90 and later).  Time loops
+// issue one short kernel per half-sweep; launched with
+// launch_chained(), the next kernel's CTAs are scheduled while the current
+// grid drains instead of after it has finished.  Every chained kernel calls
+// pdl_begin() first, before touching global memory: it lets its own dependent
+// launch early, then waits until the preceding kernel has completed and its
+// memory is visible (griddepcontrol.wait), so read-after-write and
+// write-after-read between consecutive half-sweeps stay ordered.  Without a
+// programmatic predecessor both instructions are no-ops.
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+extern int64_t g_cfg_pdl;  // NPBGB_CFG_PDL
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_chained(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                           cudaStream_t st, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = g_cfg_pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 }  // namespace npbgb

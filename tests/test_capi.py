@@ -76,6 +76,7 @@ def test_argument_errors_are_status_codes_not_crashes():
     assert b"workspace" in lib.npbgb_last_error()
     assert lib.npbgb_vadv_workspace_bytes(256, 256, 160) == 8 * 159 * 256 * 256
     assert lib.npbgb_vadv_workspace_bytes(4, 4, 1) == 0
+    assert lib.npbgb_set_config(_lib.NPBGB_CFG_PDL, 2) == _lib.NPBGB_ERR_ARG
 
 
 def test_noop_sizes_return_ok_without_touching_memory():

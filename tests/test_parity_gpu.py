@@ -272,6 +272,38 @@ def test_channel_flow_step_cap():
     assert _lib.load().npbgb_device_status(None) == _lib.NPBGB_OK
 
 
+@pytest.mark.parametrize("pdl", [0, 1])
+def test_chained_launch_modes_bit_exact(pdl):
+    """Programmatic dependent launch on or off: the same bits from every time loop."""
+    from npbench_gb300 import _lib
+    old = _lib.set_config(_lib.NPBGB_CFG_PDL, pdl)
+    try:
+        for dt in (np.float64, np.float32):
+            A, B = workloads.uniform_pair((333, 517), dt, seed=21)
+            dA, dB = _dev(A), _dev(B)
+            stencils.jacobi_2d_kernel(23, dA, dB)
+            cref.jacobi_2d_kernel(23, A, B)
+            assert bits_equal(_host(dA), A) and bits_equal(_host(dB), B)
+            H, G = workloads.uniform_heat((45, 66, 130), dt, seed=22)
+            dH, dG = _dev(H), _dev(G)
+            stencils.heat_3d_kernel(9, dH, dG)
+            cref.heat_3d_kernel(9, H, G)
+            assert bits_equal(_host(dH), H) and bits_equal(_host(dG), G)
+            A, B = workloads.uniform_pair((20000,), dt, seed=23)
+            dA, dB = _dev(A), _dev(B)
+            stencils.jacobi_1d_kernel(70, dA, dB)
+            cref.jacobi_1d_kernel(70, A, B)
+            assert bits_equal(_host(dA), A) and bits_equal(_host(dB), B)
+            ex, ey, hz, fict = workloads.init_fdtd_2d(40, 130, 170, dt)
+            dev = [_dev(x) for x in (ex, ey, hz, fict)]
+            stencils.fdtd_2d_kernel(40, *dev)
+            cref.fdtd_2d_kernel(40, ex, ey, hz, fict)
+            for d, h in zip(dev[:3], (ex, ey, hz)):
+                assert bits_equal(_host(d), h)
+    finally:
+        _lib.set_config(_lib.NPBGB_CFG_PDL, old)
+
+
 def test_reference_initializer_presets(golden):
     seen = 0
     for c in golden[0]["cases"]:
