@@ -736,8 +736,10 @@ def run_batch(args):
         args, ups * args.steps / (ms * 1e-3), ms_step, "f32+f64",
         f"batched jacobi_2d: {args.batch_grids} grids, sides log-uniform [64, 2048], half "
         f"float32 / half float64, TSTEPS uniform [10, 500]",
-        {"cells": cells, "updates_per_step": ups, "bands": info["bands"], "ctas": info["ctas"],
-         "band_rows": 64, "graph": True, "l2": f"{cells * 6 * 2 / 1e9:.1f} GB resident, "
+        {"cells": cells, "updates_per_step": ups, "form": info["mode"],
+         "tiles" if info["mode"] == "stepped" else "bands": info["bands"],
+         "launches" if info["mode"] == "stepped" else "ctas": info["ctas"],
+         "rows_per_tile" if info["mode"] == "stepped" else "band_rows": 64, "graph": True, "l2": f"{cells * 6 * 2 / 1e9:.1f} GB resident, "
                                                 "far above L2"},
         roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                   "frac": ach / peak, "peak_kind": kind, "traffic": None},

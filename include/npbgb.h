@@ -68,6 +68,13 @@ extern "C" {
 #define NPBGB_CFG_PDL 10              /* 1 (default): the per-half-sweep launches of the
                                          time loops use programmatic dependent launch;
                                          0: plain stream order */
+#define NPBGB_CFG_BATCH_MODE 11       /* form of a batch, read when it is planned:
+                                         0 (default) automatic by size, 1 persistent,
+                                         2 stepped (NPBGB_BATCH_*) */
+
+/* Batch forms. */
+#define NPBGB_BATCH_PERSISTENT 1
+#define NPBGB_BATCH_STEPPED 2
 
 /* Grid kinds for batches. */
 #define NPBGB_KIND_JACOBI2D 0
@@ -247,6 +254,14 @@ NPBGB_API int32_t npbgb_batch_replan(npbgb_batch* batch, const npbgb_grid* grids
                                      int32_t band_rows);
 NPBGB_API int32_t npbgb_batch_info(const npbgb_batch* batch, int64_t* nbands, int64_t* nctas,
                                    int64_t* updates);
+/* The form the batch was planned in (NPBGB_BATCH_PERSISTENT or NPBGB_BATCH_STEPPED).
+ * Persistent: one cooperative launch whose CTAs advance bands of rows as their
+ * neighbours allow (best when the batch is small).  Stepped: one launch per
+ * half-sweep index over all tiles of the grids still active, chained by
+ * programmatic dependent launch (best when the batch fills the GPU; batches of
+ * 2^24 cells or more by default).  In the stepped form npbgb_batch_info reports
+ * the tiles as nbands and the launches as nctas.  Both forms leave the same bits. */
+NPBGB_API int32_t npbgb_batch_mode(const npbgb_batch* batch, int32_t* mode);
 NPBGB_API int32_t npbgb_batch_destroy(npbgb_batch* batch);
 
 /* Runs a batch of Jacobi-2D grids like npbgb_batch_create + npbgb_batch_launch, for callers that

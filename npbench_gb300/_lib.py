@@ -29,6 +29,9 @@ NPBGB_CFG_F64_CVT = 7
 NPBGB_CFG_JACOBI_HW_WARPS = 8
 NPBGB_CFG_BATCH_CTAS_PER_SM = 9
 NPBGB_CFG_PDL = 10
+NPBGB_CFG_BATCH_MODE = 11
+NPBGB_BATCH_PERSISTENT = 1
+NPBGB_BATCH_STEPPED = 2
 
 NPBGB_KIND_JACOBI2D = 0
 NPBGB_KIND_HEAT3D = 1
@@ -56,6 +59,7 @@ SIGNATURES = {
     "npbgb_batch_create": (_i32, [ctypes.POINTER(Grid), _i64, _i32, ctypes.POINTER(_vp)]),
     "npbgb_batch_launch": (_i32, [_vp, _i32, _vp]),
     "npbgb_batch_replan": (_i32, [_vp, ctypes.POINTER(Grid), _i64, _i32]),
+    "npbgb_batch_mode": (_i32, [_vp, ctypes.POINTER(_i32)]),
     "npbgb_batch_info": (_i32, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64),
                                  ctypes.POINTER(_i64)]),
     "npbgb_batch_destroy": (_i32, [_vp]),

@@ -4,7 +4,9 @@
         batch.launch()              # one counter reset + one cooperative persistent kernel
         batch.launch(graph=True)    # the same, captured once into a CUDA graph and replayed
 
-Every entry (A, B, TSTEPS) is a pair of CUDA tensors of one dtype (float32 or
+Batches of 2^24 cells or more run in the stepped form (one chained launch per
+half-sweep over all grids still active), smaller ones in the persistent form;
+NPBGB_CFG_BATCH_MODE forces either.  Every entry (A, B, TSTEPS) is a pair of CUDA tensors of one dtype (float32 or
 float64) with its own step count: 2D pairs are Jacobi-2D grids, 3D pairs
 Heat-3D grids.  After a launch each pair holds what ``kernel(TSTEPS, A, B)``
 of polybench/jacobi_2d/jacobi_2d_numpy.py:4-10 or
@@ -85,10 +87,16 @@ class Batch:
                    "npbgb_batch_launch")
 
     def info(self):
+        """{"mode": "persistent" | "stepped", "bands", "ctas", "updates"}; in the
+        stepped form "bands" counts tiles and "ctas" launches."""
         nb, nc, up = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
-        _lib.check(_lib.load().npbgb_batch_info(self._h, ctypes.byref(nb), ctypes.byref(nc),
-                                                ctypes.byref(up)), "npbgb_batch_info")
-        return {"bands": nb.value, "ctas": nc.value, "updates": up.value}
+        lib = _lib.load()
+        _lib.check(lib.npbgb_batch_info(self._h, ctypes.byref(nb), ctypes.byref(nc),
+                                        ctypes.byref(up)), "npbgb_batch_info")
+        mode = ctypes.c_int32()
+        _lib.check(lib.npbgb_batch_mode(self._h, ctypes.byref(mode)), "npbgb_batch_mode")
+        name = "stepped" if mode.value == _lib.NPBGB_BATCH_STEPPED else "persistent"
+        return {"mode": name, "bands": nb.value, "ctas": nc.value, "updates": up.value}
 
     def close(self):
         if self._h is not None:

@@ -19,6 +19,15 @@
 // Per point the arithmetic is that of jacobi2d.cu (bit-identical to
 // polybench/jacobi_2d/jacobi_2d_numpy.py:6-10), including the fixed-point
 // binary64 path.
+//
+// Large batches take a second form ("stepped"): one launch per half-sweep
+// index s covers every tile of every grid that still has a half-sweep s to do,
+// and consecutive launches are chained (programmatic dependent launch), so the
+// kernel boundary is the only dependency and no CTA ever waits on another.
+// Grids are sorted by their half-sweep count, so the grids active at s are a
+// prefix and launch s simply covers the first N_s tiles; a tile table maps each
+// CTA to its grid.  Small batches keep the persistent form, whose launch count
+// does not grow with the step count.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -37,6 +46,7 @@ namespace npbgb {
 extern int64_t g_cfg_f64_emulation;
 extern int64_t g_cfg_jacobi_hw_warps;
 extern int64_t g_cfg_batch_ctas_per_sm;
+extern int64_t g_cfg_batch_mode;
 
 namespace {
 
@@ -55,6 +65,19 @@ struct BandDesc {
   int16_t kind;     // NPBGB_KIND_JACOBI2D / NPBGB_KIND_HEAT3D
   int32_t left;     // band before (axis-0 indices < r0) of the same grid, or -1
   int32_t right;    // band after (indices >= r1), or -1
+};
+
+// One grid of a stepped batch.
+struct StepGrid {
+  void* a;
+  void* b;
+  int64_t first_tile;  // index of the grid's first tile in the tile table
+  int32_t n0, n1, n2;
+  int32_t step0;       // half-sweeps already done (parity of the first source)
+  int32_t count;       // half-sweeps to do in this launch chain
+  int32_t chunk;       // rows (Jacobi-2D) or planes (Heat-3D) per tile
+  int32_t tx, ty;      // tiles along the contiguous axis and the next one
+  int16_t dtype, kind;
 };
 
 __device__ unsigned int g_batch_error;  // bit 0: a CTA made no progress for the limit
@@ -181,6 +204,59 @@ batch_persistent(const BandDesc* __restrict__ bands, uint32_t* done, const int32
   }
 }
 
+// Half-sweep s of every tile in [0, gridDim.x): CTA t finds its grid in the
+// tile table and processes one tile (Jacobi-2D: 8 warps x 32 columns x chunk
+// rows; Heat-3D: a 32 x 8 column tile streamed over chunk planes).  Four CTAs
+// per SM, as the single-grid fixed-point strip kernel runs.
+__global__ void __launch_bounds__(kBThreads, 4)
+batch_step(const StepGrid* __restrict__ grids, const int32_t* __restrict__ tile_grid, int32_t s,
+           int f64_emulation, int hw_warps, uint32_t one) {
+  pdl_begin();
+  const int64_t t = blockIdx.x;
+  const StepGrid G = grids[tile_grid[t]];
+  const int64_t r = t - G.first_tile;
+  const bool odd = ((G.step0 + s) & 1) != 0;
+  const void* src = odd ? G.b : G.a;
+  void* dst = odd ? G.a : G.b;
+  const int64_t bx = r % G.tx, rest = r / G.tx;
+  if (G.kind == NPBGB_KIND_HEAT3D) {
+    __shared__ hcore::PlaneBuf<double, true> plane;  // the largest element type
+    const int64_t by = rest % G.ty, bz = rest / G.ty;
+    const int64_t k0 = 1 + bx * hcore::kTK, j0 = 1 + by * hcore::kTJ;
+    const int64_t ib = 1 + bz * G.chunk, ie = min(ib + G.chunk, int64_t(G.n0) - 1);
+    if (G.dtype == NPBGB_F64) {
+      if (f64_emulation)
+        hcore::tile_stream<double, true, false>(static_cast<const double*>(src),
+                                                static_cast<double*>(dst), G.n1, G.n2, j0, k0, ib,
+                                                ie, plane);
+      else
+        hcore::tile_stream<double, false, false>(static_cast<const double*>(src),
+                                                 static_cast<double*>(dst), G.n1, G.n2, j0, k0, ib,
+                                                 ie, reinterpret_cast<hcore::PlaneBuf<double, false>&>(plane));
+    } else {
+      hcore::tile_stream<float, false, false>(static_cast<const float*>(src),
+                                              static_cast<float*>(dst), G.n1, G.n2, j0, k0, ib,
+                                              ie, reinterpret_cast<hcore::PlaneBuf<float, false>&>(plane));
+    }
+    return;
+  }
+  const int warp = threadIdx.x >> 5;
+  const int64_t k0 = 1 + (bx * kBWarps + warp) * 32;
+  if (k0 >= G.n1 - 1) return;  // warp-uniform; the strip path has no CTA barrier
+  const int64_t ib = 1 + rest * G.chunk, ie = min(ib + G.chunk, int64_t(G.n0) - 1);
+  if (G.dtype == NPBGB_F64) {
+    const double* sp = static_cast<const double*>(src);
+    double* dp = static_cast<double*>(dst);
+    if (!f64_emulation || warp < hw_warps)
+      jcore::strip_rows<double, false, false, 1>(sp, dp, G.n1, k0, ib, ie, one);
+    else
+      jcore::strip_rows<double, true, false, 1>(sp, dp, G.n1, k0, ib, ie, one);
+  } else {
+    jcore::strip_rows<float, false, false, 4>(static_cast<const float*>(src),
+                                              static_cast<float*>(dst), G.n1, k0, ib, ie, one);
+  }
+}
+
 using PersistentFn = void (*)(const BandDesc*, uint32_t*, const int32_t*, const int32_t*, int, int,
                               uint32_t);
 
@@ -216,6 +292,12 @@ struct npbgb_batch {
   int ctas_per_sm = 2;  // persistent kernel variant chosen when planned
   cudaGraphExec_t graph = nullptr;
   cudaStream_t graph_stream = nullptr;
+  // Stepped form (mode NPBGB_BATCH_STEPPED).
+  int32_t mode = NPBGB_BATCH_PERSISTENT;
+  npbgb::StepGrid* d_step = nullptr;
+  int32_t* d_tiles = nullptr;
+  int64_t cap_step = 0, cap_tiles = 0, ntiles = 0;
+  std::vector<int32_t> launch_tiles;  // CTAs of launch s = tiles of the grids active at s
 };
 
 namespace {
@@ -279,6 +361,8 @@ double band_work(const npbgb::BandDesc& d) {
 void free_batch(npbgb_batch* b) {
   if (!b) return;
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->d_step);
+  cudaFree(b->d_tiles);
   cudaFree(b->d_bands);
   cudaFree(b->d_done);
   cudaFree(b->d_cta_off);
@@ -286,8 +370,20 @@ void free_batch(npbgb_batch* b) {
   delete b;
 }
 
+int32_t launch_stepped(npbgb_batch* b, cudaStream_t st) {
+  using namespace npbgb;
+  const int f64_emul = int(g_cfg_f64_emulation);
+  const int hw_warps = int(g_cfg_jacobi_hw_warps >= 0 ? g_cfg_jacobi_hw_warps : 1);
+  cudaError_t e = cudaSuccess;
+  for (size_t s = 0; s < b->launch_tiles.size() && e == cudaSuccess; ++s)
+    e = launch_chained(batch_step, dim3{unsigned(b->launch_tiles[s])}, dim3{unsigned(kBThreads)}, 0,
+                       st, b->d_step, b->d_tiles, int32_t(s), f64_emul, hw_warps, 1u);
+  return cuda_status(e, "batch: stepped launch");
+}
+
 int32_t launch_batch(npbgb_batch* b, cudaStream_t st) {
   using namespace npbgb;
+  if (b->mode == NPBGB_BATCH_STEPPED) return launch_stepped(b, st);
   cudaError_t e = cudaMemsetAsync(b->d_done, 0, sizeof(uint32_t) * size_t(b->nbands), st);
   if (e != cudaSuccess) return cuda_status(e, "batch: reset counters");
   int f64_emul = int(g_cfg_f64_emulation);
@@ -312,6 +408,96 @@ int32_t launch_batch(npbgb_batch* b, cudaStream_t st) {
 
 namespace {
 
+// Batches of at least this many cells take the stepped form by default: each
+// half-sweep launch then has enough tiles to fill the GPU many times over.
+constexpr int64_t kSteppedCells = int64_t(1) << 24;
+
+// The stepped form of `grids` (already validated by plan_grid).
+int32_t plan_stepped(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int32_t band_rows,
+                     int64_t updates) {
+  using namespace npbgb;
+  std::vector<StepGrid> sg;
+  for (int64_t g = 0; g < count; ++g) {
+    const npbgb_grid& G = grids[g];
+    const bool heat = G.kind == NPBGB_KIND_HEAT3D;
+    const int64_t total = G.tsteps > 1 ? 2 * int64_t(G.tsteps - 1) : 0;
+    int64_t todo = total - G.step0;
+    if (G.nsteps > 0 && G.nsteps < todo) todo = G.nsteps;
+    if (todo <= 0 || G.n0 < 3 || G.n1 < 3 || (heat && G.n2 < 3)) continue;
+    StepGrid d{};
+    d.a = G.a;
+    d.b = G.b;
+    d.n0 = int32_t(G.n0);
+    d.n1 = int32_t(G.n1);
+    d.n2 = heat ? int32_t(G.n2) : 1;
+    d.step0 = G.step0;
+    d.count = int32_t(todo);
+    d.dtype = int16_t(G.dtype);
+    d.kind = int16_t(G.kind);
+    const int32_t rows = G.band_rows > 0 ? G.band_rows : (band_rows > 0 ? band_rows : (heat ? 16 : 32));
+    d.chunk = rows;
+    if (heat) {
+      d.tx = int32_t(cdiv(G.n2 - 2, hcore::kTK));
+      d.ty = int32_t(cdiv(G.n1 - 2, hcore::kTJ));
+    } else {
+      d.tx = int32_t(cdiv(G.n1 - 2, 32 * kBWarps));
+      d.ty = 1;
+    }
+    sg.push_back(d);
+  }
+  std::stable_sort(sg.begin(), sg.end(),
+                   [](const StepGrid& x, const StepGrid& y) { return x.count > y.count; });
+  std::vector<int32_t> tiles;
+  for (size_t q = 0; q < sg.size(); ++q) {
+    StepGrid& d = sg[q];
+    const int64_t n = int64_t(d.tx) * d.ty * cdiv(int64_t(d.n0) - 2, d.chunk);
+    d.first_tile = int64_t(tiles.size());
+    if (int64_t(tiles.size()) + n > 0x7fffffff) return set_error(NPBGB_ERR_NOMEM, "batch: too many tiles");
+    tiles.insert(tiles.end(), size_t(n), int32_t(q));
+  }
+  // Launch s covers the grids with count > s: a prefix of the sorted list.
+  std::vector<int32_t> launch_tiles;
+  {
+    size_t active = sg.size();
+    const int32_t smax = sg.empty() ? 0 : sg.front().count;
+    for (int32_t st = 0; st < smax; ++st) {
+      while (active > 0 && sg[active - 1].count <= st) --active;
+      launch_tiles.push_back(int32_t(active == sg.size() ? int64_t(tiles.size())
+                                                         : sg[active].first_tile));
+    }
+  }
+  cudaError_t e;
+  const int64_t need_step = std::max<int64_t>(1, int64_t(sg.size()));
+  if (need_step > b->cap_step) {
+    cudaFree(b->d_step);
+    b->d_step = nullptr;
+    b->cap_step = 0;
+    if ((e = cudaMalloc(&b->d_step, sizeof(StepGrid) * size_t(need_step))) != cudaSuccess)
+      return cuda_status(e, "batch: alloc");
+    b->cap_step = need_step;
+  }
+  const int64_t need_tiles = std::max<int64_t>(1, int64_t(tiles.size()));
+  if (need_tiles > b->cap_tiles) {
+    cudaFree(b->d_tiles);
+    b->d_tiles = nullptr;
+    b->cap_tiles = 0;
+    if ((e = cudaMalloc(&b->d_tiles, sizeof(int32_t) * size_t(need_tiles))) != cudaSuccess)
+      return cuda_status(e, "batch: alloc");
+    b->cap_tiles = need_tiles;
+  }
+  if (!sg.empty() &&
+      ((e = cudaMemcpy(b->d_step, sg.data(), sizeof(StepGrid) * sg.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+       (e = cudaMemcpy(b->d_tiles, tiles.data(), sizeof(int32_t) * tiles.size(), cudaMemcpyHostToDevice)) != cudaSuccess))
+    return cuda_status(e, "batch: upload");
+  b->mode = NPBGB_BATCH_STEPPED;
+  b->ntiles = int64_t(tiles.size());
+  b->launch_tiles = std::move(launch_tiles);
+  b->nbands = b->ntiles;  // "nothing to do" checks use nbands
+  b->nctas = int(b->launch_tiles.size());
+  b->updates = updates;
+  return NPBGB_OK;
+}
+
 // Plans `grids` into batch b, reusing its device buffers when they are large
 // enough (they grow otherwise).  Invalidates a captured graph.
 int32_t plan_into(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int32_t band_rows) {
@@ -328,6 +514,21 @@ int32_t plan_into(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int32_
     if (int64_t(bands.size()) > 0x7fffffff) return set_error(NPBGB_ERR_NOMEM, "batch: too many bands");
     updates += up;
   }
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  int64_t cells = 0;
+  for (int64_t g = 0; g < count; ++g) {
+    const npbgb_grid& G = grids[g];
+    cells += int64_t(G.n0) * G.n1 * (G.kind == NPBGB_KIND_HEAT3D ? G.n2 : 1);
+  }
+  const int32_t mode = g_cfg_batch_mode != 0
+                           ? int32_t(g_cfg_batch_mode)
+                           : (cells >= kSteppedCells ? NPBGB_BATCH_STEPPED : NPBGB_BATCH_PERSISTENT);
+  if (mode == NPBGB_BATCH_STEPPED) return plan_stepped(b, grids, count, band_rows, updates);
+  b->mode = NPBGB_BATCH_PERSISTENT;
+  b->launch_tiles.clear();
   int per_sm = 0;
   const int ctas_per_sm = int(g_cfg_batch_ctas_per_sm);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_kernel(ctas_per_sm), kBThreads, 0);
@@ -359,10 +560,6 @@ int32_t plan_into(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int32_
   }
   off[size_t(nctas)] = int32_t(flat.size());
 
-  if (b->graph) {
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-  }
   cudaError_t e;
   const int64_t need_bands = std::max<int64_t>(1, int64_t(bands.size()));
   if (need_bands > b->cap_bands) {
@@ -470,6 +667,13 @@ int32_t npbgb_batch_info(const npbgb_batch* b, int64_t* nbands, int64_t* nctas, 
   if (nbands) *nbands = b->nbands;
   if (nctas) *nctas = b->nctas;
   if (updates) *updates = b->updates;
+  return NPBGB_OK;
+}
+
+int32_t npbgb_batch_mode(const npbgb_batch* b, int32_t* mode) {
+  using namespace npbgb;
+  if (!b || !mode) return set_error(NPBGB_ERR_ARG, "batch: null handle or output");
+  *mode = b->mode;
   return NPBGB_OK;
 }
 

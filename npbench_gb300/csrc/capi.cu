@@ -21,6 +21,7 @@ int64_t g_cfg_jacobi_hw_warps = -1;  // -1: default
 int64_t g_cfg_batch_ctas_per_sm = 3;
 int64_t g_cfg_jacobi_chunk = 0;
 int64_t g_cfg_pdl = 1;
+int64_t g_cfg_batch_mode = 0;
 
 uint32_t take_heat_device_error();
 uint32_t take_batch_device_error();
@@ -140,6 +141,10 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       if (value != 0 && value != 1) return set_error(NPBGB_ERR_ARG, "PDL: 0 or 1");
       g_cfg_pdl = value;
       return NPBGB_OK;
+    case NPBGB_CFG_BATCH_MODE:
+      if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "batch mode: 0, 1 or 2");
+      g_cfg_batch_mode = value;
+      return NPBGB_OK;
     default:
       return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
   }
@@ -159,6 +164,7 @@ int32_t npbgb_get_config(int32_t key, int64_t* value) {
     case NPBGB_CFG_JACOBI_HW_WARPS: *value = g_cfg_jacobi_hw_warps; return NPBGB_OK;
     case NPBGB_CFG_BATCH_CTAS_PER_SM: *value = g_cfg_batch_ctas_per_sm; return NPBGB_OK;
     case NPBGB_CFG_PDL: *value = g_cfg_pdl; return NPBGB_OK;
+    case NPBGB_CFG_BATCH_MODE: *value = g_cfg_batch_mode; return NPBGB_OK;
     default: return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
   }
 }

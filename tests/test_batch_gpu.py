@@ -1,4 +1,9 @@
-"""Batched persistent launch == per-grid launches == the oracle, on the GPU."""
+"""Batched launches == per-grid launches == the oracle, on the GPU.
+
+Every test runs twice: with the batch forced into its persistent form (one
+cooperative launch, neighbour counters) and into its stepped form (one chained
+launch per half-sweep index), which must leave the same bits.
+"""
 import numpy as np
 import pytest
 
@@ -14,6 +19,14 @@ from npbench_gb300.batch import Batch  # noqa: E402
 from oracle import cref  # noqa: E402
 
 DEV = torch.device("cuda", 0)
+
+
+@pytest.fixture(autouse=True, params=[_lib.NPBGB_BATCH_PERSISTENT, _lib.NPBGB_BATCH_STEPPED],
+                ids=["persistent", "stepped"])
+def batch_mode(request):
+    old = _lib.set_config(_lib.NPBGB_CFG_BATCH_MODE, request.param)
+    yield request.param
+    _lib.set_config(_lib.NPBGB_CFG_BATCH_MODE, old)
 
 
 def _mixed_batch(n, seed, max_side=300, max_t=40):
@@ -142,3 +155,12 @@ def test_batch_resumed_in_pieces_equals_one_run():
         ra, rb = A.copy(), B.copy()
         (cref.jacobi_2d_kernel if A.ndim == 2 else cref.heat_3d_kernel)(T, ra, rb)
         assert bits_equal(dA.cpu().numpy(), ra) and bits_equal(dB.cpu().numpy(), rb), n
+
+
+def test_batch_reports_its_form(batch_mode):
+    A = torch.rand((40, 50), dtype=torch.float64, device=DEV)
+    B = A.clone()
+    with Batch([(A, B, 5)]) as bt:
+        info = bt.info()
+    assert info["mode"] == ("stepped" if batch_mode == _lib.NPBGB_BATCH_STEPPED else "persistent")
+    assert info["updates"] == 8 * 38 * 48
