@@ -16,29 +16,50 @@ performs at most nsteps (0 = all remaining).  The tensors must stay alive
 while the batch is used.
 """
 import ctypes
+import threading
 
 from . import _lib
 
 __all__ = ["Batch"]
 
+_MODES = {None: 0, "auto": 0, "persistent": _lib.NPBGB_BATCH_PERSISTENT,
+          "stepped": _lib.NPBGB_BATCH_STEPPED}
+_plan_lock = threading.Lock()
+
+
+def _planned(mode, fn):
+    """Runs fn() (a create or replan) with the batch form `mode` in force."""
+    code = _MODES[mode]
+    if code == 0:
+        return fn()
+    with _plan_lock:
+        old = _lib.set_config(_lib.NPBGB_CFG_BATCH_MODE, code)
+        try:
+            return fn()
+        finally:
+            _lib.set_config(_lib.NPBGB_CFG_BATCH_MODE, old)
+
 
 class Batch:
-    def __init__(self, grids, band_rows=0, band_rows_of=None):
-        """grids: iterable of (A, B, TSTEPS); band_rows_of(A) may pick rows per band."""
+    def __init__(self, grids, band_rows=0, band_rows_of=None, mode=None):
+        """grids: iterable of (A, B, TSTEPS); band_rows_of(A) may pick rows per band;
+        mode: None (by size), "persistent" or "stepped"."""
         self._h = None
         arr = self._structs(grids, band_rows_of)
         h = ctypes.c_void_p()
-        _lib.check(_lib.load().npbgb_batch_create(arr, len(grids), int(band_rows), ctypes.byref(h)),
-                   "npbgb_batch_create")
+        _planned(mode, lambda: _lib.check(
+            _lib.load().npbgb_batch_create(arr, len(grids), int(band_rows), ctypes.byref(h)),
+            "npbgb_batch_create"))
         self._h = h
 
-    def replan(self, grids, band_rows=0, band_rows_of=None):
+    def replan(self, grids, band_rows=0, band_rows_of=None, mode=None):
         """Re-plan this batch for a new grid list, reusing its device buffers."""
         if self._h is None:
             raise RuntimeError("batch destroyed")
         arr = self._structs(grids, band_rows_of)
-        _lib.check(_lib.load().npbgb_batch_replan(self._h, arr, len(grids), int(band_rows)),
-                   "npbgb_batch_replan")
+        _planned(mode, lambda: _lib.check(
+            _lib.load().npbgb_batch_replan(self._h, arr, len(grids), int(band_rows)),
+            "npbgb_batch_replan"))
 
     def _structs(self, grids, band_rows_of):
         import torch
