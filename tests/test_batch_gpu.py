@@ -164,3 +164,15 @@ def test_batch_reports_its_form(batch_mode):
         info = bt.info()
     assert info["mode"] == ("stepped" if batch_mode == _lib.NPBGB_BATCH_STEPPED else "persistent")
     assert info["updates"] == 8 * 38 * 48
+
+
+def test_batch_form_can_be_chosen_per_batch(batch_mode):
+    """Batch(..., mode=...) overrides the configured form for that plan only."""
+    A = torch.rand((40, 50), dtype=torch.float32, device=DEV)
+    B = A.clone()
+    for name in ("persistent", "stepped"):
+        with Batch([(A, B, 3)], mode=name) as bt:
+            assert bt.info()["mode"] == name
+            bt.replan([(A, B, 4)], mode=name)
+            assert bt.info()["mode"] == name
+    assert _lib.get_config(_lib.NPBGB_CFG_BATCH_MODE) == batch_mode
