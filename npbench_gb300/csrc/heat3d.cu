@@ -172,6 +172,25 @@ heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ sr
 #pragma unroll
     for (int r = 0; r < R + 2; ++r) col[r] = pc[(row0 + r) * G::BX + tx + 1];
     const int64_t gbase = i * s0 + (j0 + row0) * s1 + k;
+    if constexpr (!FX && sizeof(T) == 4 && R % 2 == 0) {
+      // binary32: rows r and r+1 in one packed f32x2 evaluation.
+      if (k_ok) {
+#pragma unroll
+        for (int r = 0; r < R; r += 2) {
+          const int row = row0 + r;
+          if (j0 + row >= n1 - 1) break;
+          const int off = (row + 1) * G::BX + (tx + 1);
+          const int64_t g = gbase + r * s1;
+          const F2 o = hcore::heat_point2(
+              f2(col[r + 1], col[r + 2]), f2(pp[off], pp[off + G::BX]), f2(pm[off], pm[off + G::BX]),
+              f2(col[r + 2], col[r + 3]), f2(col[r], col[r + 1]),
+              f2(pc[off + 1], pc[off + 1 + G::BX]), f2(pc[off - 1], pc[off - 1 + G::BX]));
+          dst[g] = f2x(o);
+          if (j0 + row + 1 < n1 - 1) dst[g + s1] = f2y(o);
+        }
+      }
+      continue;
+    }
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int row = row0 + r;

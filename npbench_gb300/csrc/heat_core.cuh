@@ -37,6 +37,17 @@ __device__ __forceinline__ T heat_point(T c, T ip, T im, T jp, T jm, T kp, T km)
   return add_rn(add_rn(add_rn(t0, t1), t2), c);
 }
 
+// Two binary32 points at once (packed f32x2, npbgb_common.cuh); each result is
+// bit-identical to heat_point<float>.  Element x is the first point, y the second.
+__device__ __forceinline__ F2 heat_point2(F2 c, F2 ip, F2 im, F2 jp, F2 jm, F2 kp, F2 km) {
+  const F2 two = f2(2.0f, 2.0f), eighth = f2(0.125f, 0.125f);
+  const F2 c2 = mul2(two, c);
+  const F2 t0 = mul2(eighth, add2(sub2(ip, c2), im));
+  const F2 t1 = mul2(eighth, add2(sub2(jp, c2), jm));
+  const F2 t2 = mul2(eighth, add2(sub2(kp, c2), km));
+  return add2(add2(add2(t0, t1), t2), c);
+}
+
 // Fixed-point form of heat_point; inputs in frame 59, result as a double.
 __device__ __forceinline__ double heat_point_fx(int64_t c, int64_t ip, int64_t im, int64_t jp,
                                                 int64_t jm, int64_t kp, int64_t km) {

@@ -99,6 +99,29 @@ struct Strip {
   }
 };
 
+// binary32, two consecutive output rows i and i+1 at once: rows i-1 .. i+2 of
+// the column (x0..x3) and the halo values of rows i and i+1 (h1, h2).  The
+// five operators run as packed f32x2 instructions (two IEEE round-to-nearest
+// operations each), so both results are bit-identical to Strip::point.
+template <bool CG>
+__device__ __forceinline__ void points2_f32(const Strip<float, false, CG>& sp, int64_t i, float x0,
+                                            float x1, float x2, float x3, float h1, float h2) {
+  const int lane = threadIdx.x & 31;
+  float w1 = __shfl_up_sync(0xffffffffu, x1, 1), e1 = __shfl_down_sync(0xffffffffu, x1, 1);
+  float w2 = __shfl_up_sync(0xffffffffu, x2, 1), e2 = __shfl_down_sync(0xffffffffu, x2, 1);
+  if (lane == 0) { w1 = h1; w2 = h2; }
+  if (lane == 31) { e1 = h1; e2 = h2; }
+  F2 acc = add2(f2(x1, x2), f2(w1, w2));
+  acc = add2(acc, f2(e1, e2));
+  acc = add2(acc, f2(x2, x3));
+  acc = add2(acc, f2(x0, x1));
+  const F2 out = mul2(f2(0.2f, 0.2f), acc);
+  if (sp.active) {
+    st<CG>(sp.dst + i * sp.nx + sp.j, f2x(out));
+    st<CG>(sp.dst + (i + 1) * sp.nx + sp.j, f2y(out));
+  }
+}
+
 // One strip (columns k0 .. k0+31) over rows [r0, r1).  Warp-collective.
 template <typename T, bool FX, bool CG, int U>
 __device__ __forceinline__ void strip_rows(const T* src, T* dst, int64_t nx, int64_t k0, int64_t r0,
@@ -115,8 +138,14 @@ __device__ __forceinline__ void strip_rows(const T* src, T* dst, int64_t nx, int
   for (; i + U <= r1; i += U) {
 #pragma unroll
     for (int u = 0; u < U; ++u) s.load(i + 1 + u, x[2 + u], h[2 + u]);
+    if constexpr (!FX && std::is_same<T, float>::value && U % 2 == 0) {
 #pragma unroll
-    for (int u = 0; u < U; ++u) s.point(i + u, x[u], x[u + 1], x[u + 2], h[u + 1]);
+      for (int u = 0; u < U; u += 2)
+        points2_f32<CG>(s, i + u, x[u], x[u + 1], x[u + 2], x[u + 3], h[u + 1], h[u + 2]);
+    } else {
+#pragma unroll
+      for (int u = 0; u < U; ++u) s.point(i + u, x[u], x[u + 1], x[u + 2], h[u + 1]);
+    }
     x[0] = x[U];
     x[1] = x[U + 1];
     h[1] = h[U + 1];
