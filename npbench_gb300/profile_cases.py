@@ -17,6 +17,8 @@ hdiff      hdiff 256x256x160 float64, 3 calls             hdiff_tile, -s 1
 vadv       vadv 256x256x160 float64, 3 calls              vadv_columns, -s 1
 cavity     cavity_flow 101x101, nt=20, nit=50, 2 calls    cavity_bands, -s 1
 batch      256 mixed Jacobi-2D grids, 2 launches          batch_persistent, -s 1
+batch_step 256 mixed grids, stepped form, one pass        batch_step, -s 20
+jacobi_f64_1000  Jacobi-2D 1000^2 float64, TSTEPS=3       jacobi2d_strip, -s 2
 ========== ============================================== ===================
 """
 import sys
@@ -54,6 +56,22 @@ def run(case):
         a, b, c = (torch.from_numpy(t).to(dev) for t in (u, v, p))
         for _ in range(2):
             stencils.cavity_flow(101, 101, 20, 50, a, b, dt, dx, dy, c, 1.0, 0.1)
+    elif case == "jacobi_f64_1000":
+        A, B = workloads.uniform_pair((1000, 1000), np.float64, seed=11)
+        a, b = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+        stencils.jacobi_2d_kernel(3, a, b)
+    elif case == "batch_step":
+        from npbench_gb300.batch import Batch
+        specs = workloads.batch_jacobi_specs(256, seed=0, tsteps=(10, 40))
+        g = torch.Generator(device=dev)
+        g.manual_seed(0)
+        work = []
+        for (ny, nx), dtp, T in specs:
+            tdt = torch.float64 if dtp == np.float64 else torch.float32
+            work.append((torch.rand((ny, nx), dtype=tdt, device=dev, generator=g),
+                         torch.rand((ny, nx), dtype=tdt, device=dev, generator=g), T))
+        with Batch(work, mode="stepped") as bt:
+            bt.launch()
     elif case == "batch":
         from npbench_gb300.batch import Batch
         specs = workloads.batch_jacobi_specs(256, seed=0, tsteps=(10, 40))
