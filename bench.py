@@ -713,7 +713,7 @@ def run_batch(args):
 
     ups = sum(2 * (T - 1) * (s[0] - 2) * (s[1] - 2) for s, _, T in specs)
     alg = sum(2 * (T - 1) * (s[0] - 2) * (s[1] - 2) * 2 * np.dtype(dt).itemsize for s, dt, T in specs)
-    with Batch(work, band_rows=64) as batch:
+    with Batch(work, band_rows=128) as batch:
         info = batch.info()
         with ClockSampler(0) as clk:
             ms = _timed_steps(torch, dev, stream, lambda: batch.launch(graph=True), reset,
@@ -739,7 +739,7 @@ def run_batch(args):
         {"cells": cells, "updates_per_step": ups, "form": info["mode"],
          "tiles" if info["mode"] == "stepped" else "bands": info["bands"],
          "launches" if info["mode"] == "stepped" else "ctas": info["ctas"],
-         "rows_per_tile" if info["mode"] == "stepped" else "band_rows": 64, "graph": True, "l2": f"{cells * 6 * 2 / 1e9:.1f} GB resident, "
+         "rows_per_tile" if info["mode"] == "stepped" else "band_rows": 128, "graph": True, "l2": f"{cells * 6 * 2 / 1e9:.1f} GB resident, "
                                                 "far above L2"},
         roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                   "frac": ach / peak, "peak_kind": kind, "traffic": None},

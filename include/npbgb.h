@@ -62,7 +62,7 @@ extern "C" {
                                      convert instructions; 0: integer bit operations */
 #define NPBGB_CFG_JACOBI_HW_WARPS 8 /* jacobi2d / batch binary64: warps per CTA (of 8)
                                        that use hardware binary64 next to the
-                                       fixed-point warps; -1 (default) = 1 */
+                                       fixed-point warps; -1 (default) = 4 */
 #define NPBGB_CFG_BATCH_CTAS_PER_SM 9 /* persistent batch kernel: 2 or 3 (default)
                                          CTAs per SM (read when a batch is planned) */
 #define NPBGB_CFG_PDL 10              /* 1 (default): the per-half-sweep launches of the

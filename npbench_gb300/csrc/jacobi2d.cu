@@ -40,8 +40,8 @@ jacobi2d_strip(const T* __restrict__ src, T* __restrict__ dst, int64_t ny, int64
   if (k0 >= nx - 1) return;  // whole strip outside the interior (warp-uniform)
   const int64_t ib = 1 + int64_t(blockIdx.y) * chunk;
   const int64_t ie = (ib + chunk < ny - 1) ? ib + chunk : ny - 1;
-  // Rows loaded ahead: 4 for the memory-bound forms; 1 for the fixed-point
-  // form, which is integer-pipe bound and wants the registers for occupancy.
+  // Rows loaded ahead: 4 for binary32; 1 for binary64, whose chunks are short
+  // (2 ahead measured 5-10% slower at 500^2 to 4096^2 with 4 hardware warps).
   if (FX && warp < hw_warps)
     jcore::strip_rows<T, false, false, 1>(src, dst, nx, k0, ib, ie, one);
   else
@@ -50,11 +50,13 @@ jacobi2d_strip(const T* __restrict__ src, T* __restrict__ dst, int64_t ny, int64
 
 int pick_chunk(int64_t ny, int64_t col_blocks) {
   if (g_cfg_jacobi_chunk > 0) return int(g_cfg_jacobi_chunk);
-  // About 16 warps per SM over 152 SMs, rows per warp at least 8.
+  // About 16 warps per SM over 152 SMs, rows per warp at least 3 (small
+  // grids want short chunks for enough CTAs: 3-4 rows measured best at 500^2
+  // and 1000^2, the computed chunk at 2000^2 and 4096^2).
   const int64_t target_blocks = int64_t(sm_count()) * 16 / kWarps * 4;
   int64_t chunks = cdiv(target_blocks, col_blocks > 0 ? col_blocks : 1);
   int64_t c = cdiv(ny - 2, chunks > 0 ? chunks : 1);
-  if (c < 8) c = 8;
+  if (c < 3) c = 3;
   if (c > ny - 2) c = ny - 2;
   return int(c);
 }
@@ -67,7 +69,7 @@ int32_t run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st)
   const int64_t gy = cdiv(ny - 2, chunk);
   if (gx > 0x7fffffff || gy > 65535) return set_error(NPBGB_ERR_ARG, "jacobi2d: extent too large");
   const dim3 grid{unsigned(gx), unsigned(gy)};
-  const int hw = int(g_cfg_jacobi_hw_warps >= 0 ? g_cfg_jacobi_hw_warps : 1);
+  const int hw = jacobi_hw_warps();
   const dim3 block{32u * kWarps};
   cudaError_t e = cudaSuccess;
   for (int32_t t = 1; t < tsteps && e == cudaSuccess; ++t) {

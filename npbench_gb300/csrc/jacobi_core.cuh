@@ -18,6 +18,17 @@
 #include "npbgb_common.cuh"
 
 namespace npbgb {
+
+extern int64_t g_cfg_jacobi_hw_warps;
+
+// Warps of 8 per CTA that take the hardware binary64 path next to the
+// fixed-point warps (binary64 Jacobi-2D).  Measured on GB300 at 500^2 to
+// 4096^2, 4 of 8 keeps both the integer and the binary64 pipe busiest
+// (1.2-2.4x faster than 1 of 8); NPBGB_CFG_JACOBI_HW_WARPS overrides.
+inline int jacobi_hw_warps() {
+  return int(g_cfg_jacobi_hw_warps >= 0 ? g_cfg_jacobi_hw_warps : 4);
+}
+
 namespace jcore {
 
 template <bool CG, typename T>
