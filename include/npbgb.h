@@ -54,10 +54,10 @@ extern "C" {
                                      arrays allow it; 0: plain loads only */
 #define NPBGB_CFG_JACOBI_CHUNK 4  /* rows per warp in jacobi2d; 0 = automatic */
 #define NPBGB_CFG_HEAT_ROWS 5     /* axis-1 tile rows per thread in heat3d (TMA): 1, 2, 4;
-                                     0 (default) = 4 for binary32, 1 for binary64 */
+                                     0 (default) = 4 for binary32, 2 for binary64 */
 #define NPBGB_CFG_HEAT_HW_ROWS 6  /* heat3d binary64: tile rows per CTA evaluated with
                                      hardware binary64 next to the fixed-point rows;
-                                     -1 (default) = 2 */
+                                     -1 (default) = a quarter of the tile rows */
 #define NPBGB_CFG_F64_CVT 7       /* 1: fixed-point conversions use the binary64
                                      convert instructions; 0: integer bit operations */
 #define NPBGB_CFG_JACOBI_HW_WARPS 8 /* jacobi2d / batch binary64: warps per CTA (of 8)

@@ -237,10 +237,13 @@ heat3d_ldg(const T* __restrict__ src, T* __restrict__ dst, int64_t n0, int64_t n
   hcore::tile_stream<T, FX, false>(src, dst, n1, n2, j0, k0, ib, ie, plane);
 }
 
-int auto_chunk(int64_t n0, int64_t tiles, int ctas_per_sm) {
-  // Smallest number of axis-0 chunks that fills about two waves of CTAs.
+int auto_chunk(int64_t n0, int64_t tiles, int ctas_per_sm, int waves) {
+  // Smallest number of axis-0 chunks that fills about `waves` waves of CTAs:
+  // 2 for binary32 (memory-bound; long chunks amortise the halo planes), 16
+  // for binary64 (pipe-bound; many short CTAs balance the last wave: 8-plane
+  // chunks measured 6% faster than 64 at 256^3).
   const int64_t slots = int64_t(sm_count()) * (ctas_per_sm > 0 ? ctas_per_sm : 1);
-  int64_t chunks = cdiv(2 * slots, tiles > 0 ? tiles : 1);
+  int64_t chunks = cdiv(int64_t(waves) * slots, tiles > 0 ? tiles : 1);
   if (chunks < 1) chunks = 1;
   int64_t c = cdiv(n0 - 2, chunks);
   if (c < 4) c = 4;
@@ -268,12 +271,15 @@ int32_t launch_tma(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tstep
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heat3d_tma<T, FX, R, CVT>, kThreads, smem);
   const int64_t gx = cdiv(n2 - 2, kTK), gy = cdiv(n1 - 2, G::TJ);
-  const int chunk = g_cfg_heat_chunk > 0 ? int(g_cfg_heat_chunk) : auto_chunk(n0, gx * gy, per_sm);
+  const int chunk = g_cfg_heat_chunk > 0 ? int(g_cfg_heat_chunk)
+                                         : auto_chunk(n0, gx * gy, per_sm, FX ? 16 : 2);
   const int64_t gz = cdiv(n0 - 2, chunk);
   if (gy > 65535 || gz > 65535 || gx > 0x7fffffff)
     return set_error(NPBGB_ERR_ARG, "heat3d: extent too large");
   const dim3 grid{unsigned(gx), unsigned(gy), unsigned(gz)};
-  int hw = g_cfg_heat_hw_rows >= 0 ? int(g_cfg_heat_hw_rows) : (FX ? 2 : 0);
+  // A quarter of the tile rows on the hardware binary64 pipe (measured best
+  // at 256^3 with 1 or 2 rows per warp).
+  int hw = g_cfg_heat_hw_rows >= 0 ? int(g_cfg_heat_hw_rows) : (FX ? G::TJ / 4 : 0);
   if (hw > G::TJ) hw = G::TJ;
   const dim3 block{unsigned(kThreads)};
   cudaError_t e = cudaSuccess;
@@ -292,7 +298,8 @@ int32_t launch_ldg(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tstep
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heat3d_ldg<T, FX>, kThreads, 0);
   const int64_t gx = cdiv(n2 - 2, kTK), gy = cdiv(n1 - 2, kTJ);
-  const int chunk = g_cfg_heat_chunk > 0 ? int(g_cfg_heat_chunk) : auto_chunk(n0, gx * gy, per_sm);
+  const int chunk = g_cfg_heat_chunk > 0 ? int(g_cfg_heat_chunk)
+                                         : auto_chunk(n0, gx * gy, per_sm, FX ? 16 : 2);
   const int64_t gz = cdiv(n0 - 2, chunk);
   if (gy > 65535 || gz > 65535 || gx > 0x7fffffff)
     return set_error(NPBGB_ERR_ARG, "heat3d: extent too large");
@@ -313,7 +320,7 @@ int32_t run(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps, cuda
   if (g_cfg_heat_tma) {
     // Tuned on GB300 (256^3): binary32 is memory-latency bound and wants more
     // rows per thread; binary64 (integer-pipe bound) wants one.
-    const int rows = g_cfg_heat_rows > 0 ? int(g_cfg_heat_rows) : (sizeof(T) == 4 ? 4 : 1);
+    const int rows = g_cfg_heat_rows > 0 ? int(g_cfg_heat_rows) : (sizeof(T) == 4 ? 4 : 2);
     const bool cvt = g_cfg_f64_cvt != 0;
     int32_t r;
     if (rows >= 4)
