@@ -1,0 +1,95 @@
+"""npbench_gb300.autotune: the per-shape cache of launch settings.
+
+CPU: cache keys, the JSON round trip, and that a cached setting is applied for
+exactly the duration of a call and restored after it (the library's knobs are
+host-side state, so this needs no GPU).  GPU: tuning a small grid stores a
+setting, every candidate it timed left the default setting's bits, and a
+tuned call still matches the oracle bit for bit.
+"""
+import json
+
+import numpy as np
+import pytest
+
+from npbench_gb300 import _lib, autotune
+
+
+@pytest.fixture
+def cache(tmp_path, monkeypatch):
+    path = tmp_path / "tune.json"
+    monkeypatch.setenv("NPBGB_TUNE_CACHE", str(path))
+    autotune.load_cache(refresh=True)
+    was = autotune.enabled()
+    yield path
+    (autotune.enable if was else autotune.disable)()
+    monkeypatch.delenv("NPBGB_TUNE_CACHE")
+    autotune.load_cache(refresh=True)
+
+
+def test_keys_name_benchmark_dtype_and_shape():
+    assert autotune.key("jacobi_2d", (2800, 2800), np.float64) == "jacobi_2d/float64/2800x2800"
+    assert autotune.key("heat_3d", [120, 120, 120], "float32") == "heat_3d/float32/120x120x120"
+    torch = pytest.importorskip("torch")
+    assert autotune.key("heat_3d", (4, 5, 6), torch.float64) == "heat_3d/float64/4x5x6"
+
+
+def test_search_spaces():
+    sp = autotune._space("jacobi_2d", np.float64)
+    assert {"JACOBI_HW_WARPS": 4, "JACOBI_CHUNK": 3} in sp and len(sp) == 49
+    assert all(c["JACOBI_HW_WARPS"] == -1 for c in autotune._space("jacobi_2d", np.float32))
+    heat = autotune._space("heat_3d", np.float64)
+    assert {"HEAT_ROWS": 2, "HEAT_HW_ROWS": 4, "HEAT_CHUNK": 8} in heat
+    with pytest.raises(ValueError):
+        autotune._space("hdiff", np.float64)
+
+
+def test_cached_setting_applies_for_the_call_only(cache):
+    cache.write_text(json.dumps({"jacobi_2d/float64/40x50": {
+        "config": {"JACOBI_HW_WARPS": 6, "JACOBI_CHUNK": 5}, "ms": 1.0, "default_ms": 2.0}}))
+    autotune.load_cache(refresh=True)
+    before = (_lib.get_config(_lib.NPBGB_CFG_JACOBI_HW_WARPS),
+              _lib.get_config(_lib.NPBGB_CFG_JACOBI_CHUNK))
+    autotune.disable()
+    with autotune.applied("jacobi_2d", (40, 50), np.float64) as cfg:
+        assert cfg is None
+    autotune.enable()
+    with autotune.applied("jacobi_2d", (40, 50), np.float64) as cfg:
+        assert cfg == {"JACOBI_HW_WARPS": 6, "JACOBI_CHUNK": 5}
+        assert _lib.get_config(_lib.NPBGB_CFG_JACOBI_HW_WARPS) == 6
+        assert _lib.get_config(_lib.NPBGB_CFG_JACOBI_CHUNK) == 5
+    with autotune.applied("jacobi_2d", (41, 50), np.float64) as cfg:  # other shape: nothing
+        assert cfg is None
+    assert (_lib.get_config(_lib.NPBGB_CFG_JACOBI_HW_WARPS),
+            _lib.get_config(_lib.NPBGB_CFG_JACOBI_CHUNK)) == before
+
+
+def test_store_merges_entries(cache):
+    autotune._store("a/float64/1x1", {"config": {}, "ms": 1.0})
+    autotune._store("b/float64/2x2", {"config": {}, "ms": 2.0})
+    data = json.loads(cache.read_text())
+    assert set(data) == {"a/float64/1x1", "b/float64/2x2"}
+
+
+@pytest.mark.gpu
+def test_tune_then_tuned_call_is_bit_exact(cache):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from conftest import bits_equal
+    from npbench_gb300 import stencils, workloads
+    from oracle import cref
+    space = [{"JACOBI_HW_WARPS": hw, "JACOBI_CHUNK": ch} for hw in (0, 4, 8) for ch in (0, 3)]
+    entry = autotune.tune("jacobi_2d", (130, 300), np.float64, tsteps=5, space=space)
+    assert entry["candidates"] == 6 and entry["ms"] <= entry["default_ms"]
+    assert autotune.key("jacobi_2d", (130, 300), np.float64) in json.loads(cache.read_text())
+    autotune.enable()
+    A, B = workloads.uniform_pair((130, 300), np.float64, seed=5)
+    dA = torch.from_numpy(A).cuda()
+    dB = torch.from_numpy(B).cuda()
+    stencils.jacobi_2d_kernel(9, dA, dB)
+    cref.jacobi_2d_kernel(9, A, B)
+    assert bits_equal(dA.cpu().numpy(), A) and bits_equal(dB.cpu().numpy(), B)
+    heat = autotune.tune("heat_3d", (20, 30, 70), np.float32, tsteps=4,
+                         space=[{"HEAT_ROWS": r, "HEAT_HW_ROWS": -1, "HEAT_CHUNK": c}
+                                for r in (1, 4) for c in (0, 4)])
+    assert heat["candidates"] == 4
