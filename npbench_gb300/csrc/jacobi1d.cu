@@ -7,8 +7,8 @@
 // The arrays are small (NPBench's presets go up to 34000 points), so a plain
 // one-launch-per-half-sweep loop is bound by launch latency.  Instead each
 // launch performs kSteps half-sweeps with temporal blocking: a CTA stages its
-// segment of kW points (128 to 1024, chosen per array so that the CTAs
-// cover the SMs) plus kSteps halo points on each side into shared
+// segment of w points (one segment per SM, at least 32) plus kSteps halo
+// points on each side into shared
 // memory, runs the half-sweeps there (the valid region shrinks by one point
 // per side and half-sweep, so every kept value is computed exactly as the
 // reference computes it), and writes back its segment of both arrays: A
@@ -23,70 +23,72 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kSteps = 32;            // half-sweeps per launch (even)
 
-// kW: points written per CTA; chosen per array so that the segments cover the
-// SMs (the arithmetic is bound by the small binary64 pipe, so idle SMs cost).
-template <typename T, int kW>
+// w: points written per CTA, chosen per array so that the CTAs cover the SMs
+// exactly (the arithmetic is bound by the small binary64 pipe, so an idle SM
+// costs and so does an SM with a larger share).  The two staged copies live in
+// dynamic shared memory, w + 2*kSteps points each.
+template <typename T>
 __global__ void __launch_bounds__(kThreads)
-jacobi1d_block(T* __restrict__ a, T* __restrict__ b, int64_t n, int steps) {
+jacobi1d_block(T* __restrict__ a, T* __restrict__ b, int64_t n, int steps, int w) {
   pdl_begin();
-  constexpr int kSpan = kW + 2 * kSteps;  // staged points per CTA
-  __shared__ T buf[2][kSpan];
+  extern __shared__ __align__(16) unsigned char jac1_smem[];
+  const int span = w + 2 * kSteps;  // staged points per CTA
+  T* buf0 = reinterpret_cast<T*>(jac1_smem);
+  T* buf1 = buf0 + span;
   const T k = T(0.33333);
-  const int64_t seg = int64_t(blockIdx.x) * kW;       // first written point - 1 (interior starts at 1)
+  const int64_t seg = int64_t(blockIdx.x) * w;        // first written point - 1 (interior starts at 1)
   const int64_t base = 1 + seg - kSteps;              // global index of buf[.][0]
-  // Stage A (state h) into buf[0] and B into buf[1]; points outside [0, n) are unused.
-  for (int q = threadIdx.x; q < kSpan; q += kThreads) {
+  // Stage A (state h) into buf0 and B into buf1; points outside [0, n) are unused.
+  for (int q = threadIdx.x; q < span; q += kThreads) {
     const int64_t g = base + q;
     const bool in = g >= 0 && g < n;
-    buf[0][q] = in ? a[g] : T(0);
-    buf[1][q] = in ? b[g] : T(0);
+    buf0[q] = in ? a[g] : T(0);
+    buf1[q] = in ? b[g] : T(0);
   }
   __syncthreads();
   // Half-sweep s reads buf[s & 1] and writes buf[(s + 1) & 1] for local points
-  // q in [s + 1, kSpan - 1 - s) whose global index is an interior point.
+  // q in [s + 1, span - 1 - s) whose global index is an interior point.
   for (int s = 0; s < steps; ++s) {
-    const T* src = buf[s & 1];
-    T* dst = buf[(s + 1) & 1];
-    for (int q = s + 1 + threadIdx.x; q < kSpan - 1 - s; q += kThreads) {
+    const T* src = (s & 1) ? buf1 : buf0;
+    T* dst = (s & 1) ? buf0 : buf1;
+    for (int q = s + 1 + threadIdx.x; q < span - 1 - s; q += kThreads) {
       const int64_t g = base + q;
       if (g >= 1 && g < n - 1) dst[q] = mul_rn(k, add_rn(add_rn(src[q - 1], src[q]), src[q + 1]));
     }
     __syncthreads();
   }
-  // steps is even: buf[0] holds the newest field (A) and buf[1] the one before (B).
-  for (int q = kSteps + threadIdx.x; q < kSteps + kW; q += kThreads) {
+  // steps is even: buf0 holds the newest field (A) and buf1 the one before (B).
+  for (int q = kSteps + threadIdx.x; q < kSteps + w; q += kThreads) {
     const int64_t g = base + q;
     if (g >= 1 && g < n - 1) {
-      a[g] = buf[0][q];
-      b[g] = buf[1][q];
+      a[g] = buf0[q];
+      b[g] = buf1[q];
     }
   }
-}
-
-template <typename T, int kW>
-int32_t run_w(T* a, T* b, int64_t n, int32_t tsteps, cudaStream_t st) {
-  const int64_t blocks = cdiv(n - 2, kW);
-  if (blocks > 0x7fffffff) return set_error(NPBGB_ERR_ARG, "jacobi1d: extent too large");
-  int64_t left = 2 * int64_t(tsteps - 1);  // half-sweeps, even
-  cudaError_t e = cudaSuccess;
-  while (left > 0 && e == cudaSuccess) {
-    const int s = int(left < kSteps ? left : kSteps);
-    e = launch_chained(jacobi1d_block<T, kW>, dim3{unsigned(blocks)}, dim3{unsigned(kThreads)}, 0,
-                       st, a, b, n, s);
-    left -= s;
-  }
-  return cuda_status(e, "jacobi1d_block");
 }
 
 template <typename T>
 int32_t run(T* a, T* b, int64_t n, int32_t tsteps, cudaStream_t st) {
   if (tsteps <= 1 || n < 3) return NPBGB_OK;
-  // Widest segment that still gives every SM a CTA.
-  const int64_t per_sm = cdiv(n - 2, sm_count());
-  if (per_sm <= 128) return run_w<T, 128>(a, b, n, tsteps, st);
-  if (per_sm <= 256) return run_w<T, 256>(a, b, n, tsteps, st);
-  if (per_sm <= 512) return run_w<T, 512>(a, b, n, tsteps, st);
-  return run_w<T, 1024>(a, b, n, tsteps, st);
+  // One segment per SM: at least 32 points, and at most what keeps both
+  // staged copies within the default 48 KB of dynamic shared memory (larger
+  // arrays get more CTAs).
+  const int64_t w_max = int64_t(48 * 1024 / (2 * sizeof(T))) - 2 * kSteps;
+  int64_t w = cdiv(n - 2, sm_count());
+  if (w < 32) w = 32;
+  if (w > w_max) w = w_max;
+  const int64_t blocks = cdiv(n - 2, w);
+  if (blocks > 0x7fffffff) return set_error(NPBGB_ERR_ARG, "jacobi1d: extent too large");
+  const size_t smem = 2 * size_t(w + 2 * kSteps) * sizeof(T);
+  int64_t left = 2 * int64_t(tsteps - 1);  // half-sweeps, even
+  cudaError_t e = cudaSuccess;
+  while (left > 0 && e == cudaSuccess) {
+    const int s = int(left < kSteps ? left : kSteps);
+    e = launch_chained(jacobi1d_block<T>, dim3{unsigned(blocks)}, dim3{unsigned(kThreads)}, smem,
+                       st, a, b, n, s, int(w));
+    left -= s;
+  }
+  return cuda_status(e, "jacobi1d_block");
 }
 
 }  // namespace
