@@ -1,0 +1,110 @@
+// Exact IEEE binary64 addition (round to nearest, ties to even) on the
+// integer pipes, for operands in a safe range.
+//
+// GB300's binary64 pipe retires about 1.6 operations per SM per clock while
+// its integer pipes retire tens of 32-bit operations, so an addition built
+// from integer instructions can run next to the hardware one and add to the
+// binary64 throughput of a kernel.  Unlike the fixed-point helpers (fx64.cuh)
+// this works for operands of any magnitude within the range below:
+//
+//   dadd_ok(a, b): both a and b finite, normal and with biased exponent in
+//                  [64, 1983] (|x| between about 2^-959 and 2^960);
+//   dadd_int(a, b) then returns exactly fl(a + b): +0 for an exact zero sum,
+//                  otherwise a normal double (the exponent range keeps the
+//                  result away from subnormals and overflow).
+//
+// Method (the textbook one): order the operands by magnitude, give both
+// significands 9 guard bits (leading bit at bit 61), shift the smaller right
+// by the exponent difference keeping a sticky bit, add or subtract, put the
+// leading bit back at 61 (right by one with sticky after a carry, left after
+// cancellation, which is exact), and round the 9 low bits to nearest even.
+// With 9 guard bits and a sticky bit the rounding is exact in every case
+// (at most one bit of cancellation can follow a lossy alignment).
+//
+// Host and device: the header compiles for both, so the host build is
+// checked against the CPU's IEEE addition.
+#pragma once
+
+#include <cstdint>
+
+#include "fx64.cuh"
+
+namespace npbgb {
+namespace f64emu {
+
+// Leading zeros of a 64-bit value from two 32-bit counts.
+NPBGB_FX_FN int clz64_32(uint64_t v) {
+  const int hi = fx::clz32(static_cast<uint32_t>(v >> 32));
+  return hi < 32 ? hi : 32 + fx::clz32(static_cast<uint32_t>(v));
+}
+
+NPBGB_FX_FN bool dadd_ok(uint64_t a, uint64_t b) {
+  const uint32_t ea = static_cast<uint32_t>(a >> 52) & 0x7ffu;
+  const uint32_t eb = static_cast<uint32_t>(b >> 52) & 0x7ffu;
+  return (ea - 64u) < 1920u && (eb - 64u) < 1920u;
+}
+
+// dadd_ok, or either operand a signed zero with the other in range or zero too
+// (dadd_z handles those).
+NPBGB_FX_FN bool dadd_z_ok(uint64_t a, uint64_t b) {
+  constexpr uint64_t kAbs = 0x7fffffffffffffffull;
+  const uint32_t ea = static_cast<uint32_t>(a >> 52) & 0x7ffu;
+  const uint32_t eb = static_cast<uint32_t>(b >> 52) & 0x7ffu;
+  const bool za = (a & kAbs) == 0, zb = (b & kAbs) == 0;
+  return (za || (ea - 64u) < 1920u) && (zb || (eb - 64u) < 1920u);
+}
+
+NPBGB_FX_FN uint64_t dadd_int(uint64_t a, uint64_t b) {
+  constexpr uint64_t kAbs = 0x7fffffffffffffffull, kMant = (1ull << 52) - 1;
+  const bool swap = (b & kAbs) > (a & kAbs);
+  const uint64_t x = swap ? b : a, y = swap ? a : b;  // |x| >= |y|
+  const uint32_t ex = static_cast<uint32_t>(x >> 52) & 0x7ffu;
+  const uint32_t ey = static_cast<uint32_t>(y >> 52) & 0x7ffu;
+  const uint64_t mx = ((x & kMant) | (1ull << 52)) << 9;  // leading bit at 61
+  const uint64_t my = ((y & kMant) | (1ull << 52)) << 9;
+  uint32_t d = ex - ey;
+  d = d < 63u ? d : 63u;
+  const uint64_t lost = my & ((1ull << d) - 1);
+  const uint64_t ya = (my >> d) | (lost != 0 ? 1ull : 0ull);
+  const bool sub = ((x ^ y) >> 63) != 0;
+  const uint64_t s = sub ? mx - ya : mx + ya;
+  if (s == 0) return 0;  // x + (-x) = +0 in round to nearest
+  const int lz = clz64_32(s);  // 1 (carry), 2 (aligned) or more (cancellation)
+  uint64_t n;
+  int e = int(ex);
+  if (lz == 1) {
+    n = (s >> 1) | (s & 1ull);
+    e += 1;
+  } else {
+    n = s << (lz - 2);
+    e -= lz - 2;
+  }
+  // n: leading bit 61, mantissa bits 61..9, round bit 8, sticky bits 7..0.
+  const uint64_t rest = n & 0x1ffull, lsb = (n >> 9) & 1ull;
+  const uint64_t up = (rest > 0x100ull || (rest == 0x100ull && lsb)) ? 1ull : 0ull;
+  const uint64_t m = (n >> 9) + up;  // in [2^52, 2^53]; 2^53 carries into the exponent
+  return (x & 0x8000000000000000ull) + ((static_cast<uint64_t>(e - 1) << 52) + m);
+}
+
+}  // namespace f64emu
+}  // namespace npbgb
+
+namespace npbgb {
+namespace f64emu {
+
+// fl(a + b) for dadd_z_ok operands: zeros follow IEEE round-to-nearest
+// (x + 0 = x for x != 0; +0 + -0 = +0; -0 + -0 = -0).
+NPBGB_FX_FN uint64_t dadd_z(uint64_t a, uint64_t b) {
+  constexpr uint64_t kAbs = 0x7fffffffffffffffull;
+  const bool za = (a & kAbs) == 0, zb = (b & kAbs) == 0;
+  if (za || zb) return za ? (zb ? (a & b) : b) : a;
+  return dadd_int(a, b);
+}
+
+// fl(a - b) = fl(a + (-b)) (IEEE defines subtraction so), same operand rules.
+NPBGB_FX_FN uint64_t dsub_z(uint64_t a, uint64_t b) {
+  return dadd_z(a, b ^ 0x8000000000000000ull);
+}
+
+}  // namespace f64emu
+}  // namespace npbgb
