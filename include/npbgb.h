@@ -71,6 +71,16 @@ extern "C" {
 #define NPBGB_CFG_BATCH_MODE 11       /* form of a batch, read when it is planned:
                                          0 (default) automatic by size, 1 persistent,
                                          2 stepped (NPBGB_BATCH_*) */
+#define NPBGB_CFG_HDIFF_EMU 12        /* hdiff: which Laplacian and flux items run on the
+                                         integer pipes (exact binary64 addition in
+                                         integer arithmetic) next to the hardware
+                                         binary64 ones.  Bit t of the low byte: the
+                                         Laplacian items i of a warp with i % 8 == t;
+                                         bits 8..15 the same for the flux items,
+                                         bits 16..23 for the output points.
+                                         -1 (default) = the library's choice; 0 =
+                                         hardware binary64 only.  Results are
+                                         identical for every mask. */
 
 /* Batch forms. */
 #define NPBGB_BATCH_PERSISTENT 1

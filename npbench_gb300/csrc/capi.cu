@@ -22,6 +22,7 @@ int64_t g_cfg_batch_ctas_per_sm = 3;
 int64_t g_cfg_jacobi_chunk = 0;
 int64_t g_cfg_pdl = 1;
 int64_t g_cfg_batch_mode = 0;
+int64_t g_cfg_hdiff_emu = -1;  // -1: default mask
 
 uint32_t take_heat_device_error();
 uint32_t take_batch_device_error();
@@ -145,6 +146,10 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "batch mode: 0, 1 or 2");
       g_cfg_batch_mode = value;
       return NPBGB_OK;
+    case NPBGB_CFG_HDIFF_EMU:
+      if (value < -1 || value > 0xffffff) return set_error(NPBGB_ERR_ARG, "hdiff emu: -1 .. 0xffffff");
+      g_cfg_hdiff_emu = value;
+      return NPBGB_OK;
     default:
       return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
   }
@@ -165,6 +170,7 @@ int32_t npbgb_get_config(int32_t key, int64_t* value) {
     case NPBGB_CFG_BATCH_CTAS_PER_SM: *value = g_cfg_batch_ctas_per_sm; return NPBGB_OK;
     case NPBGB_CFG_PDL: *value = g_cfg_pdl; return NPBGB_OK;
     case NPBGB_CFG_BATCH_MODE: *value = g_cfg_batch_mode; return NPBGB_OK;
+    case NPBGB_CFG_HDIFF_EMU: *value = g_cfg_hdiff_emu; return NPBGB_OK;
     default: return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
   }
 }

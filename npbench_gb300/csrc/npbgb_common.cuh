@@ -101,6 +101,7 @@ __device__ __forceinline__ void pdl_begin() {
 }
 
 extern int64_t g_cfg_pdl;  // NPBGB_CFG_PDL
+extern int64_t g_cfg_hdiff_emu;  // NPBGB_CFG_HDIFF_EMU
 
 template <typename... KArgs, typename... Args>
 cudaError_t launch_chained(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
