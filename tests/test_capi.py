@@ -77,6 +77,12 @@ def test_argument_errors_are_status_codes_not_crashes():
     assert lib.npbgb_vadv_workspace_bytes(256, 256, 160) == 8 * 159 * 256 * 256
     assert lib.npbgb_vadv_workspace_bytes(4, 4, 1) == 0
     assert lib.npbgb_set_config(_lib.NPBGB_CFG_PDL, 2) == _lib.NPBGB_ERR_ARG
+    assert lib.npbgb_set_config(_lib.NPBGB_CFG_HDIFF_EMU, 1 << 24) == _lib.NPBGB_ERR_ARG
+    assert lib.npbgb_set_config(_lib.NPBGB_CFG_HDIFF_EMU, -2) == _lib.NPBGB_ERR_ARG
+    old = _lib.get_config(_lib.NPBGB_CFG_HDIFF_EMU)
+    assert old == -1  # the library's default mask
+    assert _lib.set_config(_lib.NPBGB_CFG_HDIFF_EMU, 0xabcdef) == -1
+    assert _lib.set_config(_lib.NPBGB_CFG_HDIFF_EMU, old) == 0xabcdef
 
 
 def test_noop_sizes_return_ok_without_touching_memory():

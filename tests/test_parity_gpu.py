@@ -23,7 +23,7 @@ torch = pytest.importorskip("torch")
 if not torch.cuda.is_available():
     pytest.skip("no CUDA device", allow_module_level=True)
 
-from npbench_gb300 import stencils, workloads  # noqa: E402
+from npbench_gb300 import _lib, stencils, workloads  # noqa: E402
 from oracle import cref  # noqa: E402
 
 DEV = torch.device("cuda", 0)
@@ -442,6 +442,52 @@ def test_hdiff_ragged_shapes(IJK):
     stencils.hdiff(_dev(inf), d, _dev(coeff))
     cref.hdiff(inf, out, coeff)
     assert bits_equal(_host(d), out), (IJK, first_diff(_host(d), out))
+
+
+def _wide_range(shape, rng):
+    """Doubles across the whole binary64 range: random exponents from the
+    subnormals to 2^1023, random signs, signed zeros, repeated neighbours (exact
+    zero differences) and a few infinities."""
+    m = rng.random(shape) + 1.0
+    e = rng.integers(-1074, 1024, size=shape)
+    v = np.ldexp(m, e) * rng.choice([-1.0, 1.0], size=shape)
+    v[rng.random(shape) < 0.08] = 0.0
+    v[rng.random(shape) < 0.04] = -0.0
+    rep = rng.random(shape) < 0.15
+    v[1:][rep[1:]] = v[:-1][rep[1:]]
+    v[rng.random(shape) < 0.005] = np.inf
+    near = rng.random(shape) < 0.3  # keep many values where the integer path runs
+    v[near] = np.ldexp(rng.random(shape) + 0.5, rng.integers(-8, 8, size=shape))[near]
+    return v
+
+
+@pytest.mark.parametrize("mask", [0x000000, 0x00ff00, 0xffffff, 0x55aa55, 0x0f0f0f])
+def test_hdiff_integer_pipe_masks_bit_exact(golden, mask):
+    """Every NPBGB_CFG_HDIFF_EMU mask (which items use the integer-pipe binary64
+    addition) leaves the oracle's bits, on the golden cases (special values
+    included) and on inputs spanning the binary64 range."""
+    manifest, arrays = golden
+    old = _lib.set_config(_lib.NPBGB_CFG_HDIFF_EMU, mask)
+    try:
+        for c in manifest["cases"]:
+            if c["bench"] != "hdiff" or "init" in c:
+                continue
+            name = c["name"]
+            out = _dev(arrays[f"{name}/out_in"])
+            stencils.hdiff(_dev(arrays[f"{name}/in"]), out, _dev(arrays[f"{name}/coeff"]))
+            assert bits_equal(_host(out), arrays[f"{name}/out"]), (hex(mask), name)
+        rng = np.random.default_rng(mask + 7)
+        for IJK in [(9, 10, 40), (17, 33, 64)]:
+            I, J, K = IJK
+            inf = _wide_range((I + 4, J + 4, K), rng)
+            coeff = _wide_range((I, J, K), rng)
+            out = np.zeros((I, J, K))
+            d = _dev(out)
+            stencils.hdiff(_dev(inf), d, _dev(coeff))
+            cref.hdiff(inf, out, coeff)
+            assert bits_equal(_host(d), out), (hex(mask), IJK, first_diff(_host(d), out))
+    finally:
+        _lib.set_config(_lib.NPBGB_CFG_HDIFF_EMU, old)
 
 
 def test_host_numpy_arrays_are_updated_in_place(golden):
