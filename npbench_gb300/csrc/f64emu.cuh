@@ -108,3 +108,40 @@ NPBGB_FX_FN uint64_t dsub_z(uint64_t a, uint64_t b) {
 
 }  // namespace f64emu
 }  // namespace npbgb
+
+#if defined(__CUDACC__)
+// Device forms on raw bit patterns, for kernels that keep emulated values in
+// integer registers.  Operands outside the emulation's range take the hardware
+// instruction, out of line (so it is not predicated into the common path);
+// every form returns the IEEE round-to-nearest result.
+namespace npbgb {
+namespace f64emu {
+
+constexpr uint64_t kSignBit = 0x8000000000000000ull;
+
+__device__ __forceinline__ uint64_t u64(double v) { return static_cast<uint64_t>(__double_as_longlong(v)); }
+__device__ __forceinline__ double f64(uint64_t b) { return __longlong_as_double(static_cast<long long>(b)); }
+
+static __device__ __noinline__ uint64_t add_bits_hw(uint64_t a, uint64_t b) {
+  return u64(__dadd_rn(f64(a), f64(b)));
+}
+// fl(a + b)
+__device__ __forceinline__ uint64_t add_bits(uint64_t a, uint64_t b) {
+  return dadd_z_ok(a, b) ? dadd_z(a, b) : add_bits_hw(a, b);
+}
+// fl(a - b)
+__device__ __forceinline__ uint64_t sub_bits(uint64_t a, uint64_t b) { return add_bits(a, b ^ kSignBit); }
+
+static __device__ __noinline__ uint64_t half_bits_hw(uint64_t d) { return u64(__dmul_rn(0.5, f64(d))); }
+// fl(0.5 * d): an exponent decrement for normal d whose half is normal, d itself
+// for signed zeros, the hardware product otherwise.
+__device__ __forceinline__ uint64_t half_bits(uint64_t d) {
+  const uint32_t e = static_cast<uint32_t>(d >> 52) & 0x7ffu;
+  if (e - 2u < 2045u) return d - (1ull << 52);
+  if ((d << 1) == 0) return d;
+  return half_bits_hw(d);
+}
+
+}  // namespace f64emu
+}  // namespace npbgb
+#endif

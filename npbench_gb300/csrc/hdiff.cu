@@ -83,24 +83,19 @@ __device__ __forceinline__ double limit(double res, double hi, double lo) {
 }
 
 // ---------------------------------------------------------------------------
-// Integer-pipe forms.  Every other Laplacian and flux item of a warp is
+// Integer-pipe forms.  Items of the Laplacian, flux and output stages can be
 // evaluated with the exact integer emulation of binary64 addition
 // (f64emu.cuh) on the raw bit patterns, so that the integer pipes take part of
-// the additions while the binary64 pipe does the rest.  Each emulated
-// operation checks its operands and takes the hardware operation (out of
-// line) for anything outside the emulation's range (subnormals, infinities,
+// the additions while the binary64 pipe does the rest; NPBGB_CFG_HDIFF_EMU
+// picks the items (default: every flux item, measured best on GB300).  Each
+// emulated operation checks its operands and takes the hardware operation (out
+// of line) for anything outside the emulation's range (subnormals, infinities,
 // NaN, magnitudes beyond about 2^+-960); results are the IEEE ones either way.
-constexpr uint64_t kSign = 0x8000000000000000ull;
 constexpr uint32_t kDefaultEmu = 0xff00;  // every flux item
-
-__device__ __forceinline__ uint64_t u64(double v) { return static_cast<uint64_t>(__double_as_longlong(v)); }
-__device__ __forceinline__ double f64(uint64_t b) { return __longlong_as_double(static_cast<long long>(b)); }
-
-__device__ __noinline__ uint64_t add_bits_hw(uint64_t a, uint64_t b) { return u64(add_rn(f64(a), f64(b))); }
-__device__ __forceinline__ uint64_t add_bits(uint64_t a, uint64_t b) {
-  return f64emu::dadd_z_ok(a, b) ? f64emu::dadd_z(a, b) : add_bits_hw(a, b);
-}
-__device__ __forceinline__ uint64_t sub_bits(uint64_t a, uint64_t b) { return add_bits(a, b ^ kSign); }
+using f64emu::add_bits;
+using f64emu::f64;
+using f64emu::sub_bits;
+using f64emu::u64;
 
 // fl(fl(4*c) - s) from bits: 4*c is an exponent increment when c is normal and
 // the result stays in the emulation's range; other c take the literal form.
