@@ -189,35 +189,35 @@ heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ sr
           if (j0 + row + 1 < n1 - 1) dst[g + s1] = f2y(o);
         }
       }
-      continue;
-    }
+    } else {
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int row = row0 + r;
-      if (!k_ok || j0 + row >= n1 - 1) continue;
-      const int off = (row + 1) * G::BX + (tx + 1);
-      const int64_t g = gbase + r * s1;
-      const T* q = src + g;
-      T out;
-      if constexpr (FX) {
-        const bool hw = row >= G::TJ - hw_rows;  // warp-uniform
-        if (hw) {
-          out = heat_point<T>(q[0], q[s0], q[-s0], q[s1], q[-s1], q[1], q[-1]);
-        } else {
-          const int64_t c = col[r + 1], ip = pp[off], im = pm[off], jp = col[r + 2], jm = col[r],
-                        kp = pc[off + 1], km = pc[off - 1];
-          const uint32_t tag =
-              hi32(c) | hi32(ip) | hi32(im) | hi32(jp) | hi32(jm) | hi32(kp) | hi32(km);
-          if (!(tag & kPoisonHi))
-            out = heat_point_fxm<CVT, false>(c, ip, im, jp, jm, kp, km, one);
-          else
+      for (int r = 0; r < R; ++r) {
+        const int row = row0 + r;
+        if (!k_ok || j0 + row >= n1 - 1) continue;
+        const int off = (row + 1) * G::BX + (tx + 1);
+        const int64_t g = gbase + r * s1;
+        const T* q = src + g;
+        T out;
+        if constexpr (FX) {
+          const bool hw = row >= G::TJ - hw_rows;  // warp-uniform
+          if (hw) {
             out = heat_point<T>(q[0], q[s0], q[-s0], q[s1], q[-s1], q[1], q[-1]);
+          } else {
+            const int64_t c = col[r + 1], ip = pp[off], im = pm[off], jp = col[r + 2], jm = col[r],
+                          kp = pc[off + 1], km = pc[off - 1];
+            const uint32_t tag =
+                hi32(c) | hi32(ip) | hi32(im) | hi32(jp) | hi32(jm) | hi32(kp) | hi32(km);
+            if (!(tag & kPoisonHi))
+              out = heat_point_fxm<CVT, false>(c, ip, im, jp, jm, kp, km, one);
+            else
+              out = heat_point<T>(q[0], q[s0], q[-s0], q[s1], q[-s1], q[1], q[-1]);
+          }
+        } else {
+          out = heat_point<T>(col[r + 1], pp[off], pm[off], col[r + 2], col[r], pc[off + 1],
+                              pc[off - 1]);
         }
-      } else {
-        out = heat_point<T>(col[r + 1], pp[off], pm[off], col[r + 2], col[r], pc[off + 1],
-                            pc[off - 1]);
+        dst[g] = out;
       }
-      dst[g] = out;
     }
   }
 }

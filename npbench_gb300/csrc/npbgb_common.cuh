@@ -61,16 +61,8 @@ __device__ __forceinline__ F2 f2(float a, float b) {
   asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
   return r;
 }
-__device__ __forceinline__ float f2x(F2 a) {
-  float x, y;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a.v));
-  return x;
-}
-__device__ __forceinline__ float f2y(F2 a) {
-  float x, y;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a.v));
-  return y;
-}
+__device__ __forceinline__ float f2x(F2 a) { return __uint_as_float(static_cast<uint32_t>(a.v)); }
+__device__ __forceinline__ float f2y(F2 a) { return __uint_as_float(static_cast<uint32_t>(a.v >> 32)); }
 __device__ __forceinline__ F2 add2(F2 a, F2 b) {
   F2 r;
   asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
