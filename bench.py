@@ -48,6 +48,13 @@ HALF_SWEEPS = 2 * (TSTEPS - 1)
 INTERIOR = (N_GRID - 2) ** 3
 UPDATES_PER_STEP = HALF_SWEEPS * INTERIOR
 FALLBACK_HBM_GBS = 6800.0
+# Rate of GB300's binary64 pipe for DADD / DMUL, measured with a probe kernel of
+# independent dependent chains on this hardware (ops/s, whole GPU).
+FP64_PIPE_OPS = 5.0e11
+# Separately rounded binary64 operations per Heat-3D update as the reference
+# writes it: 2*c once, then per axis a subtraction, an addition and the product
+# by 0.125, and three additions joining the axes.
+HEAT_FP64_OPS = 13
 
 
 def parse():
@@ -266,6 +273,13 @@ def run_gb300(args, world, rank, local):
                 "traffic": ncu_traffic("heat3d_f64_256"),
                 "kernel": "heat3d half-sweep float64", "alg_bytes_per_launch": alg_bytes,
                 "launch_ms": launch_ms}
+    # The binary64 arithmetic bound: the reference's operations per update at the
+    # achieved rate, against what the binary64 pipe alone retires.  Above 1 because
+    # most additions run exactly in fixed point on the integer pipes.
+    fp64_equiv = HEAT_FP64_OPS * INTERIOR / (launch_ms * 1e-3)
+    fp64_roof = {"ops_per_update": HEAT_FP64_OPS, "achieved_ops_per_s": fp64_equiv,
+                 "fp64_pipe_ops_per_s": FP64_PIPE_OPS, "frac": fp64_equiv / FP64_PIPE_OPS,
+                 "peak_kind": "probe of DADD/DMUL throughput on GB300"}
 
     # End to end through the public call with host buffers.
     hA = torch.from_numpy(A0).pin_memory()
@@ -325,6 +339,7 @@ def run_gb300(args, world, rank, local):
                        "l2": "inputs larger than L2 (2 x 128 MiB), no flush",
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": roofline,
+            "fp64_roofline": fp64_roof,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * A64.nbytes,
                     "d2h_bytes_per_step": 2 * A64.nbytes},
             "gpu_launches": HALF_SWEEPS * args.steps,
