@@ -8,7 +8,9 @@
   through the plugin, validates it against the harness's own NumPy run
   (test.py:103-126), reports SUCCESS and writes its timings into the
   harness's ``npbench.db`` (test.py:133-163); ``run_benchmark.py`` does the
-  same end to end, line counts included (run_benchmark.py:1-59).  It uses the NPBench tree that
+  same end to end, line counts included (run_benchmark.py:1-59), and next to NumPy's rows
+  ``npbench_gb300.report`` turns the database into plot_results.py's speed-up table and
+  heat map.  It uses the NPBench tree that
   ``__graft_entry__.build()`` installs into baseline/_ref/npbench, and is
   skipped where that tree was never built.
 """
@@ -148,3 +150,18 @@ def test_run_benchmark_writes_results_db(tmp_path):
     with sqlite3.connect(os.path.join(tree, "npbench.db")) as con:
         lc = con.execute("SELECT framework, count FROM lcounts").fetchall()
     assert any(fw == "gb300" and n > 0 for fw, n in lc), lc
+    # NumPy's own rows next to ours, then the speed-up report over the database
+    # (the table of plot_results.py, without pandas/matplotlib).
+    r = subprocess.run([sys.executable, "run_benchmark.py", "-b", "heat_3d", "-f", "numpy", "-p",
+                        "S", "-r", "3"], cwd=tree, env=env, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    from npbench_gb300 import report
+    table = report.speedup_table(report.load_results(os.path.join(tree, "npbench.db")), "S")
+    assert table["frameworks"] == ["gb300", "numpy"], table["frameworks"]
+    (bd,) = table["benchmarks"]
+    assert 0 < table["ratio"][bd]["gb300"] < 1, table["ratio"]  # faster than NumPy
+    svg = os.path.join(tree, "heatmap.svg")
+    report.main(["--db", os.path.join(tree, "npbench.db"), "-p", "S", "--svg", svg])
+    import xml.etree.ElementTree as ET
+    assert ET.parse(svg).getroot().tag.endswith("svg")
