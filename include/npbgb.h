@@ -82,6 +82,13 @@ extern "C" {
                                          -1 (default) = the library's choice; 0 =
                                          hardware binary64 only.  Results are
                                          identical for every mask. */
+#define NPBGB_CFG_JACOBI1D_CTAS 14    /* jacobi1d: segments (CTAs) per SM; 0 (default)
+                                         = the library's choice.  Reading returns
+                                         the value in effect. */
+#define NPBGB_CFG_JACOBI1D_DEPTH 15   /* jacobi1d: half-sweeps per launch, which is
+                                         also the halo width; an even number up to
+                                         64, 0 (default) = the library's choice.
+                                         Reading returns the value in effect. */
 
 /* Batch forms. */
 #define NPBGB_BATCH_PERSISTENT 1

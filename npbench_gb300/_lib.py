@@ -31,6 +31,8 @@ NPBGB_CFG_BATCH_CTAS_PER_SM = 9
 NPBGB_CFG_PDL = 10
 NPBGB_CFG_BATCH_MODE = 11
 NPBGB_CFG_HDIFF_EMU = 12
+NPBGB_CFG_JACOBI1D_CTAS = 14
+NPBGB_CFG_JACOBI1D_DEPTH = 15
 NPBGB_BATCH_PERSISTENT = 1
 NPBGB_BATCH_STEPPED = 2
 

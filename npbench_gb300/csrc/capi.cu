@@ -23,6 +23,10 @@ int64_t g_cfg_jacobi_chunk = 0;
 int64_t g_cfg_pdl = 1;
 int64_t g_cfg_batch_mode = 0;
 int64_t g_cfg_hdiff_emu = -1;  // -1: default mask
+int64_t g_cfg_jacobi1d_ctas = 0;   // 0: default
+int64_t g_cfg_jacobi1d_depth = 0;  // 0: default
+int64_t jacobi1d_effective_depth();  // jacobi1d.cu
+int64_t jacobi1d_effective_ctas();
 
 uint32_t take_heat_device_error();
 uint32_t take_batch_device_error();
@@ -150,6 +154,15 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       if (value < -1 || value > 0xffffff) return set_error(NPBGB_ERR_ARG, "hdiff emu: -1 .. 0xffffff");
       g_cfg_hdiff_emu = value;
       return NPBGB_OK;
+    case NPBGB_CFG_JACOBI1D_CTAS:
+      if (value < 0 || value > 8) return set_error(NPBGB_ERR_ARG, "jacobi1d CTAs per SM: 0 .. 8");
+      g_cfg_jacobi1d_ctas = value;
+      return NPBGB_OK;
+    case NPBGB_CFG_JACOBI1D_DEPTH:
+      if (value < 0 || value > 64 || (value & 1))
+        return set_error(NPBGB_ERR_ARG, "jacobi1d depth: 0 or an even number up to 64");
+      g_cfg_jacobi1d_depth = value;
+      return NPBGB_OK;
     default:
       return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
   }
@@ -171,6 +184,8 @@ int32_t npbgb_get_config(int32_t key, int64_t* value) {
     case NPBGB_CFG_PDL: *value = g_cfg_pdl; return NPBGB_OK;
     case NPBGB_CFG_BATCH_MODE: *value = g_cfg_batch_mode; return NPBGB_OK;
     case NPBGB_CFG_HDIFF_EMU: *value = g_cfg_hdiff_emu; return NPBGB_OK;
+    case NPBGB_CFG_JACOBI1D_CTAS: *value = jacobi1d_effective_ctas(); return NPBGB_OK;
+    case NPBGB_CFG_JACOBI1D_DEPTH: *value = jacobi1d_effective_depth(); return NPBGB_OK;
     default: return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
   }
 }

@@ -95,9 +95,11 @@ __device__ __forceinline__ void pdl_begin() {
 extern int64_t g_cfg_pdl;  // NPBGB_CFG_PDL
 extern int64_t g_cfg_hdiff_emu;  // NPBGB_CFG_HDIFF_EMU
 
+// allow_pdl = false launches in plain stream order whatever NPBGB_CFG_PDL says
+// (for launch shapes where early residency of the next grid measured slower).
 template <typename... KArgs, typename... Args>
-cudaError_t launch_chained(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
-                           cudaStream_t st, Args&&... args) {
+cudaError_t launch_chained_if(bool allow_pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block,
+                              size_t smem, cudaStream_t st, Args&&... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
@@ -107,8 +109,14 @@ cudaError_t launch_chained(void (*kernel)(KArgs...), dim3 grid, dim3 block, size
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = g_cfg_pdl ? 1 : 0;
+  cfg.numAttrs = (allow_pdl && g_cfg_pdl) ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_chained(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                           cudaStream_t st, Args&&... args) {
+  return launch_chained_if(true, kernel, grid, block, smem, st, std::forward<Args>(args)...);
 }
 
 }  // namespace npbgb

@@ -19,6 +19,8 @@ cavity     cavity_flow 101x101, nt=20, nit=50, 2 calls    cavity_bands, -s 1
 batch      256 mixed Jacobi-2D grids, 2 launches          batch_persistent, -s 1
 batch_step 256 mixed grids, stepped form, one pass        batch_step, -s 20
 jacobi_f64_1000  Jacobi-2D 1000^2 float64, TSTEPS=3       jacobi2d_strip, -s 2
+jacobi1d   Jacobi-1D N=32000 float64, TSTEPS=64           jacobi1d_block, -s 2
+fdtd       FDTD-2D 1000x1200 float64, TMAX=3 (6 launches) fdtd_e / fdtd_h, -s 1
 ========== ============================================== ===================
 """
 import sys
@@ -60,6 +62,14 @@ def run(case):
         A, B = workloads.uniform_pair((1000, 1000), np.float64, seed=11)
         a, b = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
         stencils.jacobi_2d_kernel(3, a, b)
+    elif case == "jacobi1d":
+        A, B = workloads.init_jacobi_1d(32000, np.float64)
+        a, b = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+        stencils.jacobi_1d_kernel(64, a, b)
+    elif case == "fdtd":
+        fields = workloads.init_fdtd_2d(3, 1000, 1200)
+        ex, ey, hz, fict = (torch.from_numpy(t).to(dev) for t in fields)
+        stencils.fdtd_2d_kernel(3, ex, ey, hz, fict)
     elif case == "batch_step":
         from npbench_gb300.batch import Batch
         specs = workloads.batch_jacobi_specs(256, seed=0, tsteps=(10, 40))

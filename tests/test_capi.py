@@ -83,6 +83,9 @@ def test_argument_errors_are_status_codes_not_crashes():
     assert old == -1  # the library's default mask
     assert _lib.set_config(_lib.NPBGB_CFG_HDIFF_EMU, 0xabcdef) == -1
     assert _lib.set_config(_lib.NPBGB_CFG_HDIFF_EMU, old) == 0xabcdef
+    for key, bad in ((_lib.NPBGB_CFG_JACOBI1D_CTAS, 9), (_lib.NPBGB_CFG_JACOBI1D_DEPTH, 33),
+                     (_lib.NPBGB_CFG_JACOBI1D_DEPTH, 66), (_lib.NPBGB_CFG_JACOBI1D_CTAS, -1)):
+        assert lib.npbgb_set_config(key, bad) == _lib.NPBGB_ERR_ARG
 
 
 def test_noop_sizes_return_ok_without_touching_memory():

@@ -461,6 +461,25 @@ def _wide_range(shape, rng):
     return v
 
 
+@pytest.mark.parametrize("ctas,depth", [(1, 2), (1, 32), (2, 48), (4, 64), (8, 16)])
+def test_jacobi_1d_launch_shapes_bit_exact(ctas, depth):
+    """Every Jacobi-1D launch shape (segments per SM, half-sweeps per launch)
+    leaves the oracle's bits, also for sweep counts that are not a multiple of
+    the depth."""
+    old = (_lib.set_config(_lib.NPBGB_CFG_JACOBI1D_CTAS, ctas),
+           _lib.set_config(_lib.NPBGB_CFG_JACOBI1D_DEPTH, depth))
+    try:
+        for n, T in ((32000, 37), (5000, 50), (40, 9)):
+            A, B = workloads.init_jacobi_1d(n, np.float64)
+            dA, dB = _dev(A), _dev(B)
+            stencils.jacobi_1d_kernel(T, dA, dB)
+            cref.jacobi_1d_kernel(T, A, B)
+            assert bits_equal(_host(dA), A) and bits_equal(_host(dB), B), (ctas, depth, n, T)
+    finally:
+        _lib.set_config(_lib.NPBGB_CFG_JACOBI1D_CTAS, old[0])
+        _lib.set_config(_lib.NPBGB_CFG_JACOBI1D_DEPTH, old[1])
+
+
 @pytest.mark.parametrize("mask", [0x000000, 0x00ff00, 0xffffff, 0x55aa55, 0x0f0f0f])
 def test_hdiff_integer_pipe_masks_bit_exact(golden, mask):
     """Every NPBGB_CFG_HDIFF_EMU mask (which items use the integer-pipe binary64
