@@ -14,13 +14,18 @@ The two 128 MiB arrays exceed the 129 MB L2, so no L2 flush is needed.
                 -> host copies of A and B, all inside the timed interval;
 * ``roofline``  algorithmic bytes (16 B per float64 update: read one value,
                 write one) of one half-sweep launch over its measured duration;
+* ``fp64_roofline`` the reference's 13 binary64 operations per update at the
+                achieved rate against the binary64 pipe's measured rate;
 * ``fp32``      the same workload in float32 with its error against float64;
-* ``cpu_baseline`` the NumPy restatement of the reference kernel on a bounded
-                sample (16 half-sweeps of the same grid), one host core
+* ``cpu_baseline`` the reference's arithmetic on the host: the C restatement
+                (oracle/stencils.c, bit-identical to the reference's NumPy code)
+                with OpenMP on all host threads, the whole workload 10 times;
+                ``numpy_1core`` beside it times the NumPy restatement on one core
                 (NumPy's elementwise ufuncs are single-threaded).
 
-``--impl reference`` times only that CPU implementation (the reference's own
-arithmetic) on the host cores and prints its line with ``"impl": "reference"``.
+``--impl reference`` times only that CPU implementation (the C restatement on
+all host threads, one whole workload per step) and prints its line with
+``"impl": "reference"``.
 
 With N > 1 (torchrun), every rank runs an independent replica on its own GPU
 (the path has no exchange between independent grids): ``value`` is the total
@@ -181,29 +186,85 @@ def cpu_numpy_sample(dtype=np.float64, half_sweeps=2, seed=0):
     return half_sweeps * INTERIOR / dt, dt
 
 
+def host_threads():
+    """Threads the OpenMP loops of the C restatement use (OMP_NUM_THREADS, else all cores)."""
+    try:
+        return max(1, int(os.environ.get("OMP_NUM_THREADS", "")))
+    except ValueError:
+        return os.cpu_count() or 1
+
+
+def cpu_port(setup, run, units, what, parallel=True, reps=3, numpy=None):
+    """Times the C restatement of the reference's arithmetic (oracle/stencils.c,
+    bit-identical to the reference's NumPy code) on the host cores.
+
+    setup() returns fresh arguments (untimed), run(*args) is timed; the median
+    of ``reps`` runs gives ``units / s``.  ``parallel``: the C loops use OpenMP
+    on all host threads (False for the kernels whose C form is sequential).
+    ``numpy``: optional (setup, run, units, what) timed once with the NumPy
+    restatement, one core, reported beside it as ``numpy_1core``.
+    """
+    run(*setup())  # warm-up: builds the library and starts the thread pool
+    dts = []
+    for _ in range(reps):
+        a = setup()
+        t0 = time.perf_counter()
+        run(*a)
+        dts.append(time.perf_counter() - t0)
+    dt = statistics.median(dts)
+    cores = host_threads() if parallel else 1
+    out = {"value": units / dt, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"{what}: C restatement of the reference (OpenMP, {cores} of "
+                     f"{os.cpu_count()} host threads), median of {reps} runs, {dt:.2f} s each"}
+    if numpy is not None:
+        n_setup, n_run, n_units, n_what = numpy
+        a = n_setup()
+        t0 = time.perf_counter()
+        n_run(*a)
+        ndt = time.perf_counter() - t0
+        out["numpy_1core"] = {"value": n_units / ndt, "unit": UNIT, "cores": 1,
+                              "sample": f"{n_what}: NumPy restatement (single-threaded ufuncs), "
+                                        f"{ndt:.2f} s"}
+    return out
+
+
 def run_reference(args, world, rank):
+    """The reference's CPU path: heat_3d(TSTEPS=100) on the 256^3 float64 grid, each
+    step one whole workload through the C restatement of heat_3d_numpy.py (bit-identical
+    to it) on all host threads; NumPy's own single-threaded rate is reported beside it."""
     if rank != 0:
         return
-    ups = []
+    from npbench_gb300 import workloads
+    from oracle import cref
+    A0, B0 = workloads.uniform_heat((N_GRID,) * 3, np.float64, seed=0)
+    A, B = A0.copy(), B0.copy()
     for _ in range(max(0, args.warmup)):
-        cpu_numpy_sample()
+        np.copyto(A, A0)
+        np.copyto(B, B0)
+        cref.heat_3d_kernel(TSTEPS, A, B)
     t_total = 0.0
     for _ in range(args.steps):
-        v, dt = cpu_numpy_sample()
-        ups.append(v)
-        t_total += dt
-    value = 2 * INTERIOR * args.steps / t_total
-    sample = (f"2 half-sweeps of the 256^3 float64 heat grid per step "
-              f"(heat_3d_numpy.py arithmetic via its NumPy restatement)")
+        np.copyto(A, A0)
+        np.copyto(B, B0)
+        t0 = time.perf_counter()
+        cref.heat_3d_kernel(TSTEPS, A, B)
+        t_total += time.perf_counter() - t0
+    value = UPDATES_PER_STEP * args.steps / t_total
+    cores = host_threads()
+    v_np, dt_np = cpu_numpy_sample(half_sweeps=2)
+    sample = (f"the whole workload (TSTEPS={TSTEPS}, {HALF_SWEEPS} half-sweeps) per step, C "
+              f"restatement of heat_3d_numpy.py (OpenMP, {cores} of {os.cpu_count()} host threads)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic U[0,1) from default_rng(0)",
-        "config": {"workload": "heat_3d 256^3 float64 (bounded sample: 2 half-sweeps per step)",
+        "config": {"workload": "heat_3d 256^3 float64, TSTEPS=100 (198 half-sweeps)",
                    "TSTEPS": TSTEPS, "grid": [N_GRID] * 3},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": sample},
+        "numpy_1core": {"value": v_np, "unit": UNIT, "cores": 1,
+                        "sample": f"2 half-sweeps through the NumPy restatement, {dt_np:.2f} s"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -321,11 +382,15 @@ def run_gb300(args, world, rank, local):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v, dt = cpu_numpy_sample(half_sweeps=50)
-        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"50 half-sweeps of the 256^3 float64 grid, NumPy restatement of "
-                         f"heat_3d_numpy.py, {dt:.1f} s; host has {os.cpu_count()} cores, "
-                         f"NumPy ufuncs use one"}
+        from oracle import cref, stencils_np
+        hA = A0.copy()
+        cpu = cpu_port(lambda: (hA.copy(), hA.copy()),
+                       lambda a, b: cref.heat_3d_kernel(TSTEPS, a, b), UPDATES_PER_STEP,
+                       f"the whole workload (TSTEPS={TSTEPS}) on the same 256^3 float64 grid",
+                       reps=10,
+                       numpy=(lambda: (hA.copy(), hA.copy()),
+                              lambda a, b: stencils_np.heat_3d_kernel(3, a, b), 4 * INTERIOR,
+                              "TSTEPS=3 (4 half-sweeps) on the same grid"))
 
     if rank == 0:
         line = {
@@ -410,13 +475,12 @@ def run_jacobi2d(args):
     ach = 16.0 * (n - 2) ** 2 / (ms_step / hs * 1e-3) / 1e9
     cpu = None
     if not args.no_cpu_baseline:
-        from oracle import stencils_np
-        a, b = A0.copy(), B0.copy()
-        t0 = time.perf_counter()
-        stencils_np.jacobi_2d_kernel(11, a, b)
-        dt = time.perf_counter() - t0
-        cpu = {"value": 20 * (n - 2) ** 2 / dt, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"TSTEPS=11 (20 half-sweeps) of the same grid, {dt:.2f} s"}
+        from oracle import cref, stencils_np
+        cpu = cpu_port(lambda: (A0.copy(), B0.copy()), lambda a, b: cref.jacobi_2d_kernel(T, a, b),
+                       ups, f"the whole workload (TSTEPS={T}) on the same grid", reps=5,
+                       numpy=(lambda: (A0.copy(), B0.copy()),
+                              lambda a, b: stencils_np.jacobi_2d_kernel(11, a, b),
+                              20 * (n - 2) ** 2, "TSTEPS=11 (20 half-sweeps)"))
     print(json.dumps(_base_line(
         args, ups * args.steps / (ms * 1e-3), ms_step, "f64",
         "jacobi_2d 1000^2 float64, TSTEPS=100 (198 half-sweeps)",
@@ -448,14 +512,11 @@ def run_hdiff(args):
     ach = alg / (ms_step * 1e-3) / 1e9
     cpu = None
     if not args.no_cpu_baseline:
-        from oracle import stencils_np
-        o = out0.copy()
-        t0 = time.perf_counter()
-        for _ in range(3):
-            stencils_np.hdiff(inf, o, coeff)
-        dt = (time.perf_counter() - t0) / 3
-        cpu = {"value": pts / dt, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"3 calls on the same 256x256x160 input, {dt:.2f} s each"}
+        from oracle import cref, stencils_np
+        cpu = cpu_port(lambda: (out0.copy(),), lambda o: cref.hdiff(inf, o, coeff), pts,
+                       "one call on the same 256x256x160 input", reps=5,
+                       numpy=(lambda: (out0.copy(),), lambda o: stencils_np.hdiff(inf, o, coeff),
+                              pts, "one call"))
     print(json.dumps(_base_line(
         args, pts * args.steps / (ms * 1e-3), ms_step, "f64",
         "hdiff 256x256x160 float64 (reference initialize), one call per step",
@@ -488,16 +549,12 @@ def run_jacobi1d(args):
     ups = 2 * (T - 1) * (n - 2)
     cpu = None
     if not args.no_cpu_baseline:
-        from oracle import stencils_np
-        dts = []
-        for _ in range(3):
-            a, b = A0.copy(), B0.copy()
-            t0 = time.perf_counter()
-            stencils_np.jacobi_1d_kernel(T, a, b)
-            dts.append(time.perf_counter() - t0)
-        dt = statistics.median(dts)
-        cpu = {"value": ups / dt, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"the whole workload (TSTEPS={T}) 3 times, median {dt:.2f} s"}
+        from oracle import cref, stencils_np
+        cpu = cpu_port(lambda: (A0.copy(), B0.copy()), lambda a, b: cref.jacobi_1d_kernel(T, a, b),
+                       ups, f"the whole workload (TSTEPS={T})", parallel=False,
+                       numpy=(lambda: (A0.copy(), B0.copy()),
+                              lambda a, b: stencils_np.jacobi_1d_kernel(T, a, b), ups,
+                              f"the whole workload (TSTEPS={T})"))
     peak, kind = measured_peaks()
     ach = 16.0 * ups / (ms / args.steps * 1e-3) / 1e9
     from npbench_gb300 import _lib
@@ -541,13 +598,11 @@ def run_vadv(args):
     ach = alg / (ms_step * 1e-3) / 1e9
     cpu = None
     if not args.no_cpu_baseline:
-        from oracle import stencils_np
-        o = us0.copy()
-        t0 = time.perf_counter()
-        stencils_np.vadv(o, u, w, up, ut, dtr)
-        dt = time.perf_counter() - t0
-        cpu = {"value": pts / dt, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"1 call on the same 256x256x160 input, {dt:.2f} s"}
+        from oracle import cref, stencils_np
+        cpu = cpu_port(lambda: (us0.copy(),), lambda o: cref.vadv(o, u, w, up, ut, dtr), pts,
+                       "one call on the same 256x256x160 input",
+                       numpy=(lambda: (us0.copy(),), lambda o: stencils_np.vadv(o, u, w, up, ut, dtr),
+                              pts, "one call"))
     print(json.dumps(_base_line(
         args, pts * args.steps / (ms * 1e-3), ms_step, "f64",
         "vadv 256x256x160 float64 (paper preset, reference initialize), one call per step",
@@ -590,13 +645,16 @@ def run_cavity(args):
     ach = alg / (ms_step * 1e-3) / 1e9
     cpu = None
     if not args.no_cpu_baseline:
-        from oracle import stencils_np
-        u, v, p = (x.copy() for x in (u0, v0, p0))
-        t0 = time.perf_counter()
-        stencils_np.cavity_flow(nx, ny, 20, nit, u, v, dt, dx, dy, p, rho, nu)
-        dt_cpu = time.perf_counter() - t0
-        cpu = {"value": 20 * (nit + 2) * (ny - 2) * (nx - 2) / dt_cpu, "unit": UNIT, "cores": 1,
-               "kind": "port", "sample": f"nt=20 of the same problem, {dt_cpu:.2f} s"}
+        from oracle import cref, stencils_np
+        fresh = lambda: tuple(x.copy() for x in (u0, v0, p0))  # noqa: E731
+        cpu = cpu_port(fresh,
+                       lambda u, v, p: cref.cavity_flow(nx, ny, nt, nit, u, v, dt, dx, dy, p, rho,
+                                                        nu),
+                       ups, f"the whole workload (nt={nt}, nit={nit})", parallel=False,
+                       numpy=(fresh,
+                              lambda u, v, p: stencils_np.cavity_flow(nx, ny, 20, nit, u, v, dt,
+                                                                      dx, dy, p, rho, nu),
+                              20 * (nit + 2) * (ny - 2) * (nx - 2), "nt=20 of the same problem"))
     print(json.dumps(_base_line(
         args, ups * args.steps / (ms * 1e-3), ms_step, "f64",
         "cavity_flow 101x101 float64, nt=700, nit=50 (paper preset, reference initialize), "
@@ -643,13 +701,15 @@ def run_channel(args):
     ach = alg / (ms_step * 1e-3) / 1e9
     cpu = None
     if not args.no_cpu_baseline:
-        from oracle import stencils_np
-        u, v, p = (x.copy() for x in (u0, v0, p0))
-        t0 = time.perf_counter()
-        ns = stencils_np.channel_flow(nit, u, v, dt, dx, dy, p, rho, nu, F)
-        dt_cpu = time.perf_counter() - t0
-        cpu = {"value": ns * (nit + 2) * (ny - 2) * nx / dt_cpu, "unit": UNIT, "cores": 1,
-               "kind": "port", "sample": f"the whole run ({ns} steps), {dt_cpu:.2f} s"}
+        from oracle import cref, stencils_np
+        fresh = lambda: tuple(x.copy() for x in (u0, v0, p0))  # noqa: E731
+        cpu = cpu_port(fresh,
+                       lambda u, v, p: cref.channel_flow(nit, u, v, dt, dx, dy, p, rho, nu, F),
+                       ups, f"the whole run ({nsteps} steps)", parallel=False,
+                       numpy=(fresh,
+                              lambda u, v, p: stencils_np.channel_flow(nit, u, v, dt, dx, dy, p,
+                                                                       rho, nu, F),
+                              ups, f"the whole run ({nsteps} steps)"))
     print(json.dumps(_base_line(
         args, ups * args.steps / (ms * 1e-3), ms_step, "f64",
         "channel_flow 101x101 float64, nit=50, to convergence (paper preset, reference "
@@ -687,13 +747,14 @@ def run_fdtd2d(args):
     cells = T * nx * ny  # cell-steps (each updates ex, ey and hz)
     cpu = None
     if not args.no_cpu_baseline:
-        from oracle import stencils_np
-        ex, ey, hz, fict = (x.copy() for x in host)
-        t0 = time.perf_counter()
-        stencils_np.fdtd_2d_kernel(20, ex, ey, hz, fict)
-        dt = time.perf_counter() - t0
-        cpu = {"value": 20 * nx * ny / dt, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"TMAX=20 on the same fields, {dt:.2f} s"}
+        from oracle import cref, stencils_np
+        fresh = lambda: tuple(x.copy() for x in host)  # noqa: E731
+        cpu = cpu_port(fresh, lambda ex, ey, hz, fict: cref.fdtd_2d_kernel(T, ex, ey, hz, fict),
+                       cells, f"the whole workload (TMAX={T})",
+                       numpy=(fresh,
+                              lambda ex, ey, hz, fict: stencils_np.fdtd_2d_kernel(20, ex, ey, hz,
+                                                                                  fict),
+                              20 * nx * ny, "TMAX=20 on the same fields"))
     peak, kind = measured_peaks()
     ach = 48.0 * cells / (ms / args.steps * 1e-3) / 1e9
     print(json.dumps(_base_line(
