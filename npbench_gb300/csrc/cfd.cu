@@ -140,9 +140,16 @@ __device__ bool wait_neighbours(const uint32_t* done, int b, int nb, uint32_t s)
 
 // bar.sync orders every thread's stores before thread 0's release, and a
 // release is cumulative (PTX memory model), so no separate fence is needed.
+// The counter counts sweeps, so publishing sweep s is an increment by one; a
+// release reduction measured 26% faster per neighbour hand-off on GB300 than a
+// release store of s (1.43 against 1.93 us in a chain of 99 bands).
+__device__ __forceinline__ void red_release_add(uint32_t* p, uint32_t v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 __device__ __forceinline__ void publish(uint32_t* done, int b, uint32_t s) {
+  (void)s;  // done[b] == s - 1 here: every band publishes its sweeps in order, once each
   __syncthreads();
-  if (threadIdx.x == 0) st_release(done + b, s);
+  if (threadIdx.x == 0) red_release_add(done + b, 1u);
 }
 
 // Points are addressed by their offset o and the offsets oe/ow of their east
