@@ -87,8 +87,8 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void red_release_add(uint32_t* p, uint32_t v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 // One half-sweep of band rows [r0, r1) from src to dst over all interior
@@ -183,11 +183,12 @@ batch_persistent(const BandDesc* __restrict__ bands, uint32_t* done, const int32
           band_half_sweep<float, false>(static_cast<const float*>(src), static_cast<float*>(dst),
                                         d.n1, d.r0, d.r1, hw_warps, one);
         }
+        // bar.sync orders the CTA's stores before thread 0's release, which is
+        // cumulative; the counter is written by this CTA only and goes s -> s+1,
+        // so a release reduction publishes it (measured faster per hand-off on
+        // GB300 than a fence plus release store).
         __syncthreads();
-        if (tid == 0) {
-          __threadfence();
-          st_release(done + idx, uint32_t(s + 1));
-        }
+        if (tid == 0) red_release_add(done + idx, 1u);
         progressed = true;
       }
     }
