@@ -191,7 +191,8 @@ def test_golden_cavity_flow_bit_exact(golden):
 
 
 @pytest.mark.parametrize("shape,nt,nit", [((101, 101), 700, 50), ((400, 37), 5, 7),
-                                          ((3, 300), 4, 3), ((161, 5), 6, 9)])
+                                          ((3, 300), 4, 3), ((161, 5), 6, 9), ((4, 50), 5, 6),
+                                          ((7, 2000), 3, 4), ((153, 11), 4, 5)])
 def test_cavity_flow_vs_oracle(shape, nt, nit):
     """The paper preset (one persistent launch for 700 steps of 50 pressure
     iterations) and band splits with several rows per band, from random fields."""
@@ -247,7 +248,8 @@ def test_golden_channel_flow_bit_exact(golden):
     assert n >= 10
 
 
-@pytest.mark.parametrize("shape,nit", [((101, 101), 50), ((400, 37), 3), ((161, 2), 4)])
+@pytest.mark.parametrize("shape,nit", [((101, 101), 50), ((400, 37), 3), ((161, 2), 4),
+                                       ((5, 64), 6), ((40, 9), 7)])
 def test_channel_flow_vs_oracle(shape, nit):
     """The paper preset (989 steps of 50 pressure iterations in one launch) and
     band splits with several rows per band, from the reference's initial state."""
