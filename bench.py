@@ -812,6 +812,31 @@ def run_batch(args):
         comp = {"per_grid_launches_updates_per_s": ups / (ms_pg * 1e-3),
                 "per_grid_ms": ms_pg, "batched_over_per_grid": ms_pg / ms_step,
                 "per_grid_kernel_launches": sum(2 * (T - 1) for _, _, T in specs)}
+    cpu = None
+    if not args.no_cpu_baseline:
+        # The first 64 grids of the same configuration, seeded host inputs: timed
+        # through the C restatement on all host threads, and run as a GPU batch
+        # that must match it bit for bit.
+        from oracle import cref
+        sample = specs[:64]
+        rng = np.random.default_rng(1)
+        host = [(rng.random(sh).astype(dt), rng.random(sh).astype(dt), T) for sh, dt, T in sample]
+        gpu = [(torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev), T) for a, b, T in host]
+        with Batch(gpu) as sb:
+            sb.launch()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for a, b, T in host:
+            cref.jacobi_2d_kernel(T, a, b)
+        dt_cpu = time.perf_counter() - t0
+        exact = all(np.array_equal(a.view(np.uint8), ga.cpu().numpy().view(np.uint8)) and
+                    np.array_equal(b.view(np.uint8), gb.cpu().numpy().view(np.uint8))
+                    for (a, b, _), (ga, gb, _) in zip(host, gpu))
+        ups_s = sum(2 * (T - 1) * (sh[0] - 2) * (sh[1] - 2) for sh, _, T in sample)
+        cpu = {"value": ups_s / dt_cpu, "unit": UNIT, "cores": host_threads(), "kind": "port",
+               "sample": f"the first {len(sample)} grids of the batch ({ups_s:.3g} updates), C "
+                         f"restatement on {host_threads()} host threads, {dt_cpu:.2f} s; the GPU "
+                         f"batch of the same grids {'matches it bit for bit' if exact else 'DIFFERS'}"}
     cells = sum(s[0] * s[1] for s, _, _ in specs)
     print(json.dumps(_base_line(
         args, ups * args.steps / (ms * 1e-3), ms_step, "f32+f64",
@@ -824,7 +849,8 @@ def run_batch(args):
                                                 "far above L2"},
         roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                   "frac": ach / peak, "peak_kind": kind, "traffic": None},
-        comparator=comp, gpu_launches=args.steps, clocks=clk.summary())), flush=True)
+        comparator=comp, gpu_launches=args.steps, clocks=clk.summary(),
+        cpu_baseline=cpu)), flush=True)
 
 
 def run_serve(args):
@@ -860,6 +886,26 @@ def run_serve(args):
         run_sequential(seq, arrivals)
         comp = latency_stats(seq)
         comp["served_over_sequential_updates_per_s"] = st["updates_per_s"] / comp["updates_per_s"]
+    cpu = None
+    if not args.no_cpu_baseline:
+        # The stream's requests in arrival order, up to about 2e10 updates,
+        # through the C restatement on all host threads.
+        from oracle import cref
+        rng = np.random.default_rng(2)
+        done_ups, t_cpu, n = 0, 0.0, 0
+        for shape, dt, T, _ in specs:
+            if done_ups > 2e10:
+                break
+            a = rng.random(shape).astype(dt)
+            b = a.copy() if len(shape) == 3 else rng.random(shape).astype(dt)
+            t0 = time.perf_counter()
+            (cref.jacobi_2d_kernel if len(shape) == 2 else cref.heat_3d_kernel)(T, a, b)
+            t_cpu += time.perf_counter() - t0
+            done_ups += 2 * (T - 1) * int(np.prod([x - 2 for x in shape]))
+            n += 1
+        cpu = {"value": done_ups / t_cpu, "unit": UNIT, "cores": host_threads(), "kind": "port",
+               "sample": f"the stream's first {n} requests ({done_ups:.3g} updates), C "
+                         f"restatement on {host_threads()} host threads, {t_cpu:.2f} s"}
     print(json.dumps(_base_line(
         args, st["updates_per_s"], st["span_s"] * 1e3, "f32+f64",
         f"served stream: {args.requests} requests, Poisson {args.rate:g} req/s, 2D Jacobi "
@@ -867,7 +913,7 @@ def run_serve(args):
         {"quantum_half_sweeps": args.quantum, "hbm_budget_gb": 150, "rounds": srv.rounds,
          "peak_resident_gb": srv.admission.peak / 1e9},
         latency={"p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"]},
-        comparator=comp, clocks=clk.summary())), flush=True)
+        comparator=comp, clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
 
 
 def main():
