@@ -30,7 +30,7 @@ constexpr int kUnroll = 4;
 // Grid: x over groups of kWarps column strips, y over chunks of rows.  With
 // FX, warps below hw_warps take the hardware binary64 path so that the
 // binary64 pipe works next to the integer pipe (same results either way).
-template <typename T, bool FX>
+template <typename T, bool FX, bool MAD>
 __global__ void __launch_bounds__(32 * kWarps)
 jacobi2d_strip(const T* __restrict__ src, T* __restrict__ dst, int64_t ny, int64_t nx, int chunk,
                int hw_warps, uint32_t one) {
@@ -45,7 +45,7 @@ jacobi2d_strip(const T* __restrict__ src, T* __restrict__ dst, int64_t ny, int64
   if (FX && warp < hw_warps)
     jcore::strip_rows<T, false, false, 1>(src, dst, nx, k0, ib, ie, one);
   else
-    jcore::strip_rows<T, FX, false, FX ? 1 : kUnroll>(src, dst, nx, k0, ib, ie, one);
+    jcore::strip_rows<T, FX, false, FX ? 1 : kUnroll, MAD>(src, dst, nx, k0, ib, ie, one);
 }
 
 int pick_chunk(int64_t ny, int64_t col_blocks) {
@@ -71,11 +71,13 @@ int32_t run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st)
   const dim3 grid{unsigned(gx), unsigned(gy)};
   const int hw = jacobi_hw_warps();
   const dim3 block{32u * kWarps};
+  // Fixed-point additions as multiply-adds below 2^21 cells (see Strip).
+  auto kern = (FX && ny * nx < (int64_t(1) << 21)) ? jacobi2d_strip<T, FX, true>
+                                                   : jacobi2d_strip<T, FX, false>;
   cudaError_t e = cudaSuccess;
   for (int32_t t = 1; t < tsteps && e == cudaSuccess; ++t) {
-    e = launch_chained(jacobi2d_strip<T, FX>, grid, block, 0, st, a, b, ny, nx, chunk, hw, 1u);
-    if (e == cudaSuccess)
-      e = launch_chained(jacobi2d_strip<T, FX>, grid, block, 0, st, b, a, ny, nx, chunk, hw, 1u);
+    e = launch_chained(kern, grid, block, 0, st, a, b, ny, nx, chunk, hw, 1u);
+    if (e == cudaSuccess) e = launch_chained(kern, grid, block, 0, st, b, a, ny, nx, chunk, hw, 1u);
   }
   return cuda_status(e, "jacobi2d_strip");
 }
