@@ -178,7 +178,7 @@ NPBGB_API int32_t npbgb_hdiff(const void* in_field, void* out_field, const void*
  *   kernel(TSTEPS, A, B)   polybench/jacobi_1d/jacobi_1d_numpy.py:4-8
  * A and B have n points; tsteps-1 times: dst[i] = 0.33333 * ((src[i-1] + src[i]) + src[i+1])
  * over [1, n-1), A -> B then B -> A.  Temporal blocking in shared memory: one
- * launch per 32 half-sweeps. */
+ * launch per NPBGB_CFG_JACOBI1D_DEPTH half-sweeps (48 by default). */
 NPBGB_API int32_t npbgb_jacobi1d(void* A, void* B, int64_t n, int32_t tsteps, int32_t dtype,
                                  void* stream);
 
