@@ -57,7 +57,7 @@ extern "C" {
                                      0 (default) = 4 for binary32, 2 for binary64 */
 #define NPBGB_CFG_HEAT_HW_ROWS 6  /* heat3d binary64: tile rows per CTA evaluated with
                                      hardware binary64 next to the fixed-point rows;
-                                     -1 (default) = 5 of 16 with 2 rows per thread,
+                                     -1 (default) = 7 of 16 with 2 rows per thread,
                                      3 of 8 with 1, 8 of 32 with 4 */
 #define NPBGB_CFG_F64_CVT 7       /* 1: fixed-point conversions use the binary64
                                      convert instructions; 0: integer bit operations */

@@ -55,7 +55,8 @@ def _space(bench, dtype):
     elif bench == "heat_3d":
         for rows in (1, 2, 4):
             tj = 8 * rows
-            for hw in (sorted({0, tj // 8, tj // 4, 5 * tj // 16, 3 * tj // 8}) if f64 else (-1,)):
+            for hw in (sorted({0, tj // 8, tj // 4, 5 * tj // 16, 3 * tj // 8, 7 * tj // 16})
+                       if f64 else (-1,)):
                 for ch in (0, 4, 8, 16, 32):
                     out.append({"HEAT_ROWS": rows, "HEAT_HW_ROWS": hw, "HEAT_CHUNK": ch})
     else:

@@ -306,11 +306,12 @@ int32_t launch_tma(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tstep
   if (gy > 65535 || gz > 65535 || gx > 0x7fffffff)
     return set_error(NPBGB_ERR_ARG, "heat3d: extent too large");
   const dim3 grid{unsigned(gx), unsigned(gy), unsigned(gz)};
-  // Tile rows on the hardware binary64 pipe, measured best at 256^3: 5 of 16
-  // with 2 rows per warp (31.4 ms per 198 half-sweeps against 33.5 with 4 and
-  // 33.0 with 6; the warp holding rows 10 and 11 mixes both pipes), 3 of 8
-  // with 1 row per warp, 8 of 32 with 4.
-  const int hw_default = R == 2 ? 5 : (R == 1 ? 3 : G::TJ / 4);
+  // Tile rows on the hardware binary64 pipe, measured best at 256^3: 7 of 16
+  // with 2 rows per warp once the hardware rows' exact products by 2 and
+  // 0.125 moved to the integer pipe (30.7 ms per 198 half-sweeps against 31.4
+  // with 6 or 8, and 31.4 for 5 rows with binary64 products); 3 of 8 with 1
+  // row per warp, 8 of 32 with 4.
+  const int hw_default = R == 2 ? 7 : (R == 1 ? 3 : G::TJ / 4);
   int hw = g_cfg_heat_hw_rows >= 0 ? int(g_cfg_heat_hw_rows) : (FX ? hw_default : 0);
   if (hw > G::TJ) hw = G::TJ;
   const dim3 block{unsigned(kThreads)};

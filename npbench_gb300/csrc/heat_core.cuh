@@ -27,13 +27,36 @@ __device__ __forceinline__ T ld(const T* p) {
   if constexpr (CG) return __ldcg(p); else return *p;
 }
 
+// The exact binary64 products 2*x and 0.125*x on the integer pipe: an
+// exponent change for normal x whose result stays normal, x itself for
+// signed zeros.  Subnormals, infinities, NaN and overflow take the literal
+// product, out of line so that it is not predicated into the common path
+// (GB300's binary64 pipe is the bound of the hardware rows).
+static __device__ __noinline__ double twice_literal(double x) { return mul_rn(2.0, x); }
+static __device__ __noinline__ double eighth_literal(double x) { return mul_rn(0.125, x); }
+__device__ __forceinline__ double twice(double x) {
+  const uint64_t b = static_cast<uint64_t>(__double_as_longlong(x));
+  const uint32_t e = static_cast<uint32_t>(b >> 52) & 0x7ffu;
+  if (e - 1u < 2045u) return __longlong_as_double(static_cast<long long>(b + (1ull << 52)));
+  if ((b << 1) == 0) return x;
+  return twice_literal(x);
+}
+__device__ __forceinline__ double eighth(double x) {
+  const uint64_t b = static_cast<uint64_t>(__double_as_longlong(x));
+  const uint32_t e = static_cast<uint32_t>(b >> 52) & 0x7ffu;
+  if (e - 4u < 2043u) return __longlong_as_double(static_cast<long long>(b - (3ull << 52)));
+  if ((b << 1) == 0) return x;
+  return eighth_literal(x);
+}
+__device__ __forceinline__ float twice(float x) { return mul_rn(2.0f, x); }
+__device__ __forceinline__ float eighth(float x) { return mul_rn(0.125f, x); }
+
 template <typename T>
 __device__ __forceinline__ T heat_point(T c, T ip, T im, T jp, T jm, T kp, T km) {
-  const T two = T(2.0), eighth = T(0.125);
-  const T c2 = mul_rn(two, c);
-  const T t0 = mul_rn(eighth, add_rn(sub_rn(ip, c2), im));
-  const T t1 = mul_rn(eighth, add_rn(sub_rn(jp, c2), jm));
-  const T t2 = mul_rn(eighth, add_rn(sub_rn(kp, c2), km));
+  const T c2 = twice(c);
+  const T t0 = eighth(add_rn(sub_rn(ip, c2), im));
+  const T t1 = eighth(add_rn(sub_rn(jp, c2), jm));
+  const T t2 = eighth(add_rn(sub_rn(kp, c2), km));
   return add_rn(add_rn(add_rn(t0, t1), t2), c);
 }
 

@@ -40,6 +40,7 @@ def test_search_spaces():
     heat = autotune._space("heat_3d", np.float64)
     assert {"HEAT_ROWS": 2, "HEAT_HW_ROWS": 4, "HEAT_CHUNK": 8} in heat
     assert {"HEAT_ROWS": 2, "HEAT_HW_ROWS": 5, "HEAT_CHUNK": 8} in heat
+    assert {"HEAT_ROWS": 2, "HEAT_HW_ROWS": 7, "HEAT_CHUNK": 8} in heat
     with pytest.raises(ValueError):
         autotune._space("hdiff", np.float64)
 
