@@ -90,6 +90,31 @@ int main(int argc, char** argv) {
     }
     n += 2;
   }
+  // hdiff's Laplacian fl(fl(4c) - s): for c with biased exponent 64..1981, 4c is
+  // an exponent increment by two and stays in range, so the difference is one
+  // emulated subtraction of (c with exponent + 2) and s.
+  for (long long it = 0; it < iters / 4; ++it) {
+    const uint32_t ec = 64 + rng() % 1918;
+    const double c = make(ec);
+    double s;
+    switch (rng() % 4) {
+      case 0: s = make(ec + 2); break;                             // same scale as 4c
+      case 1: s = dbl(bits(c) + (2ull << 52)); break;               // s == 4c: exact zero
+      case 2: s = make(64 + rng() % 1920); break;                   // anything
+      default: s = rng() & 1 ? 0.0 : -0.0; break;                   // signed zeros
+    }
+    const double four_c = dbl(bits(c) + (2ull << 52));
+    volatile double prod = 4.0 * c;
+    if (bits(four_c) != bits(prod)) { std::printf("4C MISMATCH c=%a\n", c); return 1; }
+    if (!dadd_z_ok(bits(four_c), bits(s))) { std::printf("4C REFUSED c=%a s=%a\n", c, s); return 1; }
+    const uint64_t got = dsub_z(bits(four_c), bits(s));
+    const double want = prod - s;
+    if (got != bits(want)) {
+      std::printf("LAPLACIAN MISMATCH c=%a s=%a got=%a want=%a\n", c, s, dbl(got), want);
+      return 1;
+    }
+    ++n;
+  }
   // Refusals.
   const double bad[] = {0.0, -0.0, 1e-310, -1e-310, std::numeric_limits<double>::infinity(),
                         std::nan(""), 1e300, std::ldexp(1.0, -970), std::ldexp(1.0, 961)};
