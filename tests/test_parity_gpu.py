@@ -416,6 +416,17 @@ def test_hdiff_full_size_vs_oracle():
     assert bits_equal(_host(d), out), first_diff(_host(d), out)
 
 
+def test_jacobi_large_grid_plain_adds():
+    """Grids of 2^21 cells and more take the fixed-point path with plain integer
+    additions (smaller ones issue them as multiply-adds): 1500^2 against the oracle."""
+    for dtype in (np.float64, np.float32):
+        A, B = workloads.uniform_pair((1500, 1500), dtype, seed=21)
+        dA, dB = _dev(A), _dev(B)
+        stencils.jacobi_2d_kernel(6, dA, dB)
+        cref.jacobi_2d_kernel(6, A, B)
+        assert bits_equal(_host(dA), A) and bits_equal(_host(dB), B), dtype
+
+
 @pytest.mark.parametrize("shape", [(3, 3), (7, 300), (300, 7), (129, 257), (1000, 33)])
 def test_jacobi_ragged_shapes(shape):
     for dtype in (np.float64, np.float32):
