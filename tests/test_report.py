@@ -95,3 +95,18 @@ def test_missing_baseline_is_an_error(tmp_path):
     _db(str(path), [("jacobi_2d", "polybench", "S", "main", "gb300", "fast", 1, 0.01)])
     with pytest.raises(ValueError):
         report.speedup_table(report.load_results(str(path)), "S")
+
+
+def test_benchmark_without_numpy_rows_is_blank(tmp_path):
+    """A benchmark that NumPy never ran has no ratio (blank cells, no effect on Total)."""
+    path = tmp_path / "npbench.db"
+    _db(str(path), [("jacobi_2d", "polybench", "S", "main", "numpy", "default", 1, 2.0),
+                    ("jacobi_2d", "polybench", "S", "main", "gb300", "fast", 1, 0.02),
+                    ("hdiff", "weather", "S", "main", "gb300", "default", 1, 0.5)])
+    t = report.speedup_table(report.load_results(str(path)), "S")
+    h = ("hdiff", "weather")
+    assert math.isnan(t["ratio"][h]["gb300"]) and math.isnan(t["ratio"][h]["numpy"])
+    assert t["total"]["gb300"] == pytest.approx(0.01)
+    md = report.to_markdown(t)
+    assert "| hdiff |  |  |" in md
+    ET.fromstring(report.to_svg(t))  # well-formed with blank cells
