@@ -23,6 +23,15 @@ The two 128 MiB arrays exceed the 129 MB L2, so no L2 flush is needed.
                 ``numpy_1core`` beside it times the NumPy restatement on one core
                 (NumPy's elementwise ufuncs are single-threaded).
 
+* ``batch``     configuration 4 (4096 mixed Jacobi-2D grids, float32 and
+                float64, in one batch per step), with plain per-grid launches of
+                the same grids beside it and the float32 grids' error against
+                float64 runs; its own step counts are stated in the block;
+* ``serve``     configuration 5 (100 Poisson-arrival mixed solves through the
+                serving loop at 200, 1000 and 5000 req/s) with p50/p99 latency,
+                the same requests run one at a time with per-grid launches beside
+                it, and the float32 requests' error against float64.
+
 ``--impl reference`` times only that CPU implementation (the C restatement on
 all host threads, one whole workload per step) and prints its line with
 ``"impl": "reference"``.
@@ -70,6 +79,10 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="default workload: leave out the batched block (configuration 4)")
+    ap.add_argument("--no-serve", action="store_true",
+                    help="default workload: leave out the served-stream block (configuration 5)")
     ap.add_argument("--workload", default="heat3d",
                     choices=["heat3d", "jacobi2d", "hdiff", "batch", "serve", "jacobi1d", "fdtd2d",
                              "vadv", "cavity", "channel"],
@@ -228,6 +241,14 @@ def cpu_port(setup, run, units, what, parallel=True, reps=3, numpy=None):
     return out
 
 
+def heat_config(world):
+    """The headline workload's config, identical in both arms."""
+    return {"workload": "heat_3d 256^3 float64, TSTEPS=100 (198 half-sweeps)",
+            "grid": [N_GRID] * 3, "TSTEPS": TSTEPS, "updates_per_step": UPDATES_PER_STEP,
+            "l2": "inputs larger than L2 (2 x 128 MiB), no flush",
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
 def run_reference(args, world, rank):
     """The reference's CPU path: heat_3d(TSTEPS=100) on the 256^3 float64 grid, each
     step one whole workload through the C restatement of heat_3d_numpy.py (bit-identical
@@ -259,8 +280,7 @@ def run_reference(args, world, rank):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic U[0,1) from default_rng(0)",
-        "config": {"workload": "heat_3d 256^3 float64, TSTEPS=100 (198 half-sweeps)",
-                   "TSTEPS": TSTEPS, "grid": [N_GRID] * 3},
+        "config": heat_config(world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": sample},
         "numpy_1core": {"value": v_np, "unit": UNIT, "cores": 1,
@@ -392,17 +412,24 @@ def run_gb300(args, world, rank, local):
                               lambda a, b: stencils_np.heat_3d_kernel(3, a, b), 4 * INTERIOR,
                               "TSTEPS=3 (4 half-sweeps) on the same grid"))
 
+    # Configurations 4 and 5 as blocks of the same line (one GPU only: under
+    # torchrun the replicas report the headline workload alone).
+    batch_block = serve_block = None
+    if world == 1 and not args.no_batch:
+        batch_block = batch_measure()
+        batch_block["workload"] = BATCH_WORKLOAD.format(n=4096)
+    if world == 1 and not args.no_serve:
+        serve_block = serve_measure()
+        serve_block["workload"] = SERVE_WORKLOAD.format(n=100, rate=0).replace(
+            "Poisson 0 req/s", "Poisson arrivals at each rate")
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic U[0,1) from numpy default_rng(rank), B = copy of A",
-            "config": {"workload": "heat_3d 256^3 float64, TSTEPS=100 (198 half-sweeps)",
-                       "grid": [N_GRID] * 3, "TSTEPS": TSTEPS,
-                       "updates_per_step": UPDATES_PER_STEP,
-                       "l2": "inputs larger than L2 (2 x 128 MiB), no flush",
-                       "parallelism": "replicas" if world > 1 else "single"},
+            "config": heat_config(world),
             "roofline": roofline,
             "fp64_roofline": fp64_roof,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * A64.nbytes,
@@ -411,6 +438,8 @@ def run_gb300(args, world, rank, local):
             "clocks": clocks,
             "fp32": fp32,
             "cpu_baseline": cpu,
+            "batch": batch_block,
+            "serve": serve_block,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -768,15 +797,45 @@ def run_fdtd2d(args):
         gpu_launches=2 * T * args.steps, clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
 
 
-def run_batch(args):
-    """4096 independent Jacobi-2D grids (sides log-uniform in [64, 2048], half float32 and
-    half float64, TSTEPS uniform in [10, 500]) in one persistent launch per step."""
+def _rel_err(low, ref):
+    """(max-abs, relative L2) of a low-precision result against its float64 run."""
+    d = low.double() - ref
+    nrm = float(ref.norm())
+    return float(d.abs().max()) if d.numel() else 0.0, (float(d.norm()) / nrm if nrm > 0 else 0.0)
+
+
+def _fp32_error_report(pairs):
+    """pairs: (TSTEPS, float32 result, float64 result of the same grid).  Worst error
+    overall and per TSTEPS range, with the grid count."""
+    bins = [(0, 100), (100, 250), (250, 10**9)]
+    out = {"grids": len(pairs), "max_abs": 0.0, "rel_l2_max": 0.0, "rel_l2_max_tsteps": None,
+           "by_tsteps": {}}
+    for lo, hi in bins:
+        out["by_tsteps"][f"{lo}-{hi if hi < 10**9 else 'max'}"] = {"grids": 0, "rel_l2_max": 0.0}
+    for T, low, ref in pairs:
+        mx, rl = _rel_err(low, ref)
+        out["max_abs"] = max(out["max_abs"], mx)
+        if rl >= out["rel_l2_max"]:
+            out["rel_l2_max"], out["rel_l2_max_tsteps"] = rl, T
+        for lo, hi in bins:
+            if lo <= T < hi:
+                b = out["by_tsteps"][f"{lo}-{hi if hi < 10**9 else 'max'}"]
+                b["grids"] += 1
+                b["rel_l2_max"] = max(b["rel_l2_max"], rl)
+    return out
+
+
+def batch_measure(n_grids=4096, steps=2, warmup=1, compare=True, compare_steps=1,
+                  compare_warmup=1, fp32_error=True, cpu=False):
+    """Configuration 4: ``n_grids`` independent Jacobi-2D grids (sides log-uniform in
+    [64, 2048] per axis, half float32 and half float64, TSTEPS uniform in [10, 500])
+    advanced by one batch per step.  Returns the measurement as a dict."""
     import torch
     from npbench_gb300 import _lib, stencils, workloads
     from npbench_gb300.batch import Batch
     dev = torch.device("cuda", 0)
     stream = torch.cuda.current_stream(dev)
-    specs = workloads.batch_jacobi_specs(args.batch_grids, seed=0)
+    specs = workloads.batch_jacobi_specs(n_grids, seed=0)
     gen = torch.Generator(device=dev)
     gen.manual_seed(0)
     init, work = [], []
@@ -793,27 +852,53 @@ def run_batch(args):
             b.copy_(b0)
 
     ups = sum(2 * (T - 1) * (s[0] - 2) * (s[1] - 2) for s, _, T in specs)
-    alg = sum(2 * (T - 1) * (s[0] - 2) * (s[1] - 2) * 2 * np.dtype(dt).itemsize for s, dt, T in specs)
+    alg = sum(2 * (T - 1) * (s[0] - 2) * (s[1] - 2) * 2 * np.dtype(dt).itemsize
+              for s, dt, T in specs)
     with Batch(work, band_rows=128) as batch:
         info = batch.info()
         with ClockSampler(0) as clk:
             ms = _timed_steps(torch, dev, stream, lambda: batch.launch(graph=True), reset,
-                              args.steps, args.warmup)
+                              steps, warmup)
         _lib.device_status()
-    ms_step = ms / args.steps
+    ms_step = ms / steps
     peak, kind = measured_peaks()
     ach = alg / (ms_step * 1e-3) / 1e9
-    comp = None
-    if args.compare:
+    out = {"value": ups / (ms_step * 1e-3), "unit": UNIT, "ms_per_step": ms_step,
+           "steps": steps, "warmup": warmup, "updates_per_step": ups,
+           "cells": sum(s[0] * s[1] for s, _, _ in specs), "form": info["mode"],
+           "tiles" if info["mode"] == "stepped" else "bands": info["bands"],
+           "launches" if info["mode"] == "stepped" else "ctas": info["ctas"],
+           "rows_per_tile": 128, "graph": True,
+           "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                        "frac": ach / peak, "peak_kind": kind,
+                        "traffic": ncu_traffic("batch_4096")},
+           "clocks": clk.summary()}
+    if compare:
         def per_grid():
             for a, b, T in work:
                 stencils.jacobi_2d_kernel(T, a, b)
-        ms_pg = _timed_steps(torch, dev, stream, per_grid, reset, 1, 0)
-        comp = {"per_grid_launches_updates_per_s": ups / (ms_pg * 1e-3),
-                "per_grid_ms": ms_pg, "batched_over_per_grid": ms_pg / ms_step,
-                "per_grid_kernel_launches": sum(2 * (T - 1) for _, _, T in specs)}
-    cpu = None
-    if not args.no_cpu_baseline:
+        ms_pg = _timed_steps(torch, dev, stream, per_grid, reset, compare_steps, compare_warmup)
+        ms_pg /= compare_steps
+        out["per_grid"] = {"value": ups / (ms_pg * 1e-3), "ms_per_step": ms_pg,
+                           "steps": compare_steps, "warmup": compare_warmup,
+                           "kernel_launches": sum(2 * (T - 1) for _, _, T in specs),
+                           "what": "one jacobi_2d_kernel call per grid (chained launches, "
+                                   "tuned single-grid kernels), same inputs and steps"}
+        out["batched_over_per_grid"] = ms_pg / ms_step
+    if fp32_error:
+        # The float32 grids against float64 runs of the same (exactly widened) inputs.
+        reset()
+        with Batch(work, band_rows=128) as batch:
+            batch.launch()
+        f32 = [(g, T) for g, ((_, dt, T), _) in enumerate(zip(specs, work)) if dt == np.float32]
+        shadow = [(init[g][0].double(), init[g][1].double(), T) for g, T in f32]
+        with Batch(shadow, band_rows=128) as sb:
+            sb.launch()
+        torch.cuda.synchronize(dev)
+        out["fp32_error_vs_fp64"] = _fp32_error_report(
+            [(T, work[g][0], shadow[n][0]) for n, (g, T) in enumerate(f32)])
+        del shadow
+    if cpu:
         # The first 64 grids of the same configuration, seeded host inputs: timed
         # through the C restatement on all host threads, and run as a GPU batch
         # that must match it bit for bit.
@@ -833,64 +918,112 @@ def run_batch(args):
                     np.array_equal(b.view(np.uint8), gb.cpu().numpy().view(np.uint8))
                     for (a, b, _), (ga, gb, _) in zip(host, gpu))
         ups_s = sum(2 * (T - 1) * (sh[0] - 2) * (sh[1] - 2) for sh, _, T in sample)
-        cpu = {"value": ups_s / dt_cpu, "unit": UNIT, "cores": host_threads(), "kind": "port",
-               "sample": f"the first {len(sample)} grids of the batch ({ups_s:.3g} updates), C "
-                         f"restatement on {host_threads()} host threads, {dt_cpu:.2f} s; the GPU "
-                         f"batch of the same grids {'matches it bit for bit' if exact else 'DIFFERS'}"}
-    cells = sum(s[0] * s[1] for s, _, _ in specs)
+        out["cpu_baseline"] = {
+            "value": ups_s / dt_cpu, "unit": UNIT, "cores": host_threads(), "kind": "port",
+            "sample": f"the first {len(sample)} grids of the batch ({ups_s:.3g} updates), C "
+                      f"restatement on {host_threads()} host threads, {dt_cpu:.2f} s; the GPU "
+                      f"batch of the same grids {'matches it bit for bit' if exact else 'DIFFERS'}"}
+    del init, work
+    torch.cuda.empty_cache()
+    return out
+
+
+BATCH_WORKLOAD = ("batched jacobi_2d: {n} grids, sides log-uniform [64, 2048], half float32 / "
+                  "half float64, TSTEPS uniform [10, 500]")
+
+
+def run_batch(args):
+    """Configuration 4 on its own line (``--workload batch``)."""
+    b = batch_measure(args.batch_grids, steps=args.steps, warmup=args.warmup,
+                      compare=args.compare, cpu=not args.no_cpu_baseline)
+    extra = {k: b[k] for k in ("cells", "updates_per_step", "form", "rows_per_tile", "graph")}
     print(json.dumps(_base_line(
-        args, ups * args.steps / (ms * 1e-3), ms_step, "f32+f64",
-        f"batched jacobi_2d: {args.batch_grids} grids, sides log-uniform [64, 2048], half "
-        f"float32 / half float64, TSTEPS uniform [10, 500]",
-        {"cells": cells, "updates_per_step": ups, "form": info["mode"],
-         "tiles" if info["mode"] == "stepped" else "bands": info["bands"],
-         "launches" if info["mode"] == "stepped" else "ctas": info["ctas"],
-         "rows_per_tile" if info["mode"] == "stepped" else "band_rows": 128, "graph": True, "l2": f"{cells * 6 * 2 / 1e9:.1f} GB resident, "
-                                                "far above L2"},
-        roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-                  "frac": ach / peak, "peak_kind": kind, "traffic": None},
-        comparator=comp, gpu_launches=args.steps, clocks=clk.summary(),
-        cpu_baseline=cpu)), flush=True)
+        args, b["value"], b["ms_per_step"], "f32+f64", BATCH_WORKLOAD.format(n=args.batch_grids),
+        dict(extra, l2=f"{b['cells'] * 6 * 2 / 1e9:.1f} GB resident, far above L2"),
+        roofline=b["roofline"], comparator=b.get("per_grid"),
+        batched_over_per_grid=b.get("batched_over_per_grid"),
+        fp32_error_vs_fp64=b.get("fp32_error_vs_fp64"), gpu_launches=args.steps,
+        clocks=b["clocks"], cpu_baseline=b.get("cpu_baseline"))), flush=True)
 
 
-def run_serve(args):
-    """Poisson-arrival mixed solves through the continuous-batching server."""
+SERVE_WORKLOAD = ("served stream: {n} requests, Poisson {rate:g} req/s, 2D Jacobi 128^2-4096^2 "
+                  "and 3D heat 32^3-384^3 (log-uniform per axis), 70% float32, TSTEPS 20-1000")
+
+
+def serve_measure(rates=(200.0, 1000.0, 5000.0), n_requests=100, compare=True, fp32_error=True,
+                  quantum=64, cpu=False):
+    """Configuration 5: Poisson arrivals of mixed solves through the continuous-batching
+    server at each rate, beside the same requests run one at a time with per-grid
+    launches.  Returns {"rates": [...], "fp32_error_vs_fp64": ...}."""
     import torch
-    from npbench_gb300 import workloads
-    from npbench_gb300.server import Request, StencilServer, latency_stats, run_sequential
-    arrivals, specs = workloads.served_requests(args.requests, args.rate, seed=0)
-
-    def make():
-        return [Request(shape=s, dtype=dt, tsteps=T, seed=sd, return_host=False)
-                for s, dt, T, sd in specs]
-
-    with StencilServer(quantum=args.quantum) as warm:
+    from npbench_gb300 import stencils, workloads
+    from npbench_gb300.server import (Request, StencilServer, latency_stats, run_sequential,
+                                      _materialise)
+    with StencilServer(quantum=quantum) as warm:
         warm.submit(Request(shape=(64, 64), dtype=np.float32, tsteps=5, seed=1)).result()
-    reqs = make()
-    srv = StencilServer(quantum=args.quantum, hbm_budget_bytes=150e9).start()
-    t0 = time.perf_counter()
-    futs = []
-    with ClockSampler(0) as clk:
-        for r, at in zip(reqs, arrivals):
-            now = time.perf_counter() - t0
-            if at > now:
-                time.sleep(at - now)
-            futs.append(srv.submit(r))
-        for f in futs:
-            f.result()
-        srv.stop()
-    st = latency_stats(reqs)
-    comp = None
-    if args.compare:
-        seq = make()
-        run_sequential(seq, arrivals)
-        comp = latency_stats(seq)
-        comp["served_over_sequential_updates_per_s"] = st["updates_per_s"] / comp["updates_per_s"]
-    cpu = None
-    if not args.no_cpu_baseline:
+    out = {"requests_per_rate": n_requests, "hbm_budget_gb": 150, "rates": []}
+    kept = None
+    for rate in rates:
+        arrivals, specs = workloads.served_requests(n_requests, rate, seed=0)
+
+        def make():
+            return [Request(shape=s, dtype=dt, tsteps=T, seed=sd, return_host=False)
+                    for s, dt, T, sd in specs]
+        reqs = make()
+        srv = StencilServer(quantum=quantum, hbm_budget_bytes=150e9).start()
+        t0 = time.perf_counter()
+        futs = []
+        with ClockSampler(0) as clk:
+            for r, at in zip(reqs, arrivals):
+                now = time.perf_counter() - t0
+                if at > now:
+                    time.sleep(at - now)
+                futs.append(srv.submit(r))
+            results = [f.result() for f in futs]
+            srv.stop()
+        st = latency_stats(reqs)
+        entry = {"rate_hz": rate, "served": {k: st[k] for k in ("updates_per_s", "p50_ms",
+                                                                  "p99_ms", "mean_ms", "span_s")},
+                 "rounds": srv.rounds, "peak_resident_gb": srv.admission.peak / 1e9,
+                 "clocks": clk.summary()}
+        if compare:
+            seq = make()
+            run_sequential(seq, arrivals)
+            sq = latency_stats(seq)
+            entry["sequential"] = {k: sq[k] for k in ("updates_per_s", "p50_ms", "p99_ms",
+                                                      "mean_ms", "span_s")}
+            entry["served_over_sequential"] = st["updates_per_s"] / sq["updates_per_s"]
+        out["rates"].append(entry)
+        if fp32_error and kept is None:
+            kept = (reqs, results)
+        else:
+            del results
+        torch.cuda.empty_cache()
+    out["stream_updates"] = sum(r.updates for r in reqs)
+    if kept is not None:
+        reqs, results = kept
+        dev = torch.device("cuda", 0)
+        pairs = []
+        for r, (A, B) in zip(reqs, results):
+            if np.dtype(r.dtype) != np.float32 or r.tsteps <= 1:
+                continue
+            shadow = Request(shape=r.shape, dtype=np.float64, tsteps=r.tsteps, seed=r.seed)
+            a64, b64 = _materialise(shadow, dev)
+            (stencils.jacobi_2d_kernel if a64.dim() == 2 else stencils.heat_3d_kernel)(
+                r.tsteps, a64, b64)
+            pairs.append((r.tsteps, A, a64))
+        torch.cuda.synchronize(dev)
+        rep = _fp32_error_report(pairs)
+        rep["what"] = ("float32 requests of the stream against float64 runs of the same "
+                       "seeded draw (float32 inputs are roundings of it)")
+        out["fp32_error_vs_fp64"] = rep
+        del pairs, kept, results
+        torch.cuda.empty_cache()
+    if cpu:
         # The stream's requests in arrival order, up to about 2e10 updates,
         # through the C restatement on all host threads.
         from oracle import cref
+        _, specs = workloads.served_requests(n_requests, rates[0], seed=0)
         rng = np.random.default_rng(2)
         done_ups, t_cpu, n = 0, 0.0, 0
         for shape, dt, T, _ in specs:
@@ -903,17 +1036,27 @@ def run_serve(args):
             t_cpu += time.perf_counter() - t0
             done_ups += 2 * (T - 1) * int(np.prod([x - 2 for x in shape]))
             n += 1
-        cpu = {"value": done_ups / t_cpu, "unit": UNIT, "cores": host_threads(), "kind": "port",
-               "sample": f"the stream's first {n} requests ({done_ups:.3g} updates), C "
-                         f"restatement on {host_threads()} host threads, {t_cpu:.2f} s"}
+        out["cpu_baseline"] = {
+            "value": done_ups / t_cpu, "unit": UNIT, "cores": host_threads(), "kind": "port",
+            "sample": f"the stream's first {n} requests ({done_ups:.3g} updates), C "
+                      f"restatement on {host_threads()} host threads, {t_cpu:.2f} s"}
+    return out
+
+
+def run_serve(args):
+    """Configuration 5 on its own line (``--workload serve``) at ``--rate``."""
+    s = serve_measure(rates=(args.rate,), n_requests=args.requests, compare=args.compare,
+                      quantum=args.quantum, cpu=not args.no_cpu_baseline)
+    e = s["rates"][0]
     print(json.dumps(_base_line(
-        args, st["updates_per_s"], st["span_s"] * 1e3, "f32+f64",
-        f"served stream: {args.requests} requests, Poisson {args.rate:g} req/s, 2D Jacobi "
-        f"128^2-4096^2 and 3D heat 32^3-384^3 (log-uniform), 70% float32, TSTEPS 20-1000",
-        {"quantum_half_sweeps": args.quantum, "hbm_budget_gb": 150, "rounds": srv.rounds,
-         "peak_resident_gb": srv.admission.peak / 1e9},
-        latency={"p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"]},
-        comparator=comp, clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
+        args, e["served"]["updates_per_s"], e["served"]["span_s"] * 1e3, "f32+f64",
+        SERVE_WORKLOAD.format(n=args.requests, rate=args.rate),
+        {"quantum_half_sweeps": args.quantum, "hbm_budget_gb": 150, "rounds": e["rounds"],
+         "peak_resident_gb": e["peak_resident_gb"]},
+        latency={k: e["served"][k] for k in ("p50_ms", "p99_ms", "mean_ms")},
+        comparator=e.get("sequential"), served_over_sequential=e.get("served_over_sequential"),
+        fp32_error_vs_fp64=s.get("fp32_error_vs_fp64"), clocks=e["clocks"],
+        cpu_baseline=s.get("cpu_baseline"))), flush=True)
 
 
 def main():

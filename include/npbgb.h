@@ -296,9 +296,12 @@ NPBGB_API int32_t npbgb_batch_destroy(npbgb_batch* batch);
  * current; make that first call before any stream capture.  Every call shares
  * the array and the counters are cleared each call, so calls whose work
  * overlaps on the GPU (for example on two streams) race; calls on one stream
- * are ordered.  The plan is copied from host memory with cudaMemcpyAsync, so
- * the call returns once the plan is staged.  Results are bit-identical to
- * npbgb_batch_create + npbgb_batch_launch. */
+ * are ordered.  The plan is copied from shared static host buffers with
+ * cudaMemcpyAsync from pageable memory: each call first waits for the work
+ * already queued on `stream`, and returns once the plan is staged.  A stream
+ * that is capturing a graph is refused with NPBGB_ERR_ARG (a replay would read
+ * whatever plan a later call left in those buffers).  Results are
+ * bit-identical to npbgb_batch_create + npbgb_batch_launch. */
 NPBGB_API int32_t npbgb_batch_run_noalloc(const npbgb_grid* grids, int64_t count,
                                           int32_t band_rows, void* stream);
 

@@ -767,9 +767,21 @@ extern "C" int32_t npbgb_batch_run_noalloc(const npbgb_grid* grids, int64_t coun
   }
   if (nb == 0) return NPBGB_OK;
 
-  // Once per device, with that device current: the scratch symbol's address.
+  // The plan is staged from the shared static host buffers above, so a
+  // captured copy would replay whatever a later call left there: refuse.
+  cudaStream_t st = as_stream(stream);
+  cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(st, &capturing);
+  if (e != cudaSuccess) return cuda_status(e, "batch(no-alloc): stream state");
+  if (capturing != cudaStreamCaptureStatusNone)
+    return set_error(NPBGB_ERR_ARG,
+                     "batch(no-alloc): the stream is capturing a graph; this entry point stages "
+                     "its plan from shared host buffers and cannot be captured");
+
+  // Once per device, with that device current: the scratch symbol's address
+  // and the co-resident CTA count of that device.
   int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_status(e, "batch(no-alloc): current device");
   if (dev < 0 || dev >= kNoAllocMaxDevices) return set_error(NPBGB_ERR_ARG, "batch(no-alloc): device %d", dev);
   NoAllocDevice& D = g_noalloc_devices[dev];
@@ -777,10 +789,12 @@ extern "C" int32_t npbgb_batch_run_noalloc(const npbgb_grid* grids, int64_t coun
     void* ptr = nullptr;
     e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_status(e, "batch(no-alloc): cudaGetSymbolAddress");
-    int per_sm = 0;
+    int per_sm = 0, sms = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_persistent<2>, kBThreads, 0);
     if (e != cudaSuccess) return cuda_status(e, "batch(no-alloc): occupancy");
-    D.slots = std::max(1, per_sm) * sm_count();
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_status(e, "batch(no-alloc): SM count");
+    D.slots = std::max(1, per_sm) * std::max(1, sms);
     D.scratch = static_cast<NoAllocLayout*>(ptr);
   }
 
@@ -813,7 +827,6 @@ extern "C" int32_t npbgb_batch_run_noalloc(const npbgb_grid* grids, int64_t coun
   }
 
   // Upload the plan, clear the counters (they must start at zero), launch.
-  cudaStream_t st = as_stream(stream);
   NoAllocLayout* S = D.scratch;
   if ((e = cudaMemcpyAsync(S->bands, g_na_bands, sizeof(BandDesc) * size_t(nb), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
       (e = cudaMemcpyAsync(S->cta_off, g_na_cta_off, sizeof(int32_t) * size_t(nctas + 1), cudaMemcpyHostToDevice, st)) != cudaSuccess ||

@@ -1,8 +1,9 @@
 """Generate the golden vectors for the stencil path from the reference itself.
 
-Run in a checkout that has the NPBench sources (default ``/root/reference``):
+Run with a directory holding the NPBench sources (``--ref``, or the
+NPBENCH_SRC environment variable):
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--ref DIR]
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py --ref DIR
 
 It imports the reference's own NumPy kernels
 
@@ -55,8 +56,11 @@ def special_values(rng, shape, dtype):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("NPBENCH_SRC"),
+                    help="NPBench source tree (default: $NPBENCH_SRC)")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give --ref DIR or set NPBENCH_SRC to an NPBench source tree")
     sys.dont_write_bytecode = True
     sys.path.insert(0, args.ref)
     from npbench.benchmarks.polybench.jacobi_2d import jacobi_2d_numpy, jacobi_2d

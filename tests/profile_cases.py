@@ -1,10 +1,12 @@
-"""Small single-kernel cases for ncu captures.
+"""Small single-kernel cases for ncu captures (the recipe behind the profile summaries).
 
-    python -m npbench_gb300.profile_cases <case>
+    python tests/profile_cases.py <case>
 
 Each case runs one kernel family on an input still larger than L2 where the
 real workload is, with few launches, so that one capture
-(``ncu --set full -k regex:<kernel> -s <n> -c 1``) ends in seconds:
+(``ncu --set full --clock-control none -k regex:<kernel> -s <n> -c 1``) ends in
+seconds.  Run the case once without ncu first; capture it only after that run
+exited 0:
 
 ========== ============================================== ===================
 case       what                                           kernel to capture
@@ -23,9 +25,14 @@ jacobi1d   Jacobi-1D N=32000 float64, TSTEPS=64           jacobi1d_block, -s 2
 fdtd       FDTD-2D 1000x1200 float64, TMAX=3 (6 launches) fdtd_e / fdtd_h, -s 1
 ========== ============================================== ===================
 """
+import os
 import sys
 
 import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
 
 
 def run(case):

@@ -71,3 +71,24 @@ def test_default_run_line():
     assert e2e["d2h_bytes_per_step"] == 2 * 8 * 256 ** 3
     assert line["gpu_launches"] == 2 * 198
     assert "sm_mhz" in line["clocks"] and "reasons" in line["clocks"]
+
+
+@pytest.mark.gpu
+def test_batch_and_serve_blocks():
+    """The default line's configuration 4 and 5 blocks, on a few grids and requests."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import bench
+    b = bench.batch_measure(n_grids=48, steps=1, warmup=1, compare_steps=1, compare_warmup=0)
+    assert b["value"] > 0 and b["per_grid"]["value"] > 0
+    assert b["batched_over_per_grid"] == pytest.approx(b["per_grid"]["ms_per_step"] /
+                                                       b["ms_per_step"])
+    err = b["fp32_error_vs_fp64"]
+    assert err["grids"] == 24 and 0 < err["rel_l2_max"] < 1e-3
+    assert sum(v["grids"] for v in err["by_tsteps"].values()) == 24
+    s = bench.serve_measure(rates=(2000.0,), n_requests=6)
+    (e,) = s["rates"]
+    assert e["served"]["updates_per_s"] > 0 and e["sequential"]["updates_per_s"] > 0
+    assert e["served"]["p50_ms"] <= e["served"]["p99_ms"]
+    assert s["fp32_error_vs_fp64"]["grids"] >= 1

@@ -26,10 +26,11 @@ BUILT_TREE = os.path.join(ROOT, "baseline", "_ref", "npbench")
 
 
 def _npbench_source():
-    src = os.environ.get("NPBENCH_SRC", os.path.join(os.sep, "root", "reference"))
-    if not os.path.isdir(os.path.join(src, "npbench", "infrastructure")):
-        return None
-    return src
+    """An NPBench tree to copy: NPBENCH_SRC, else the tree build() installed."""
+    for src in (os.environ.get("NPBENCH_SRC"), BUILT_TREE):
+        if src and os.path.isdir(os.path.join(src, "npbench", "infrastructure")):
+            return src
+    return None
 
 
 def _run(tree, code, timeout=600):

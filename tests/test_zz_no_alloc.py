@@ -109,3 +109,22 @@ def test_noalloc_rejects_plans_beyond_its_capacity():
     assert st == _lib.NPBGB_ERR_NOMEM
     assert b"32768" in lib.npbgb_last_error()
     _lib.device_status()
+
+
+def test_noalloc_refuses_a_capturing_stream():
+    # The plan is staged from shared host buffers, so a captured call could be
+    # replayed against another call's plan: the entry point refuses capture
+    # before it stages or launches anything.
+    lib = _lib.load()
+    grids = _to_dev(_grids(4, 3, 60, 6))
+    arr = _struct_array(grids)
+    x = torch.zeros(8, device=DEV)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        st = lib.npbgb_batch_run_noalloc(arr, len(grids), 0, torch.cuda.current_stream().cuda_stream)
+        x.add_(1.0)
+    assert st == _lib.NPBGB_ERR_ARG
+    assert b"capturing" in lib.npbgb_last_error()
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(x.sum()) == 8.0
