@@ -71,7 +71,7 @@ extern "C" {
                                          0: plain stream order */
 #define NPBGB_CFG_BATCH_MODE 11       /* form of a batch, read when it is planned:
                                          0 (default) automatic by size, 1 persistent,
-                                         2 stepped (NPBGB_BATCH_*) */
+                                         2 stepped, 3 queue (NPBGB_BATCH_*) */
 #define NPBGB_CFG_HDIFF_EMU 12        /* hdiff: which Laplacian and flux items run on the
                                          integer pipes (exact binary64 addition in
                                          integer arithmetic) next to the hardware
@@ -93,6 +93,7 @@ extern "C" {
 /* Batch forms. */
 #define NPBGB_BATCH_PERSISTENT 1
 #define NPBGB_BATCH_STEPPED 2
+#define NPBGB_BATCH_QUEUE 3
 
 /* Grid kinds for batches. */
 #define NPBGB_KIND_JACOBI2D 0
@@ -272,15 +273,65 @@ NPBGB_API int32_t npbgb_batch_replan(npbgb_batch* batch, const npbgb_grid* grids
                                      int32_t band_rows);
 NPBGB_API int32_t npbgb_batch_info(const npbgb_batch* batch, int64_t* nbands, int64_t* nctas,
                                    int64_t* updates);
-/* The form the batch was planned in (NPBGB_BATCH_PERSISTENT or NPBGB_BATCH_STEPPED).
+/* The form the batch was planned in (NPBGB_BATCH_PERSISTENT, NPBGB_BATCH_STEPPED
+ * or NPBGB_BATCH_QUEUE).
  * Persistent: one cooperative launch whose CTAs advance bands of rows as their
  * neighbours allow (best when the batch is small).  Stepped: one launch per
  * half-sweep index over all tiles of the grids still active, chained by
  * programmatic dependent launch (best when the batch fills the GPU; batches of
- * 2^24 cells or more by default).  In the stepped form npbgb_batch_info reports
- * the tiles as nbands and the launches as nctas.  Both forms leave the same bits. */
+ * 2^24 cells or more by default).  Queue: one launch of the device-side tile
+ * work queue (npbgb_queue_create below) with every grid's first half-sweep in
+ * its ring; a grid's next half-sweep is appended by the CTA that completes its
+ * previous one, and tiles are claimed in ring order (band_rows = rows or planes
+ * per tile).  In the stepped and queue forms npbgb_batch_info reports the tiles
+ * as nbands (queue: over all half-sweeps) and the launches (stepped) or CTAs
+ * (queue) as nctas.  All forms leave the same bits. */
 NPBGB_API int32_t npbgb_batch_mode(const npbgb_batch* batch, int32_t* mode);
 NPBGB_API int32_t npbgb_batch_destroy(npbgb_batch* batch);
+
+/* Device-side tile work queue: a persistent worker kernel that advances
+ * Jacobi-2D and Heat-3D grids of any sizes, precisions and step counts while
+ * the host keeps adding grids.  Its CTAs claim tiles of grid half-sweeps from a
+ * ring in device memory; the CTA that completes a grid's half-sweep appends the
+ * next one, so grids interleave tile by tile and none waits for a launch
+ * boundary.  The host adds grids through an inbox in pinned host memory that
+ * the running kernel reads (no synchronisation, no launch per grid) and learns
+ * of finished grids by polling completion words the kernel writes to host
+ * memory.  Each grid ends bit-identical to npbgb_jacobi2d / npbgb_heat3d on it,
+ * i.e. to the reference's kernel(TSTEPS, A, B),
+ * polybench/jacobi_2d/jacobi_2d_numpy.py:4-10 and
+ * polybench/heat_3d/heat_3d_numpy.py:4-20; the reference has no queue (it
+ * runs one grid per call), so this is the serving counterpart of those calls.
+ *
+ * npbgb_queue_create: up to max_slots grids in flight; tile_rows / tile_planes
+ *   are the Jacobi-2D rows and Heat-3D planes per tile (0 = 128 / 16; a grid's
+ *   band_rows overrides); ctas_per_sm (2-4, 0 = 3) sizes the worker launch;
+ *   the worker ends after idle_us microseconds with nothing to do.  Device
+ *   buffers and pinned host memory are allocated here, never later.
+ * npbgb_queue_submit: takes a grid (npbgb_grid, step0/nsteps honoured) and
+ *   returns its slot, or -1 for a grid with nothing to do.  NPBGB_ERR_NOMEM
+ *   when every slot is busy.  The arrays must stay allocated until the slot is
+ *   reported finished.
+ * npbgb_queue_kick: launches the worker on `stream` unless one is running;
+ *   call it after submitting.  A running worker takes new grids in by itself.
+ * npbgb_queue_poll: up to cap slots finished since the last poll; their grids
+ *   are complete in device memory and the slots are free again.
+ * npbgb_queue_state: whether a worker is running, busy slots, launches so far;
+ *   NPBGB_ERR_TIMEOUT once a worker gave up a bounded wait (no tile completed
+ *   for two seconds while work was outstanding).
+ * npbgb_queue_close: no more grids; a running worker ends once all are done.
+ * npbgb_queue_destroy: closes, waits for a running worker to end, frees. */
+typedef struct npbgb_queue npbgb_queue;
+NPBGB_API int32_t npbgb_queue_create(int32_t max_slots, int32_t tile_rows, int32_t tile_planes,
+                                     int32_t ctas_per_sm, int64_t idle_us, npbgb_queue** out);
+NPBGB_API int32_t npbgb_queue_submit(npbgb_queue* queue, const npbgb_grid* grid, int32_t* slot);
+NPBGB_API int32_t npbgb_queue_kick(npbgb_queue* queue, void* stream);
+NPBGB_API int32_t npbgb_queue_poll(npbgb_queue* queue, int32_t* slots, int32_t cap,
+                                   int32_t* count);
+NPBGB_API int32_t npbgb_queue_state(npbgb_queue* queue, int32_t* running, int32_t* busy,
+                                    int64_t* launches);
+NPBGB_API int32_t npbgb_queue_close(npbgb_queue* queue);
+NPBGB_API int32_t npbgb_queue_destroy(npbgb_queue* queue);
 
 /* Runs a batch of Jacobi-2D grids like npbgb_batch_create + npbgb_batch_launch, for callers that
  * must not allocate device memory: a host whose pool or HBM budget owns every

@@ -35,6 +35,7 @@ NPBGB_CFG_JACOBI1D_CTAS = 14
 NPBGB_CFG_JACOBI1D_DEPTH = 15
 NPBGB_BATCH_PERSISTENT = 1
 NPBGB_BATCH_STEPPED = 2
+NPBGB_BATCH_QUEUE = 3
 
 NPBGB_KIND_JACOBI2D = 0
 NPBGB_KIND_HEAT3D = 1
@@ -67,6 +68,14 @@ SIGNATURES = {
                                  ctypes.POINTER(_i64)]),
     "npbgb_batch_destroy": (_i32, [_vp]),
     "npbgb_batch_run_noalloc": (_i32, [ctypes.POINTER(Grid), _i64, _i32, _vp]),
+    "npbgb_queue_create": (_i32, [_i32, _i32, _i32, _i32, _i64, ctypes.POINTER(_vp)]),
+    "npbgb_queue_submit": (_i32, [_vp, ctypes.POINTER(Grid), ctypes.POINTER(_i32)]),
+    "npbgb_queue_kick": (_i32, [_vp, _vp]),
+    "npbgb_queue_poll": (_i32, [_vp, ctypes.POINTER(_i32), _i32, ctypes.POINTER(_i32)]),
+    "npbgb_queue_state": (_i32, [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i32),
+                                 ctypes.POINTER(_i64)]),
+    "npbgb_queue_close": (_i32, [_vp]),
+    "npbgb_queue_destroy": (_i32, [_vp]),
     "npbgb_jacobi2d": (_i32, [_vp, _vp, _i64, _i64, _i32, _i32, _vp]),
     "npbgb_heat3d": (_i32, [_vp, _vp, _i64, _i64, _i64, _i32, _i32, _vp]),
     "npbgb_hdiff": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i32, _vp]),

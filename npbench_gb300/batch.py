@@ -23,7 +23,7 @@ from . import _lib
 __all__ = ["Batch"]
 
 _MODES = {None: 0, "auto": 0, "persistent": _lib.NPBGB_BATCH_PERSISTENT,
-          "stepped": _lib.NPBGB_BATCH_STEPPED}
+          "stepped": _lib.NPBGB_BATCH_STEPPED, "queue": _lib.NPBGB_BATCH_QUEUE}
 _plan_lock = threading.Lock()
 
 
@@ -116,7 +116,8 @@ class Batch:
                                         ctypes.byref(up)), "npbgb_batch_info")
         mode = ctypes.c_int32()
         _lib.check(lib.npbgb_batch_mode(self._h, ctypes.byref(mode)), "npbgb_batch_mode")
-        name = "stepped" if mode.value == _lib.NPBGB_BATCH_STEPPED else "persistent"
+        name = {_lib.NPBGB_BATCH_STEPPED: "stepped",
+                _lib.NPBGB_BATCH_QUEUE: "queue"}.get(mode.value, "persistent")
         return {"mode": name, "bands": nb.value, "ctas": nc.value, "updates": up.value}
 
     def close(self):

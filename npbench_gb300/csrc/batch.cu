@@ -39,6 +39,7 @@
 #include "heat_core.cuh"
 #include "jacobi_core.cuh"
 #include "npbgb_common.cuh"
+#include "queue.cuh"
 #include "tma.cuh"
 
 namespace npbgb {
@@ -300,6 +301,8 @@ struct npbgb_batch {
   int32_t* d_tiles = nullptr;
   int64_t cap_step = 0, cap_tiles = 0, ntiles = 0;
   std::vector<int32_t> launch_tiles;  // CTAs of launch s = tiles of the grids active at s
+  // Queue form (mode NPBGB_BATCH_QUEUE).
+  npbgb::qhost::StaticQueue* sq = nullptr;
 };
 
 namespace {
@@ -363,6 +366,7 @@ double band_work(const npbgb::BandDesc& d) {
 void free_batch(npbgb_batch* b) {
   if (!b) return;
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  npbgb::qhost::free_static(b->sq);
   cudaFree(b->d_step);
   cudaFree(b->d_tiles);
   cudaFree(b->d_bands);
@@ -386,6 +390,7 @@ int32_t launch_stepped(npbgb_batch* b, cudaStream_t st) {
 int32_t launch_batch(npbgb_batch* b, cudaStream_t st) {
   using namespace npbgb;
   if (b->mode == NPBGB_BATCH_STEPPED) return launch_stepped(b, st);
+  if (b->mode == NPBGB_BATCH_QUEUE) return qhost::launch_static(b->sq, st);
   cudaError_t e = cudaMemsetAsync(b->d_done, 0, sizeof(uint32_t) * size_t(b->nbands), st);
   if (e != cudaSuccess) return cuda_status(e, "batch: reset counters");
   int f64_emul = int(g_cfg_f64_emulation);
@@ -528,7 +533,22 @@ int32_t plan_into(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int32_
   const int32_t mode = g_cfg_batch_mode != 0
                            ? int32_t(g_cfg_batch_mode)
                            : (cells >= kSteppedCells ? NPBGB_BATCH_STEPPED : NPBGB_BATCH_PERSISTENT);
+  qhost::free_static(b->sq);
+  b->sq = nullptr;
   if (mode == NPBGB_BATCH_STEPPED) return plan_stepped(b, grids, count, band_rows, updates);
+  if (mode == NPBGB_BATCH_QUEUE) {
+    int64_t qup = 0, qtiles = 0;
+    const int32_t r = qhost::plan_static(grids, count, band_rows, int(g_cfg_batch_ctas_per_sm),
+                                         &b->sq, &qup, &qtiles);
+    if (r != NPBGB_OK) return r;
+    b->mode = NPBGB_BATCH_QUEUE;
+    b->launch_tiles.clear();
+    b->ntiles = qtiles;
+    b->nbands = qtiles;  // "nothing to do" checks use nbands
+    b->nctas = qhost::static_ctas(b->sq);
+    b->updates = qup;
+    return NPBGB_OK;
+  }
   b->mode = NPBGB_BATCH_PERSISTENT;
   b->launch_tiles.clear();
   int per_sm = 0;

@@ -31,6 +31,7 @@ int64_t jacobi1d_effective_ctas();
 uint32_t take_heat_device_error();
 uint32_t take_batch_device_error();
 uint32_t take_cfd_device_error();
+uint32_t take_queue_device_error();
 int32_t launch_wait_timeout_selftest(uint64_t limit_ns, cudaStream_t st);
 
 int32_t set_error(int32_t code, const char* fmt, ...) {
@@ -147,7 +148,7 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       g_cfg_pdl = value;
       return NPBGB_OK;
     case NPBGB_CFG_BATCH_MODE:
-      if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "batch mode: 0, 1 or 2");
+      if (value < 0 || value > 3) return set_error(NPBGB_ERR_ARG, "batch mode: 0, 1, 2 or 3");
       g_cfg_batch_mode = value;
       return NPBGB_OK;
     case NPBGB_CFG_HDIFF_EMU:
@@ -197,11 +198,14 @@ int32_t npbgb_device_status(void* stream) {
   const uint32_t h = take_heat_device_error();
   const uint32_t bt = take_batch_device_error();
   const uint32_t cf = take_cfd_device_error();
-  if (h == 0xffffffffu || bt == 0xffffffffu || cf == 0xffffffffu)
+  const uint32_t qu = take_queue_device_error();
+  if (h == 0xffffffffu || bt == 0xffffffffu || cf == 0xffffffffu || qu == 0xffffffffu)
     return set_error(NPBGB_ERR_CUDA, "reading the device error words");
   if (h) return set_error(NPBGB_ERR_TIMEOUT, "a bounded device wait gave up (heat3d)");
   if (bt) return set_error(NPBGB_ERR_TIMEOUT, "a batch CTA made no progress within its limit");
   if (cf) return set_error(NPBGB_ERR_TIMEOUT, "a cavity_flow band waited on its neighbours past its limit");
+  if (qu & 1u) return set_error(NPBGB_ERR_TIMEOUT, "a queue worker saw no tile complete within its limit");
+  if (qu) return set_error(NPBGB_ERR_STATE, "a queue worker found an invalid inbox entry");
   return NPBGB_OK;
 }
 

@@ -1,0 +1,83 @@
+// Shapes shared by the device-side tile work queue (queue.cu) and the batch
+// planner (batch.cu).
+#pragma once
+
+#include <cstdint>
+
+#include "npbgb_common.cuh"
+
+namespace npbgb {
+namespace qdev {
+
+constexpr uint32_t kSeqEmpty = 0xffffffffu;
+
+// One grid's residency in the queue (64 bytes, copied word by word).
+struct QSlot {
+  void* a;            // first source for even step0
+  void* b;
+  int32_t n0, n1, n2;
+  int16_t kind, dtype;
+  int32_t step0;      // half-sweeps already applied (parity of the first source)
+  int32_t total;      // half-sweeps to perform in this residency (>= 1)
+  int32_t ntiles;     // tiles per half-sweep
+  int32_t chunk;      // rows (Jacobi-2D) or planes (Heat-3D) per tile
+  int32_t tx, ty;     // tiles along the contiguous axis; along axis 1 (Heat-3D)
+  uint32_t gen;       // residency number, written to the completion word
+  int32_t pad;
+};
+static_assert(sizeof(QSlot) == 64, "QSlot is copied as eight 64-bit words");
+
+// One half-sweep of one grid.  seq == ring position once the entry is written.
+struct QSeg {
+  int32_t slot;
+  int32_t s;
+  int32_t ntiles;
+  uint32_t seq;
+};
+
+struct QState {
+  uint32_t head;        // ring position tiles are claimed from
+  uint32_t tail;        // next ring position to write
+  uint32_t active;      // grids taken in and not finished
+  uint32_t inbox_head;  // inbox entries taken in
+  uint32_t lock;        // inbox lock (activation and shutdown)
+  uint32_t shutdown;    // 1: every CTA leaves at its next idle moment
+  uint32_t error;       // bit 0: no tile completed within the limit; bit 1: bad inbox entry
+  uint32_t progress;    // tiles completed in this launch
+};
+
+struct QArgs {
+  QSlot* slots;                  // device slot table
+  QSeg* ring;
+  unsigned long long* claim;     // per ring entry: (position << 32) | tiles claimed
+  uint32_t* done;                // per slot: tiles completed in the residency
+  QState* st;
+  const QSlot* host_slots;       // descriptors of inbox entries
+  const int32_t* inbox;          // ring of slot indices
+  const uint32_t* inbox_ctl;     // [0] entries published, [1] closed
+  uint32_t* consumed_out;        // mirror of inbox_head for the host, or null
+  uint32_t* status_out;          // mirror of the error word for the host, or null
+  uint32_t* finished;            // per slot: gen of the last finished residency, or null
+  uint32_t ring_size, inbox_cap;
+  int32_t max_slots;
+  uint64_t idle_ns;              // end the launch after this long with nothing to do
+  int f64_emulation, hw_warps;
+  uint32_t one;                  // == 1 (keeps constant folding out of the fixed-point adds)
+};
+
+}  // namespace qdev
+
+namespace qhost {
+
+// A batch run as one queue launch: every grid's first half-sweep is in the
+// ring from the start and the inbox is empty and closed.
+struct StaticQueue;
+
+int32_t plan_static(const npbgb_grid* grids, int64_t count, int32_t tile_rows, int32_t ctas_per_sm,
+                    StaticQueue** out, int64_t* updates, int64_t* tiles);
+int32_t launch_static(StaticQueue* s, cudaStream_t st);
+void free_static(StaticQueue* s);
+int static_ctas(const StaticQueue* s);
+
+}  // namespace qhost
+}  // namespace npbgb

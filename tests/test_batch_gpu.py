@@ -1,8 +1,9 @@
 """Batched launches == per-grid launches == the oracle, on the GPU.
 
-Every test runs twice: with the batch forced into its persistent form (one
-cooperative launch, neighbour counters) and into its stepped form (one chained
-launch per half-sweep index), which must leave the same bits.
+Every test runs three times: with the batch forced into its persistent form
+(one cooperative launch, neighbour counters), into its stepped form (one
+chained launch per half-sweep index) and into its queue form (one launch of the
+device-side tile work queue), which must all leave the same bits.
 """
 import numpy as np
 import pytest
@@ -21,8 +22,9 @@ from oracle import cref  # noqa: E402
 DEV = torch.device("cuda", 0)
 
 
-@pytest.fixture(autouse=True, params=[_lib.NPBGB_BATCH_PERSISTENT, _lib.NPBGB_BATCH_STEPPED],
-                ids=["persistent", "stepped"])
+@pytest.fixture(autouse=True, params=[_lib.NPBGB_BATCH_PERSISTENT, _lib.NPBGB_BATCH_STEPPED,
+                                      _lib.NPBGB_BATCH_QUEUE],
+                ids=["persistent", "stepped", "queue"])
 def batch_mode(request):
     old = _lib.set_config(_lib.NPBGB_CFG_BATCH_MODE, request.param)
     yield request.param
@@ -162,7 +164,8 @@ def test_batch_reports_its_form(batch_mode):
     B = A.clone()
     with Batch([(A, B, 5)]) as bt:
         info = bt.info()
-    assert info["mode"] == ("stepped" if batch_mode == _lib.NPBGB_BATCH_STEPPED else "persistent")
+    assert info["mode"] == {_lib.NPBGB_BATCH_STEPPED: "stepped",
+                            _lib.NPBGB_BATCH_QUEUE: "queue"}.get(batch_mode, "persistent")
     assert info["updates"] == 8 * 38 * 48
 
 
@@ -170,7 +173,7 @@ def test_batch_form_can_be_chosen_per_batch(batch_mode):
     """Batch(..., mode=...) overrides the configured form for that plan only."""
     A = torch.rand((40, 50), dtype=torch.float32, device=DEV)
     B = A.clone()
-    for name in ("persistent", "stepped"):
+    for name in ("persistent", "stepped", "queue"):
         with Batch([(A, B, 3)], mode=name) as bt:
             assert bt.info()["mode"] == name
             bt.replan([(A, B, 4)], mode=name)
