@@ -64,8 +64,9 @@ extern "C" {
 #define NPBGB_CFG_JACOBI_HW_WARPS 8 /* jacobi2d / batch binary64: warps per CTA (of 8)
                                        that use hardware binary64 next to the
                                        fixed-point warps; -1 (default) = 4 */
-#define NPBGB_CFG_BATCH_CTAS_PER_SM 9 /* persistent batch kernel: 2 or 3 (default)
-                                         CTAs per SM (read when a batch is planned) */
+#define NPBGB_CFG_BATCH_CTAS_PER_SM 9 /* persistent and queue batch kernels: 2, 3
+                                         (default) or 4 CTAs per SM (the persistent form
+                                         uses 3 for 4); read when a batch is planned */
 #define NPBGB_CFG_PDL 10              /* 1 (default): the per-half-sweep launches of the
                                          time loops use programmatic dependent launch;
                                          0: plain stream order */
@@ -117,6 +118,11 @@ typedef struct npbgb_grid {
                         (32 rows for Jacobi-2D, 8 planes for Heat-3D) */
   int32_t step0;     /* half-sweeps already applied (0 = start of the run) */
   int32_t nsteps;    /* half-sweeps to perform now; 0 = all remaining */
+  void* a32;         /* queue forms only, else NULL: binary32 arrays of a grid run in
+                        binary64 (dtype NPBGB_F64, a and b the binary64 pair).  Before
+                        the first half-sweep a32/b32 are widened exactly into a/b; after
+                        the last, a/b are rounded to nearest back into a32/b32. */
+  void* b32;
 } npbgb_grid;
 
 typedef struct npbgb_batch npbgb_batch;

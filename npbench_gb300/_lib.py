@@ -47,7 +47,7 @@ class Grid(ctypes.Structure):
                 ("n1", ctypes.c_int64), ("n2", ctypes.c_int64), ("kind", ctypes.c_int32),
                 ("dtype", ctypes.c_int32), ("tsteps", ctypes.c_int32),
                 ("band_rows", ctypes.c_int32), ("step0", ctypes.c_int32),
-                ("nsteps", ctypes.c_int32)]
+                ("nsteps", ctypes.c_int32), ("a32", ctypes.c_void_p), ("b32", ctypes.c_void_p)]
 
 
 # Every symbol include/npbgb.h declares, with its ctypes signature.

@@ -6,7 +6,10 @@
 
 Batches of 2^24 cells or more run in the stepped form (one chained launch per
 half-sweep over all grids still active), smaller ones in the persistent form;
-NPBGB_CFG_BATCH_MODE forces either.  Every entry (A, B, TSTEPS) is a pair of CUDA tensors of one dtype (float32 or
+``mode="queue"`` runs the batch as one launch of the device-side tile work
+queue, and NPBGB_CFG_BATCH_MODE or ``mode`` forces any form.  ``guard=True``
+runs float32 grids whose float32 error would exceed NPBench's bound in float64
+(queue form).  Every entry (A, B, TSTEPS) is a pair of CUDA tensors of one dtype (float32 or
 float64) with its own step count: 2D pairs are Jacobi-2D grids, 3D pairs
 Heat-3D grids.  After a launch each pair holds what ``kernel(TSTEPS, A, B)``
 of polybench/jacobi_2d/jacobi_2d_numpy.py:4-10 or
@@ -41,10 +44,19 @@ def _planned(mode, fn):
 
 
 class Batch:
-    def __init__(self, grids, band_rows=0, band_rows_of=None, mode=None):
+    def __init__(self, grids, band_rows=0, band_rows_of=None, mode=None, guard=False):
         """grids: iterable of (A, B, TSTEPS); band_rows_of(A) may pick rows per band;
-        mode: None (by size), "persistent" or "stepped"."""
+        mode: None (by size), "persistent", "stepped" or "queue".
+
+        guard=True applies the float64 guard (``npbench_gb300.precision``): a
+        float32 grid whose float32 error is predicted above NPBench's bound runs
+        in float64 (widened exactly, rounded back once at the end), which needs
+        the queue form; the batch then takes it."""
         self._h = None
+        self.guard = bool(guard)
+        self.promoted = 0
+        if self.guard:
+            mode = self._guard_mode(grids, mode)
         arr = self._structs(grids, band_rows_of)
         h = ctypes.c_void_p()
         _planned(mode, lambda: _lib.check(
@@ -56,14 +68,31 @@ class Batch:
         """Re-plan this batch for a new grid list, reusing its device buffers."""
         if self._h is None:
             raise RuntimeError("batch destroyed")
+        if self.guard:
+            mode = self._guard_mode(grids, mode)
         arr = self._structs(grids, band_rows_of)
         _planned(mode, lambda: _lib.check(
             _lib.load().npbgb_batch_replan(self._h, arr, len(grids), int(band_rows)),
             "npbgb_batch_replan"))
 
+    def _promote(self, A, entry):
+        import torch
+        from . import precision
+        if not self.guard or A.dtype != torch.float32:
+            return False
+        return precision.needs_fp64("jacobi2d" if A.dim() == 2 else "heat3d", int(entry[2]))
+
+    def _guard_mode(self, grids, mode):
+        if any(self._promote(e[0], e) for e in grids):
+            if mode not in (None, "auto", "queue"):
+                raise ValueError("float32 grids promoted to float64 need the queue form")
+            return "queue"
+        return mode
+
     def _structs(self, grids, band_rows_of):
         import torch
         self._keep = []
+        self.promoted = 0
         arr = (_lib.Grid * max(1, len(grids)))()
         for n, entry in enumerate(grids):
             A, B, T = entry[:3]
@@ -95,6 +124,15 @@ class Batch:
             g.tsteps = int(T)
             g.band_rows = int(band_rows_of(A)) if band_rows_of else 0
             self._keep.append((A, B))
+            if self._promote(A, entry):
+                # run in float64: the queue widens A/B into this pair and rounds back
+                A64 = torch.empty(A.shape, dtype=torch.float64, device=A.device)
+                B64 = torch.empty_like(A64)
+                g.a, g.b = A64.data_ptr(), B64.data_ptr()
+                g.a32, g.b32 = A.data_ptr(), B.data_ptr()
+                g.dtype = _lib.NPBGB_F64
+                self._keep.append((A64, B64))
+                self.promoted += 1
         self.device = self._keep[0][0].device if self._keep else None
         return arr
 

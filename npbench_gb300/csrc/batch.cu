@@ -326,6 +326,10 @@ int32_t plan_grid(const npbgb_grid& G, int64_t g, int32_t band_rows, int first, 
     return set_error(NPBGB_ERR_ARG, "batch: grid %lld: bad extents", (long long)g);
   if (G.step0 < 0 || G.nsteps < 0)
     return set_error(NPBGB_ERR_ARG, "batch: grid %lld: negative step0 or nsteps", (long long)g);
+  if (G.a32 || G.b32)
+    return set_error(NPBGB_ERR_ARG,
+                     "batch: grid %lld: binary32 arrays for a binary64 run need the queue form",
+                     (long long)g);
   const int64_t total = G.tsteps > 1 ? 2 * int64_t(G.tsteps - 1) : 0;
   int64_t todo = total - G.step0;
   if (G.nsteps > 0 && G.nsteps < todo) todo = G.nsteps;
@@ -511,6 +515,36 @@ int32_t plan_into(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int32_
   using namespace npbgb;
   if (count < 0 || (count > 0 && !grids)) return set_error(NPBGB_ERR_ARG, "batch: bad grid list");
   if (band_rows < 0) return set_error(NPBGB_ERR_ARG, "batch: band_rows < 0");
+  int64_t cells = 0;
+  for (int64_t g = 0; g < count; ++g) {
+    const npbgb_grid& G = grids[g];
+    cells += int64_t(G.n0) * G.n1 * (G.kind == NPBGB_KIND_HEAT3D ? G.n2 : 1);
+  }
+  const int32_t mode = g_cfg_batch_mode != 0
+                           ? int32_t(g_cfg_batch_mode)
+                           : (cells >= kSteppedCells ? NPBGB_BATCH_STEPPED : NPBGB_BATCH_PERSISTENT);
+  if (mode == NPBGB_BATCH_QUEUE) {
+    // The queue planner validates the grids itself (it also takes binary32
+    // arrays of grids run in binary64).
+    qhost::StaticQueue* sq = nullptr;
+    int64_t qup = 0, qtiles = 0;
+    const int32_t r = qhost::plan_static(grids, count, band_rows, int(g_cfg_batch_ctas_per_sm),
+                                         &sq, &qup, &qtiles);
+    if (r != NPBGB_OK) return r;
+    if (b->graph) {
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
+    qhost::free_static(b->sq);
+    b->sq = sq;
+    b->mode = NPBGB_BATCH_QUEUE;
+    b->launch_tiles.clear();
+    b->ntiles = qtiles;
+    b->nbands = qtiles;  // "nothing to do" checks use nbands
+    b->nctas = qhost::static_ctas(b->sq);
+    b->updates = qup;
+    return NPBGB_OK;
+  }
   std::vector<BandDesc> bands;
   int64_t updates = 0;
   for (int64_t g = 0; g < count; ++g) {
@@ -525,30 +559,9 @@ int32_t plan_into(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int32_
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
   }
-  int64_t cells = 0;
-  for (int64_t g = 0; g < count; ++g) {
-    const npbgb_grid& G = grids[g];
-    cells += int64_t(G.n0) * G.n1 * (G.kind == NPBGB_KIND_HEAT3D ? G.n2 : 1);
-  }
-  const int32_t mode = g_cfg_batch_mode != 0
-                           ? int32_t(g_cfg_batch_mode)
-                           : (cells >= kSteppedCells ? NPBGB_BATCH_STEPPED : NPBGB_BATCH_PERSISTENT);
   qhost::free_static(b->sq);
   b->sq = nullptr;
   if (mode == NPBGB_BATCH_STEPPED) return plan_stepped(b, grids, count, band_rows, updates);
-  if (mode == NPBGB_BATCH_QUEUE) {
-    int64_t qup = 0, qtiles = 0;
-    const int32_t r = qhost::plan_static(grids, count, band_rows, int(g_cfg_batch_ctas_per_sm),
-                                         &b->sq, &qup, &qtiles);
-    if (r != NPBGB_OK) return r;
-    b->mode = NPBGB_BATCH_QUEUE;
-    b->launch_tiles.clear();
-    b->ntiles = qtiles;
-    b->nbands = qtiles;  // "nothing to do" checks use nbands
-    b->nctas = qhost::static_ctas(b->sq);
-    b->updates = qup;
-    return NPBGB_OK;
-  }
   b->mode = NPBGB_BATCH_PERSISTENT;
   b->launch_tiles.clear();
   int per_sm = 0;

@@ -140,7 +140,7 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       g_cfg_jacobi_hw_warps = value;
       return NPBGB_OK;
     case NPBGB_CFG_BATCH_CTAS_PER_SM:
-      if (value != 2 && value != 3) return set_error(NPBGB_ERR_ARG, "batch CTAs per SM: 2 or 3");
+      if (value < 2 || value > 4) return set_error(NPBGB_ERR_ARG, "batch CTAs per SM: 2, 3 or 4");
       g_cfg_batch_ctas_per_sm = value;
       return NPBGB_OK;
     case NPBGB_CFG_PDL:

@@ -273,7 +273,7 @@ __device__ void complete_tile(const QArgs& q, int32_t slot, int32_t s, const QSl
   const uint32_t old = atom_add_acq_rel(&q.done[slot], 1u);
   atomicAdd(&q.st->progress, 1u);
   if (old + 1u == uint32_t(s + 1) * uint32_t(G.ntiles)) {
-    if (s + 1 < G.total) {
+    if (s + 1 < G.steps) {
       produce(q, slot, s + 1, G.ntiles);
     } else {
       if (q.finished) st_rel_sys(&q.finished[slot], G.gen);
@@ -294,8 +294,37 @@ __device__ __forceinline__ void heat_tile(const QSlot& G, const void* src, void*
                                   reinterpret_cast<hcore::PlaneBuf<T, FX>&>(plane));
 }
 
-__device__ __forceinline__ void sweep_tile(const QArgs& q, const QSlot& G, int32_t s, int32_t tile,
+// Tile `tile` of a conversion segment: a contiguous share of both arrays,
+// binary32 -> binary64 (exact) or binary64 -> binary32 (round to nearest even).
+__device__ __forceinline__ void convert_tile(const QSlot& G, int32_t tile, bool widen) {
+  const int64_t per = (G.cells + G.ntiles - 1) / G.ntiles;
+  const int64_t i0 = int64_t(tile) * per;
+  const int64_t i1 = min(i0 + per, G.cells);
+  double* a = static_cast<double*>(G.a);
+  double* b = static_cast<double*>(G.b);
+  float* a32 = static_cast<float*>(G.a32);
+  float* b32 = static_cast<float*>(G.b32);
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    if (widen) {
+      __stcg(a + i, double(__ldcg(a32 + i)));
+      __stcg(b + i, double(__ldcg(b32 + i)));
+    } else {
+      __stcg(a32 + i, __double2float_rn(__ldcg(a + i)));
+      __stcg(b32 + i, __double2float_rn(__ldcg(b + i)));
+    }
+  }
+}
+
+__device__ __forceinline__ void sweep_tile(const QArgs& q, const QSlot& G, int32_t seg, int32_t tile,
                                            hcore::PlaneBuf<double, true>& plane) {
+  int32_t s = seg;  // half-sweep index
+  if (G.conv) {
+    if (seg == 0 || seg == G.steps - 1) {
+      convert_tile(G, tile, seg == 0);
+      return;
+    }
+    s = seg - 1;
+  }
   const bool odd = ((G.step0 + s) & 1) != 0;
   const void* src = odd ? G.b : G.a;
   void* dst = odd ? G.a : G.b;
@@ -404,6 +433,12 @@ int32_t describe(const npbgb_grid& G, int64_t g, int32_t tile_rows, int32_t tile
   if (todo <= 0 || G.n0 < 3 || G.n1 < 3 || (heat && n2 < 3)) return NPBGB_OK;  // total = 0
   if (!G.a || !G.b || G.a == G.b)
     return set_error(NPBGB_ERR_ARG, "queue: grid %lld: null or aliased arrays", (long long)g);
+  const bool conv = G.a32 || G.b32;
+  if (conv && (!G.a32 || !G.b32 || G.a32 == G.b32 || G.dtype != NPBGB_F64 || G.a32 == G.a ||
+               G.a32 == G.b || G.b32 == G.a || G.b32 == G.b))
+    return set_error(NPBGB_ERR_ARG,
+                     "queue: grid %lld: binary32 arrays need a binary64 grid and two distinct arrays",
+                     (long long)g);
   out->a = G.a;
   out->b = G.b;
   out->n0 = int32_t(G.n0);
@@ -411,8 +446,13 @@ int32_t describe(const npbgb_grid& G, int64_t g, int32_t tile_rows, int32_t tile
   out->n2 = int32_t(n2);
   out->kind = int16_t(G.kind);
   out->dtype = int16_t(G.dtype);
+  out->a32 = G.a32;
+  out->b32 = G.b32;
   out->step0 = G.step0;
   out->total = int32_t(todo);
+  out->conv = conv ? 1 : 0;
+  out->steps = int32_t(todo) + (conv ? 2 : 0);
+  out->cells = G.n0 * G.n1 * n2;
   int64_t ntiles;
   if (heat) {
     const int32_t c = G.band_rows > 0 ? G.band_rows : (tile_planes > 0 ? tile_planes : 16);
@@ -427,7 +467,7 @@ int32_t describe(const npbgb_grid& G, int64_t g, int32_t tile_rows, int32_t tile
     out->ty = 1;
     ntiles = int64_t(out->tx) * cdiv(G.n0 - 2, c);
   }
-  if (ntiles * todo >= (int64_t(1) << 32))
+  if (ntiles * (todo + 2) >= (int64_t(1) << 32))
     return set_error(NPBGB_ERR_ARG, "queue: grid %lld: more than 2^32 tiles in one run", (long long)g);
   out->ntiles = int32_t(ntiles);
   *updates = todo * (G.n0 - 2) * (G.n1 - 2) * (heat ? (n2 - 2) : 1);
@@ -755,12 +795,12 @@ int32_t plan_static(const npbgb_grid* grids, int64_t count, int32_t tile_rows, i
     d.gen = 1;
     slots.push_back(d);
     *updates += up;
-    *tiles += int64_t(d.ntiles) * d.total;
+    *tiles += int64_t(d.ntiles) * d.steps;
   }
   if (slots.size() > (1u << 24)) return set_error(NPBGB_ERR_NOMEM, "queue: too many grids");
   // Longest runs first: their half-sweeps chain the longest.
   std::stable_sort(slots.begin(), slots.end(), [](const qdev::QSlot& x, const qdev::QSlot& y) {
-    return int64_t(x.total) * x.ntiles > int64_t(y.total) * y.ntiles;
+    return int64_t(x.steps) * x.ntiles > int64_t(y.steps) * y.ntiles;
   });
   auto* s = new (std::nothrow) StaticQueue();
   if (!s) return set_error(NPBGB_ERR_NOMEM, "queue: host allocation");

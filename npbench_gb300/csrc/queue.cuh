@@ -11,21 +11,30 @@ namespace qdev {
 
 constexpr uint32_t kSeqEmpty = 0xffffffffu;
 
-// One grid's residency in the queue (64 bytes, copied word by word).
+// One grid's residency in the queue (128 bytes, copied word by word).  Its
+// segments are numbered 0 .. steps-1: with `conv`, segment 0 widens a32/b32
+// into a/b, segments 1 .. total are the half-sweeps and the last one rounds
+// a/b back into a32/b32; without it, segment s is half-sweep s.
 struct QSlot {
   void* a;            // first source for even step0
   void* b;
+  void* a32;          // binary32 arrays of a grid run in binary64 (conv), else null
+  void* b32;
   int32_t n0, n1, n2;
   int16_t kind, dtype;
   int32_t step0;      // half-sweeps already applied (parity of the first source)
   int32_t total;      // half-sweeps to perform in this residency (>= 1)
-  int32_t ntiles;     // tiles per half-sweep
+  int32_t ntiles;     // tiles per segment
   int32_t chunk;      // rows (Jacobi-2D) or planes (Heat-3D) per tile
   int32_t tx, ty;     // tiles along the contiguous axis; along axis 1 (Heat-3D)
   uint32_t gen;       // residency number, written to the completion word
-  int32_t pad;
+  int32_t steps;      // segments: total, plus 2 with conv
+  int32_t conv;
+  int32_t pad0;
+  int64_t cells;      // elements per array
+  int64_t pad1[4];
 };
-static_assert(sizeof(QSlot) == 64, "QSlot is copied as eight 64-bit words");
+static_assert(sizeof(QSlot) == 128, "QSlot is copied as sixteen 64-bit words");
 
 // One half-sweep of one grid.  seq == ring position once the entry is written.
 struct QSeg {

@@ -14,11 +14,15 @@ The prediction comes from ``fp32_error_model.json``, measured on the GPU by
 ``python -m npbench_gb300.precision --calibrate``: for each kind and a range of
 grid sizes, the relative L2 error of float32 against float64 runs of the same
 U[0,1) inputs (the float32 inputs are the float64 draw rounded) at TSTEPS from
-2 to 2000.  ``predicted_rel_l2`` takes, over the calibrated sizes, the largest
-error at the nearest calibrated TSTEPS at or above the request's (a step
-function from above: the error is non-decreasing in TSTEPS over the calibrated
-range), and beyond the last calibrated TSTEPS extrapolates the last segment's
-power law.  ``needs_fp64`` compares it, times a safety factor, with the bound.
+2 to 2000.  ``predicted_rel_l2`` takes the largest error over the calibrated
+sizes at each calibrated TSTEPS, interpolates linearly in log-log between
+them, and beyond the last calibrated TSTEPS carries the last segment's power
+law on.  ``needs_fp64`` compares it, times a safety factor, with the bound.
+
+Measured on GB300: Jacobi-2D grows about linearly, 4.5e-6 at TSTEPS=100 and
+4.6e-5 at 1000, nearly independent of the grid size (128^2 to 4096^2), so
+float32 Jacobi-2D runs above about TSTEPS=110 run in float64; Heat-3D stays
+below 3.5e-6 up to TSTEPS=2000 and always runs in float32.
 """
 import argparse
 import json
@@ -57,15 +61,17 @@ def predicted_rel_l2(kind, tsteps):
         return 0.0
     m = model()[_kind(kind)]
     ts = m["tsteps"]
-    worst = [max(row) for row in m["rel_l2"]]
-    for t, e in zip(ts, worst):
-        if tsteps <= t:
-            return float(e)
-    # beyond the table: the last segment's growth rate, carried on
-    t0, t1 = ts[-2], ts[-1]
-    e0, e1 = max(worst[-2], 1e-30), max(worst[-1], 1e-30)
-    slope = max(0.0, math.log(e1 / e0) / math.log(t1 / t0))
-    return float(e1 * (tsteps / t1) ** slope)
+    worst = [max(max(row), 1e-30) for row in m["rel_l2"]]
+    if tsteps <= ts[0]:
+        return float(worst[0])
+    k = 1
+    while k < len(ts) - 1 and tsteps > ts[k]:
+        k += 1
+    t0, t1, e0, e1 = ts[k - 1], ts[k], worst[k - 1], worst[k]
+    slope = math.log(e1 / e0) / math.log(t1 / t0)
+    if tsteps > t1:
+        slope = max(0.0, slope)  # beyond the table: no decrease assumed
+    return float(e0 * (tsteps / t0) ** slope)
 
 
 def needs_fp64(kind, tsteps, bound=BOUND, safety=SAFETY):

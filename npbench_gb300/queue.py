@@ -40,8 +40,12 @@ class TileQueue:
         self._keep = {}
         self._buf = (ctypes.c_int32 * self.max_slots)()
 
-    def submit(self, A, B, tsteps, step0=0, nsteps=0, band_rows=0):
-        """Queue one grid; returns its slot, or -1 if it has nothing to do."""
+    def submit(self, A, B, tsteps, step0=0, nsteps=0, band_rows=0, a32=None, b32=None):
+        """Queue one grid; returns its slot, or -1 if it has nothing to do.
+
+        With ``a32``/``b32`` (float32 tensors of A's shape), A and B are a
+        float64 pair: the queue widens a32/b32 into them, runs the grid in
+        float64 and rounds the result back into a32/b32."""
         import torch
         if self._h is None:
             raise RuntimeError("queue destroyed")
@@ -71,11 +75,25 @@ class TileQueue:
         g.tsteps = int(tsteps)
         g.band_rows = int(band_rows)
         g.step0, g.nsteps = int(step0), int(nsteps)
+        keep = (A, B)
+        if a32 is not None or b32 is not None:
+            if a32 is None or b32 is None:
+                raise ValueError("give both a32 and b32")
+            for x in (a32, b32):
+                if (not isinstance(x, torch.Tensor) or x.dtype != torch.float32 or
+                        x.shape != A.shape or x.device != self.device or not x.is_contiguous()):
+                    raise ValueError("a32/b32 must be contiguous float32 tensors of A's shape "
+                                     "on the queue's device")
+            if A.dtype != torch.float64:
+                raise TypeError("a grid with float32 arrays runs in float64: A and B must be "
+                                "float64")
+            g.a32, g.b32 = a32.data_ptr(), b32.data_ptr()
+            keep = (A, B, a32, b32)
         slot = ctypes.c_int32(-1)
         _lib.check(_lib.load().npbgb_queue_submit(self._h, ctypes.byref(g), ctypes.byref(slot)),
                    "npbgb_queue_submit")
         if slot.value >= 0:
-            self._keep[slot.value] = (A, B)
+            self._keep[slot.value] = keep
         return slot.value
 
     def kick(self, stream=None):

@@ -5,29 +5,35 @@ polybench/jacobi_2d/jacobi_2d_numpy.py:4-10 (2D) or
 polybench/heat_3d/heat_3d_numpy.py:4-20 (3D), in float32 or float64, with its
 own size and step count.
 
-Scheduling is iteration-level continuous batching:
+Requests flow through four stages, each advanced by the serving thread
+without ever waiting for the GPU:
 
-* ``submit`` queues a request and returns a ``concurrent.futures.Future``;
-* the serving thread admits queued requests, oldest first, while their two
-  device arrays fit in the HBM budget (``AdmissionController``).  Their grids
-  stay resident on the device until they finish;
-* each round advances every resident grid below ``direct_cells`` interior
-  points by up to ``quantum`` half-sweeps in ONE persistent batch launch
-  (``npbench_gb300.batch``, libnpbgb's ``npbgb_batch_*``; the batch is
-  re-planned each round, not re-allocated), so their work overlaps on the
-  device without a launch per grid;
-* larger grids fill the GPU on their own: each round also gives the resident
-  large grid with the least remaining work (shortest remaining work first,
-  which keeps latency low for short requests) a slice of about
-  ``round_updates`` lattice updates with the single-grid kernels (TMA
-  pipelines);
-* finished grids are copied back, their memory is released, and requests that
-  arrived meanwhile are admitted for the next round.
+* **admission**: queued requests are admitted oldest first while their device
+  arrays fit in the HBM budget (``AdmissionController``); their arrays are
+  allocated and their inputs uploaded on a copy stream (an event marks the
+  upload done);
+* **folding**: an uploaded grid is handed to the device-side tile work queue
+  (``npbench_gb300.queue``, libnpbgb's ``npbgb_queue_*``), whose persistent
+  worker kernel takes it in while it runs: its tiles interleave with those of
+  every other resident grid, whatever their sizes, kinds and precisions, and
+  its next half-sweep starts as soon as its own previous one is done;
+* **completion**: the worker writes a completion word to host memory when a
+  grid's last half-sweep is done; the serving thread polls those words;
+* **return**: results are copied back on the copy stream (or handed over as
+  device tensors), the budget is released and the future resolved.
 
-A grid advanced in rounds ends bit-identical to the same grid run alone (the
-batch kernel resumes runs exactly at ``step0``), which the tests check.
-``run_sequential`` is the comparator: the same requests, one at a time in
-arrival order, each with plain per-grid launches.
+Arrivals never wait for a round to end: the worker kernel keeps running while
+new grids are folded in, and ends by itself only when it has nothing left.
+
+**Float64 guard.**  A float32 request whose float32 error against float64 is
+predicted to exceed NPBench's acceptance bound (``npbench_gb300.precision``)
+runs in float64 on the GPU: the queue widens its float32 inputs exactly,
+sweeps in float64 and rounds the result to float32 once.  ``run_sequential``,
+the comparator (the same requests one at a time with plain per-grid launches,
+in arrival order), applies the same guard.
+
+A grid's result is the same alone and in the mix, bit for bit (the tests check
+it): the queue applies the same arithmetic in the same order per point.
 """
 import collections
 import concurrent.futures
@@ -38,10 +44,10 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import _lib, stencils
-from .batch import Batch
+from . import _lib, precision, stencils
 
-__all__ = ["AdmissionController", "Request", "StencilServer", "run_sequential", "latency_stats"]
+__all__ = ["AdmissionController", "Request", "StencilServer", "run_sequential", "latency_stats",
+           "guarded"]
 
 
 class AdmissionController:
@@ -73,6 +79,12 @@ class AdmissionController:
             self.in_use -= nbytes
 
 
+def guarded(kind, dtype, tsteps, fp64_guard=True):
+    """True when a request of this kind, dtype and TSTEPS runs in float64 for accuracy."""
+    return (fp64_guard and np.dtype(dtype) == np.float32 and
+            precision.needs_fp64(kind, int(tsteps)))
+
+
 @dataclass
 class Request:
     """One solve.  Give host arrays ``a`` (and ``b`` for 2D), or a ``seed``
@@ -89,9 +101,9 @@ class Request:
     t_submit: float = 0.0
     t_admit: float = 0.0
     t_done: float = 0.0
-    half_sweeps: int = 0
-    done: int = 0
-    dev: tuple = None
+    promoted: bool = False
+    dev: dict = field(default=None, repr=False)
+    out: tuple = field(default=None, repr=False)
     future: concurrent.futures.Future = field(default=None, repr=False)
 
     @property
@@ -99,8 +111,15 @@ class Request:
         return "jacobi2d" if len(self.shape) == 2 else "heat3d"
 
     @property
+    def cells(self):
+        return int(np.prod(self.shape))
+
+    @property
     def nbytes(self):
-        return 2 * int(np.prod(self.shape)) * np.dtype(self.dtype).itemsize
+        """Device bytes while resident: the pair in the request's dtype, plus the
+        float64 pair of a promoted float32 request."""
+        n = 2 * self.cells * np.dtype(self.dtype).itemsize
+        return n + (2 * self.cells * 8 if self.promoted else 0)
 
     @property
     def updates(self):
@@ -122,60 +141,82 @@ def _validate(req):
             raise ValueError("Jacobi-2D requests need both A and B")
 
 
-def _materialise(req, device):
-    """Device arrays for an admitted request (allocation happens here)."""
+def _tdtype(dtype):
     import torch
-    tdt = torch.float64 if np.dtype(req.dtype) == np.float64 else torch.float32
-    if req.a is not None:
-        A = torch.from_numpy(np.ascontiguousarray(req.a, dtype=req.dtype)).to(device)
-        B = (torch.from_numpy(np.ascontiguousarray(req.b, dtype=req.dtype)).to(device)
-             if req.b is not None else A.clone())
-    else:
-        g = torch.Generator(device=device)
-        g.manual_seed(int(req.seed))
-        A = torch.rand(req.shape, dtype=torch.float64, device=device, generator=g).to(tdt)
-        B = (torch.rand(req.shape, dtype=torch.float64, device=device, generator=g).to(tdt)
-             if len(req.shape) == 2 else A.clone())
+    return torch.float64 if np.dtype(dtype) == np.float64 else torch.float32
+
+
+def _materialise(req, device, stream=None):
+    """Device arrays (A, B) of a request in its dtype, inputs uploaded or drawn on
+    `stream` (default: the current stream)."""
+    import torch
+    tdt = _tdtype(req.dtype)
+    ctx = torch.cuda.stream(stream) if stream is not None else _nullctx()
+    with ctx:
+        if req.a is not None:
+            A = torch.empty(req.shape, dtype=tdt, device=device)
+            A.copy_(_host(req.a, req.dtype), non_blocking=True)
+            B = torch.empty_like(A)
+            B.copy_(_host(req.b if req.b is not None else req.a, req.dtype), non_blocking=True)
+        else:
+            g = torch.Generator(device=device)
+            g.manual_seed(int(req.seed))
+            A = torch.rand(req.shape, dtype=torch.float64, device=device, generator=g).to(tdt)
+            B = (torch.rand(req.shape, dtype=torch.float64, device=device, generator=g).to(tdt)
+                 if len(req.shape) == 2 else A.clone())
     return A, B
 
 
-class StencilServer:
-    """Serving thread with an HBM admission budget and continuous batching."""
+class _nullctx:
+    def __enter__(self):
+        return self
 
-    # Defaults from a sweep on GB300 with the served configuration (100 mixed
-    # requests, Poisson 1000 req/s): throughput equal to sequential per-request
-    # launches at about half their median latency.
-    def __init__(self, device=0, hbm_budget_bytes=150e9, quantum=64, band_rows=8,
-                 direct_cells=1 << 16, round_updates=8e9):
+    def __exit__(self, *exc):
+        return False
+
+
+def _host(x, dtype):
+    import torch
+    arr = np.ascontiguousarray(x, dtype=dtype)
+    t = torch.from_numpy(arr)
+    return t
+
+
+class StencilServer:
+    """Serving thread with an HBM admission budget, feeding the device-side tile queue."""
+
+    def __init__(self, device=0, hbm_budget_bytes=150e9, max_slots=4096, tile_rows=0,
+                 tile_planes=0, ctas_per_sm=0, idle_us=500, fp64_guard=True,
+                 reserve_bytes=8 << 30, poll_s=2e-4):
         import torch
-        self.device = torch.device("cuda", device) if isinstance(device, int) else device
+        self.device = torch.device("cuda", device) if isinstance(device, int) else \
+            torch.device(device)
         self.admission = AdmissionController(hbm_budget_bytes)
-        if quantum < 2 or quantum % 2:
-            raise ValueError("quantum must be an even number of half-sweeps >= 2")
-        self.quantum = int(quantum)
-        self.direct_cells = int(direct_cells)
-        self.round_updates = float(round_updates)
-        self.band_rows = int(band_rows)
-        self._batch = None
+        self.max_slots = int(max_slots)
+        self.tile_rows, self.tile_planes = int(tile_rows), int(tile_planes)
+        self.ctas_per_sm, self.idle_us = int(ctas_per_sm), int(idle_us)
+        self.fp64_guard = bool(fp64_guard)
+        self.reserve_bytes = int(min(reserve_bytes, hbm_budget_bytes))
+        self.poll_s = float(poll_s)
         self._queue = collections.deque()
-        self._active = []
         self._cv = threading.Condition()
         self._stop = False
         self._ids = itertools.count()
         self._thread = None
-        self.rounds = 0
         self.completed = []
         self.error = None
+        self.promoted = 0
+        self.launches = 0
 
     # -- client side ------------------------------------------------------
     def submit(self, req):
         _validate(req)
+        req.promoted = guarded(req.kind, req.dtype, req.tsteps, self.fp64_guard)
         if not self.admission.fits_ever(req.nbytes):
             raise ValueError(f"request needs {req.nbytes} bytes, above the HBM budget "
                              f"{self.admission.budget}")
         req.id = next(self._ids)
         req.t_submit = time.perf_counter()
-        req.half_sweeps = max(0, 2 * (req.tsteps - 1))
         req.future = concurrent.futures.Future()
         with self._cv:
             if self._stop:
@@ -211,114 +252,156 @@ class StencilServer:
         self.stop(drain=exc[0] is None)
 
     # -- serving thread ---------------------------------------------------
-    def _admit(self):
-        while self._queue:
-            req = self._queue[0]
-            if req.future.cancelled():
-                self._queue.popleft()
-                continue
-            if not self.admission.try_admit(req.nbytes):
-                break  # oldest first: later requests wait behind it
-            self._queue.popleft()
-            req.dev = _materialise(req, self.device)
-            req.t_admit = time.perf_counter()
-            if req.half_sweeps == 0:
-                self._finish(req)
-            else:
-                self._active.append(req)
-
-    def _finish(self, req):
+    def _upload(self, req):
+        """Allocates the request's device arrays and queues its input upload."""
         import torch
-        A, B = req.dev
+        A, B = _materialise(req, self.device, self._copy)
+        dev = {"A": A, "B": B}
+        if req.promoted:
+            with torch.cuda.stream(self._copy):
+                dev["A64"] = torch.empty(req.shape, dtype=torch.float64, device=self.device)
+                dev["B64"] = torch.empty(req.shape, dtype=torch.float64, device=self.device)
+        ev = torch.cuda.Event()
+        ev.record(self._copy)
+        req.dev = dev
+        return ev
+
+    def _fold(self, req):
+        """Hands an uploaded grid to the tile queue; returns its slot (-1: nothing to do)."""
+        d = req.dev
+        if req.promoted:
+            return self.tq.submit(d["A64"], d["B64"], req.tsteps, a32=d["A"], b32=d["B"])
+        return self.tq.submit(d["A"], d["B"], req.tsteps)
+
+    def _deliver(self, req):
+        """Starts returning a finished request's result; returns an event that marks it."""
+        import torch
+        A, B = req.dev["A"], req.dev["B"]
         if req.return_host:
-            torch.cuda.synchronize(self.device)
-            out = (A.cpu().numpy(), B.cpu().numpy())
+            with torch.cuda.stream(self._copy):
+                hA = torch.empty(A.shape, dtype=A.dtype, pin_memory=True)
+                hB = torch.empty(B.shape, dtype=B.dtype, pin_memory=True)
+                hA.copy_(A, non_blocking=True)
+                hB.copy_(B, non_blocking=True)
+            req.out = (hA, hB)
         else:
-            out = (A, B)
+            req.out = (A, B)
+        ev = torch.cuda.Event()
+        ev.record(self._copy)
+        return ev
+
+    def _resolve(self, req):
+        if req.return_host:
+            out = (req.out[0].numpy(), req.out[1].numpy())
+        else:
+            out = req.out
         req.dev = None
+        req.out = None
         self.admission.release(req.nbytes)
         req.t_done = time.perf_counter()
         self.completed.append(req)
         req.future.set_result(out)
 
-    @staticmethod
-    def _inner(r):
-        return int(np.prod([max(0, x - 2) for x in r.shape]))
-
-    def _round(self):
-        import torch
-        small, large = [], []
-        for r in self._active:
-            (large if self._inner(r) >= self.direct_cells else small).append(r)
-        advanced = {}
-        if small:
-            entries = [(r.dev[0], r.dev[1], r.tsteps, r.done, self.quantum) for r in small]
-            if self._batch is None:
-                self._batch = Batch(entries, band_rows=self.band_rows)
-            else:
-                self._batch.replan(entries, band_rows=self.band_rows)
-            self._batch.launch()
-            for r in small:
-                advanced[r.id] = min(self.quantum, r.half_sweeps - r.done)
-        if large:
-            r = min(large, key=lambda q: (q.half_sweeps - q.done) * self._inner(q))
-            n = int(self.round_updates // max(1, self._inner(r)))
-            n = max(2, min(r.half_sweeps - r.done, n - n % 2))
-            # done is even (every slice is even), so the next half-sweep reads A:
-            # kernel(n/2 + 1, A, B) performs exactly the next n half-sweeps.
-            A, B = r.dev
-            (stencils.jacobi_2d_kernel if A.dim() == 2 else stencils.heat_3d_kernel)(
-                n // 2 + 1, A, B)
-            advanced[r.id] = n
-        torch.cuda.current_stream(self.device).synchronize()
-        _lib.device_status()
-        self.rounds += 1
-        still = []
-        for r in self._active:
-            r.done = min(r.half_sweeps, r.done + advanced.get(r.id, 0))
-            if r.done >= r.half_sweeps:
-                self._finish(r)
-            else:
-                still.append(r)
-        self._active = still
-
     def _serve(self):
         import torch
+
+        from .queue import TileQueue
         torch.cuda.set_device(self.device)
+        self._copy = torch.cuda.Stream(self.device)
+        self._compute = torch.cuda.Stream(self.device)
+        if self.reserve_bytes > 0:
+            # One cached block for the copy stream's allocations: later arrays are
+            # carved out of it without a cudaMalloc while the worker runs.
+            with torch.cuda.stream(self._copy):
+                blk = torch.empty(self.reserve_bytes, dtype=torch.uint8, device=self.device)
+            del blk
+        self.tq = TileQueue(max_slots=self.max_slots, tile_rows=self.tile_rows,
+                            tile_planes=self.tile_planes, ctas_per_sm=self.ctas_per_sm,
+                            idle_us=self.idle_us, device=self.device)
+        waiting = collections.deque()
+        staging = []     # (request, upload event)
+        resident = {}    # slot -> request
+        returning = []   # (request, delivery event)
         try:
             while True:
                 with self._cv:
-                    while not self._queue and not self._active and not self._stop:
-                        self._cv.wait(timeout=0.05)
-                    if self._stop and not self._queue and not self._active:
+                    while self._queue:
+                        waiting.append(self._queue.popleft())
+                    if self._stop and not (waiting or staging or resident or returning):
                         return
-                    self._admit()
-                if self._active:
-                    self._round()
-                elif self._queue:
-                    # nothing resident and the oldest request does not fit: cannot happen
-                    # (fits_ever was checked at submit); back off briefly
-                    time.sleep(0.001)
+                moved = False
+                # admission, oldest first; later requests wait behind one that does not fit
+                while waiting:
+                    req = waiting[0]
+                    if req.future.cancelled():
+                        waiting.popleft()
+                        continue
+                    if not self.admission.try_admit(req.nbytes):
+                        break
+                    waiting.popleft()
+                    req.t_admit = time.perf_counter()
+                    self.promoted += int(req.promoted)
+                    staging.append((req, self._upload(req)))
+                    moved = True
+                # folding: uploaded grids into the running queue
+                still = []
+                for req, ev in staging:
+                    if not ev.query():
+                        still.append((req, ev))
+                        continue
+                    try:
+                        slot = self._fold(req)
+                    except _lib.NpbgbError as e:
+                        if e.status != _lib.NPBGB_ERR_NOMEM:
+                            raise
+                        still.append((req, ev))  # every slot busy: fold it later
+                        continue
+                    moved = True
+                    if slot < 0:
+                        returning.append((req, self._deliver(req)))
+                    else:
+                        resident[slot] = req
+                staging = still
+                if resident:
+                    self.tq.kick(self._compute)
+                    for slot in self.tq.poll():
+                        req = resident.pop(slot)
+                        returning.append((req, self._deliver(req)))
+                        moved = True
+                still = []
+                for req, ev in returning:
+                    if ev.query():
+                        self._resolve(req)
+                        moved = True
+                    else:
+                        still.append((req, ev))
+                returning = still
+                if not moved:
+                    with self._cv:
+                        if not self._queue and not self._stop:
+                            self._cv.wait(timeout=self.poll_s)
         except Exception as e:  # fail every outstanding request loudly
             self.error = e
             with self._cv:
-                pending = list(self._queue) + list(self._active)
+                pending = list(self._queue) + list(waiting) + [r for r, _ in staging] + \
+                    list(resident.values()) + [r for r, _ in returning]
                 self._queue.clear()
-                self._active = []
             for r in pending:
                 if not r.future.done():
                     r.future.set_exception(e)
         finally:
-            if self._batch is not None:
-                self._batch.close()
-                self._batch = None
+            try:
+                self.launches = self.tq.state()["launches"]
+            except Exception:
+                pass
+            self.tq.destroy()
 
 
-def run_sequential(requests, arrivals, device=0):
+def run_sequential(requests, arrivals, device=0, fp64_guard=True):
     """Comparator: the requests one at a time, in arrival order, each with plain
-    per-grid launches (``stencils.jacobi_2d_kernel`` / ``heat_3d_kernel``).
-    ``arrivals`` are offsets in seconds from the start.  Returns the requests
-    with t_submit/t_done filled in."""
+    per-grid launches (``stencils.jacobi_2d_kernel`` / ``heat_3d_kernel``), under
+    the same float64 guard as the server.  ``arrivals`` are offsets in seconds
+    from the start.  Returns the requests with t_submit/t_done filled in."""
     import torch
     dev = torch.device("cuda", device) if isinstance(device, int) else device
     t0 = time.perf_counter()
@@ -327,11 +410,21 @@ def run_sequential(requests, arrivals, device=0):
         if at > now:
             time.sleep(at - now)
         req.t_submit = t0 + at
+        req.promoted = guarded(req.kind, req.dtype, req.tsteps, fp64_guard)
         A, B = _materialise(req, dev)
-        (stencils.jacobi_2d_kernel if A.dim() == 2 else stencils.heat_3d_kernel)(req.tsteps, A, B)
+        fn = stencils.jacobi_2d_kernel if A.dim() == 2 else stencils.heat_3d_kernel
+        if req.promoted:
+            A64, B64 = A.double(), B.double()
+            fn(req.tsteps, A64, B64)
+            A.copy_(A64)
+            B.copy_(B64)
+            del A64, B64
+        else:
+            fn(req.tsteps, A, B)
         if req.return_host:
-            A.cpu()
-            B.cpu()
+            req.out = (A.cpu().numpy(), B.cpu().numpy())
+        else:
+            req.out = (A, B)
         torch.cuda.synchronize(dev)
         req.t_done = time.perf_counter()
     return requests

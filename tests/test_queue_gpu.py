@@ -147,3 +147,34 @@ def test_full_queue_refuses_with_a_status():
     for (A, B, _), (a, b, T) in zip(grids, dev):
         ra, rb = _oracle(A, B, T)
         assert bits_equal(a.cpu().numpy(), ra) and bits_equal(b.cpu().numpy(), rb)
+
+
+def test_batch_guard_promotes_long_float32_grids():
+    """Batch(guard=True): float32 Jacobi-2D grids above the calibrated float32 error
+    bound run in float64 and equal the float64 oracle rounded once; the others stay
+    float32, bit-identical to the float32 oracle; all are within 1e-5 of float64."""
+    from npbench_gb300.batch import Batch
+    rng = np.random.default_rng(21)
+    cases = [((200, 150), np.float32, 600), ((120, 90), np.float32, 30),
+             ((90, 70), np.float64, 300), ((20, 30, 24), np.float32, 300)]
+    host, dev = [], []
+    for shape, dt, T in cases:
+        A = rng.random(shape).astype(dt)
+        B = rng.random(shape).astype(dt) if len(shape) == 2 else A.copy()
+        host.append((A, B, T))
+        dev.append((torch.from_numpy(A).to(DEV), torch.from_numpy(B).to(DEV), T))
+    with Batch(dev, guard=True) as bt:
+        assert bt.promoted == 1 and bt.info()["mode"] == "queue"
+        bt.launch()
+        _lib.device_status()
+    for n, ((A, B, T), (a, b, _)) in enumerate(zip(host, dev)):
+        ga, gb = a.cpu().numpy(), b.cpu().numpy()
+        oa, ob = A.astype(np.float64), B.astype(np.float64)
+        (cref.jacobi_2d_kernel if A.ndim == 2 else cref.heat_3d_kernel)(T, oa, ob)
+        rel = np.linalg.norm(ga.astype(np.float64) - oa) / np.linalg.norm(oa)
+        assert rel <= 1e-5, (n, rel)
+        if n == 0:
+            assert np.array_equal(ga, oa.astype(np.float32)) and np.array_equal(gb, ob.astype(np.float32))
+        else:
+            ra, rb = _oracle(A, B, T)
+            assert bits_equal(ga, ra) and bits_equal(gb, rb), n

@@ -2,8 +2,11 @@
 
 The GPU test is the one the served configuration asks for: requests of mixed
 dimension, size, dtype and step count arrive while others run, are admitted as
-memory frees up under a small HBM budget, share persistent launches, and each
-result is bit-identical to the same request run alone.
+memory frees up under a small HBM budget, are folded into the running
+device-side tile queue, and each result is bit-identical to the same request
+run alone (under the same float64 guard).  The guard's own test runs a float32
+request above the calibrated error bound (promoted to float64) and one below
+it (kept float32), both within 1e-5 of the float64 oracle.
 """
 import threading
 import time
@@ -11,7 +14,8 @@ import time
 import numpy as np
 import pytest
 
-from npbench_gb300.server import AdmissionController
+from npbench_gb300 import precision
+from npbench_gb300.server import AdmissionController, guarded
 
 
 def test_admission_budget_and_peak():
@@ -46,6 +50,22 @@ def test_admission_is_thread_safe():
     assert sum(got) <= 1000 and a.in_use == sum(got)
 
 
+def test_float32_error_model_and_guard_threshold():
+    """The calibrated table: Jacobi-2D float32 error grows with TSTEPS and crosses the
+    bound (with its safety margin) between TSTEPS 100 and 200; Heat-3D never does."""
+    prev = 0.0
+    for T in (2, 10, 50, 100, 150, 200, 500, 1000, 3000):
+        e = precision.predicted_rel_l2("jacobi2d", T)
+        assert e >= prev
+        prev = e
+    assert not precision.needs_fp64("jacobi2d", 100) and precision.needs_fp64("jacobi2d", 200)
+    assert not any(precision.needs_fp64("heat3d", T) for T in (2, 100, 1000, 2000))
+    assert precision.predicted_rel_l2((10, 10), 1) == 0.0
+    assert guarded("jacobi2d", np.float32, 500) and not guarded("jacobi2d", np.float64, 500)
+    assert not guarded("jacobi2d", np.float32, 500, fp64_guard=False)
+    assert not guarded("heat3d", np.float32, 1000)
+
+
 def _requests(n, seed):
     from npbench_gb300.server import Request
     rng = np.random.default_rng(seed)
@@ -59,23 +79,43 @@ def _requests(n, seed):
             shape = tuple(int(x) for x in rng.integers(3, 40, 3))
             a = rng.random(shape).astype(dt)
             b = None
-        reqs.append(Request(shape=shape, dtype=dt, tsteps=int(rng.integers(0, 60)), a=a, b=b))
+        # 2D runs up to TSTEPS 200, so float32 ones above the error bound get promoted
+        T = int(rng.integers(0, 200 if i % 2 else 60))
+        reqs.append(Request(shape=shape, dtype=dt, tsteps=T, a=a, b=b))
     return reqs
 
 
+def _alone(r):
+    """The request run alone with per-grid launches, under the same float64 guard."""
+    import torch
+    from npbench_gb300 import stencils
+    a = torch.from_numpy(r.a).cuda()
+    b = torch.from_numpy(r.b if r.b is not None else r.a.copy()).cuda()
+    fn = stencils.jacobi_2d_kernel if a.dim() == 2 else stencils.heat_3d_kernel
+    if r.promoted:
+        a64, b64 = a.double(), b.double()
+        fn(r.tsteps, a64, b64)
+        a.copy_(a64)
+        b.copy_(b64)
+    else:
+        fn(r.tsteps, a, b)
+    return a.cpu().numpy(), b.cpu().numpy()
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("direct_cells,round_updates", [(1 << 20, 2e9), (600, 2e4)])
-def test_served_mix_equals_alone(direct_cells, round_updates):
+@pytest.mark.parametrize("tile_rows", [0, 5])
+def test_served_mix_equals_alone(tile_rows):
+    """Requests arrive from three client threads while others run, wait for
+    memory under a small budget, and each result equals the request run alone."""
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
-    from npbench_gb300 import stencils
     from npbench_gb300.server import StencilServer
     reqs = _requests(40, seed=3)
-    budget = max(r.nbytes for r in reqs) * 3  # small: forces waiting for memory
+    budget = max(2 * r.cells * 16 for r in reqs) * 3  # small: forces waiting for memory
     futures = []
-    with StencilServer(hbm_budget_bytes=budget, quantum=6, direct_cells=direct_cells,
-                       round_updates=round_updates) as srv:
+    with StencilServer(hbm_budget_bytes=budget, tile_rows=tile_rows, tile_planes=tile_rows,
+                       reserve_bytes=budget) as srv:
         def client(part):
             for r in part:
                 futures.append((r, srv.submit(r)))
@@ -86,14 +126,56 @@ def test_served_mix_equals_alone(direct_cells, round_updates):
         for t in ts:
             t.join()
         results = [(r, f.result(timeout=300)) for r, f in futures]
-    assert srv.admission.peak <= budget
-    assert srv.rounds > 1
+    assert srv.admission.peak <= budget and srv.admission.in_use == 0
+    assert srv.launches >= 1
     for r, (A, B) in results:
-        a = torch.from_numpy(r.a).cuda()
-        b = torch.from_numpy(r.b if r.b is not None else r.a.copy()).cuda()
-        (stencils.jacobi_2d_kernel if a.dim() == 2 else stencils.heat_3d_kernel)(r.tsteps, a, b)
-        assert np.array_equal(a.cpu().numpy(), A) and np.array_equal(b.cpu().numpy(), B), (
-            r.shape, r.dtype, r.tsteps)
+        a, b = _alone(r)
+        assert np.array_equal(a, A) and np.array_equal(b, B), (r.shape, r.dtype, r.tsteps)
+
+
+@pytest.mark.gpu
+def test_float64_guard_promotes_long_float32_runs():
+    """A float32 Jacobi-2D run above the calibrated error bound runs in float64
+    (and ends within 1e-5 of the float64 oracle, where plain float32 does not);
+    one below it stays float32 and is bit-identical to the float32 oracle."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from npbench_gb300 import precision
+    from npbench_gb300.server import Request, StencilServer, guarded
+    from oracle import cref
+    rng = np.random.default_rng(12)
+    A64, B64 = rng.random((300, 260)), rng.random((300, 260))
+    A32, B32 = A64.astype(np.float32), B64.astype(np.float32)
+    long_T, short_T = 900, 40
+    assert guarded("jacobi2d", np.float32, long_T) and not guarded("jacobi2d", np.float32, short_T)
+    assert precision.predicted_rel_l2("jacobi2d", long_T) > precision.BOUND
+    with StencilServer(hbm_budget_bytes=1 << 30, reserve_bytes=1 << 28) as srv:
+        f_long = srv.submit(Request(shape=A32.shape, dtype=np.float32, tsteps=long_T, a=A32, b=B32))
+        f_short = srv.submit(Request(shape=A32.shape, dtype=np.float32, tsteps=short_T, a=A32, b=B32))
+        (la, lb), (sa, sb) = f_long.result(timeout=120), f_short.result(timeout=120)
+    assert srv.promoted == 1
+    assert la.dtype == np.float32 and sa.dtype == np.float32
+
+    def rel(x, ref):
+        return float(np.linalg.norm(x.astype(np.float64) - ref) / np.linalg.norm(ref))
+    # float64 oracle of the float32 inputs (widened exactly)
+    for T, (ra, rb) in ((long_T, (la, lb)), (short_T, (sa, sb))):
+        oa, ob = A32.astype(np.float64), B32.astype(np.float64)
+        cref.jacobi_2d_kernel(T, oa, ob)
+        assert rel(ra, oa) <= 1e-5 and rel(rb, ob) <= 1e-5, T
+    # the promoted result is the float64 run rounded once
+    oa, ob = A32.astype(np.float64), B32.astype(np.float64)
+    cref.jacobi_2d_kernel(long_T, oa, ob)
+    assert np.array_equal(la, oa.astype(np.float32)) and np.array_equal(lb, ob.astype(np.float32))
+    # plain float32 would have missed the bound on the long run
+    pa, pb = A32.copy(), B32.copy()
+    cref.jacobi_2d_kernel(long_T, pa, pb)
+    assert rel(pa, oa) > 1e-5
+    # the short run stayed float32: bit-identical to the float32 oracle
+    qa, qb = A32.copy(), B32.copy()
+    cref.jacobi_2d_kernel(short_T, qa, qb)
+    assert np.array_equal(sa, qa) and np.array_equal(sb, qb)
 
 
 @pytest.mark.gpu
@@ -103,12 +185,12 @@ def test_server_rejects_oversized_and_cancels_on_stop():
         pytest.skip("no CUDA device")
     from npbench_gb300.server import Request, StencilServer
     big = Request(shape=(100, 100), dtype=np.float64, tsteps=5, seed=1)
-    srv = StencilServer(hbm_budget_bytes=big.nbytes - 1).start()
+    srv = StencilServer(hbm_budget_bytes=big.nbytes - 1, reserve_bytes=0).start()
     with pytest.raises(ValueError):
         srv.submit(big)
     srv.stop()
     # a long queue behind a budget that holds one grid; stop without draining cancels the rest
-    srv = StencilServer(hbm_budget_bytes=big.nbytes, quantum=2).start()
+    srv = StencilServer(hbm_budget_bytes=big.nbytes, reserve_bytes=0).start()
     futs = [srv.submit(Request(shape=(100, 100), dtype=np.float64, tsteps=400, seed=i))
             for i in range(6)]
     time.sleep(0.05)
