@@ -96,7 +96,6 @@ def parse():
                     help="batch/serve: also time the per-grid / sequential comparator")
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--rate", type=float, default=1000.0)
-    ap.add_argument("--quantum", type=int, default=64)
     return ap.parse_args()
 
 
@@ -825,11 +824,32 @@ def _fp32_error_report(pairs):
     return out
 
 
+BATCH_FORM = "queue"
+BATCH_TILE_ROWS = 128
+
+
+def _per_grid_guarded(work, guard):
+    """Plain per-grid launches of the batch's grids, under the same float64 guard:
+    a promoted float32 grid is widened, run in float64 and rounded back."""
+    import torch
+    from npbench_gb300 import precision, stencils
+    for a, b, T in work:
+        if guard and a.dtype == torch.float32 and precision.needs_fp64("jacobi2d", T):
+            a64, b64 = a.double(), b.double()
+            stencils.jacobi_2d_kernel(T, a64, b64)
+            a.copy_(a64)
+            b.copy_(b64)
+        else:
+            stencils.jacobi_2d_kernel(T, a, b)
+
+
 def batch_measure(n_grids=4096, steps=2, warmup=1, compare=True, compare_steps=1,
-                  compare_warmup=1, fp32_error=True, cpu=False):
+                  compare_warmup=1, fp32_error=True, cpu=False, guard=True, form=None,
+                  tile_rows=None):
     """Configuration 4: ``n_grids`` independent Jacobi-2D grids (sides log-uniform in
     [64, 2048] per axis, half float32 and half float64, TSTEPS uniform in [10, 500])
-    advanced by one batch per step.  Returns the measurement as a dict."""
+    advanced by one batch per step.  With ``guard`` the float32 grids whose float32
+    error would exceed 1e-5 run in float64 (both arms).  Returns the measurement."""
     import torch
     from npbench_gb300 import _lib, stencils, workloads
     from npbench_gb300.batch import Batch
@@ -851,10 +871,16 @@ def batch_measure(n_grids=4096, steps=2, warmup=1, compare=True, compare_steps=1
             a.copy_(a0)
             b.copy_(b0)
 
+    from npbench_gb300 import precision
+    form = form or BATCH_FORM
+    rows = tile_rows or BATCH_TILE_ROWS
+    promoted = [guard and dt == np.float32 and precision.needs_fp64("jacobi2d", T)
+                for _, dt, T in specs]
     ups = sum(2 * (T - 1) * (s[0] - 2) * (s[1] - 2) for s, _, T in specs)
-    alg = sum(2 * (T - 1) * (s[0] - 2) * (s[1] - 2) * 2 * np.dtype(dt).itemsize
-              for s, dt, T in specs)
-    with Batch(work, band_rows=128) as batch:
+    # algorithmic bytes: 2 x the element size per update, in the precision it runs in
+    alg = sum(2 * (T - 1) * (s[0] - 2) * (s[1] - 2) * 2 * (8 if p else np.dtype(dt).itemsize)
+              for (s, dt, T), p in zip(specs, promoted))
+    with Batch(work, band_rows=rows, mode=form, guard=guard) as batch:
         info = batch.info()
         with ClockSampler(0) as clk:
             ms = _timed_steps(torch, dev, stream, lambda: batch.launch(graph=True), reset,
@@ -866,33 +892,35 @@ def batch_measure(n_grids=4096, steps=2, warmup=1, compare=True, compare_steps=1
     out = {"value": ups / (ms_step * 1e-3), "unit": UNIT, "ms_per_step": ms_step,
            "steps": steps, "warmup": warmup, "updates_per_step": ups,
            "cells": sum(s[0] * s[1] for s, _, _ in specs), "form": info["mode"],
-           "tiles" if info["mode"] == "stepped" else "bands": info["bands"],
+           "tiles" if info["mode"] != "persistent" else "bands": info["bands"],
            "launches" if info["mode"] == "stepped" else "ctas": info["ctas"],
-           "rows_per_tile": 128, "graph": True,
+           "rows_per_tile": rows, "graph": True,
+           "fp64_guard": {"on": bool(guard), "float32_grids_run_in_float64": int(sum(promoted)),
+                          "float32_grids": int(sum(dt == np.float32 for _, dt, _ in specs))},
            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                         "frac": ach / peak, "peak_kind": kind,
                         "traffic": ncu_traffic("batch_4096")},
            "clocks": clk.summary()}
     if compare:
-        def per_grid():
-            for a, b, T in work:
-                stencils.jacobi_2d_kernel(T, a, b)
-        ms_pg = _timed_steps(torch, dev, stream, per_grid, reset, compare_steps, compare_warmup)
+        ms_pg = _timed_steps(torch, dev, stream, lambda: _per_grid_guarded(work, guard), reset,
+                             compare_steps, compare_warmup)
         ms_pg /= compare_steps
         out["per_grid"] = {"value": ups / (ms_pg * 1e-3), "ms_per_step": ms_pg,
                            "steps": compare_steps, "warmup": compare_warmup,
                            "kernel_launches": sum(2 * (T - 1) for _, _, T in specs),
                            "what": "one jacobi_2d_kernel call per grid (chained launches, "
-                                   "tuned single-grid kernels), same inputs and steps"}
+                                   "tuned single-grid kernels), same inputs, steps and "
+                                   "float64 guard"}
         out["batched_over_per_grid"] = ms_pg / ms_step
     if fp32_error:
-        # The float32 grids against float64 runs of the same (exactly widened) inputs.
+        # The float32 grids (as the batch left them, guard included) against float64
+        # runs of the same inputs, widened exactly.
         reset()
-        with Batch(work, band_rows=128) as batch:
+        with Batch(work, band_rows=rows, mode=form, guard=guard) as batch:
             batch.launch()
         f32 = [(g, T) for g, ((_, dt, T), _) in enumerate(zip(specs, work)) if dt == np.float32]
         shadow = [(init[g][0].double(), init[g][1].double(), T) for g, T in f32]
-        with Batch(shadow, band_rows=128) as sb:
+        with Batch(shadow, band_rows=rows, mode=form) as sb:
             sb.launch()
         torch.cuda.synchronize(dev)
         out["fp32_error_vs_fp64"] = _fp32_error_report(
@@ -951,7 +979,7 @@ SERVE_WORKLOAD = ("served stream: {n} requests, Poisson {rate:g} req/s, 2D Jacob
 
 
 def serve_measure(rates=(200.0, 1000.0, 5000.0), n_requests=100, compare=True, fp32_error=True,
-                  quantum=64, cpu=False):
+                  cpu=False):
     """Configuration 5: Poisson arrivals of mixed solves through the continuous-batching
     server at each rate, beside the same requests run one at a time with per-grid
     launches.  Returns {"rates": [...], "fp32_error_vs_fp64": ...}."""
@@ -959,18 +987,24 @@ def serve_measure(rates=(200.0, 1000.0, 5000.0), n_requests=100, compare=True, f
     from npbench_gb300 import stencils, workloads
     from npbench_gb300.server import (Request, StencilServer, latency_stats, run_sequential,
                                       _materialise)
-    with StencilServer(quantum=quantum) as warm:
+    with StencilServer() as warm:
         warm.submit(Request(shape=(64, 64), dtype=np.float32, tsteps=5, seed=1)).result()
-    out = {"requests_per_rate": n_requests, "hbm_budget_gb": 150, "rates": []}
+    out = {"requests_per_rate": n_requests, "hbm_budget_gb": 150, "rates": [],
+           "inputs": "seeded U[0,1) host arrays in pinned memory, uploaded by the server "
+                     "(and by the comparator) inside the measured span; results stay on "
+                     "the device"}
     kept = None
+    # The same requests at every rate (only the arrival times scale).
+    _, specs = workloads.served_requests(n_requests, rates[0], seed=0)
+    host = [_pinned_inputs(s, dt, sd) for s, dt, T, sd in specs]
     for rate in rates:
-        arrivals, specs = workloads.served_requests(n_requests, rate, seed=0)
+        arrivals, _ = workloads.served_requests(n_requests, rate, seed=0)
 
         def make():
-            return [Request(shape=s, dtype=dt, tsteps=T, seed=sd, return_host=False)
-                    for s, dt, T, sd in specs]
+            return [Request(shape=s, dtype=dt, tsteps=T, a=h[0], b=h[1], return_host=False)
+                    for (s, dt, T, sd), h in zip(specs, host)]
         reqs = make()
-        srv = StencilServer(quantum=quantum, hbm_budget_bytes=150e9).start()
+        srv = StencilServer(hbm_budget_bytes=150e9).start()
         t0 = time.perf_counter()
         futs = []
         with ClockSampler(0) as clk:
@@ -984,8 +1018,8 @@ def serve_measure(rates=(200.0, 1000.0, 5000.0), n_requests=100, compare=True, f
         st = latency_stats(reqs)
         entry = {"rate_hz": rate, "served": {k: st[k] for k in ("updates_per_s", "p50_ms",
                                                                   "p99_ms", "mean_ms", "span_s")},
-                 "rounds": srv.rounds, "peak_resident_gb": srv.admission.peak / 1e9,
-                 "clocks": clk.summary()}
+                 "worker_launches": srv.launches, "float32_requests_run_in_float64": srv.promoted,
+                 "peak_resident_gb": srv.admission.peak / 1e9, "clocks": clk.summary()}
         if compare:
             seq = make()
             run_sequential(seq, arrivals)
@@ -1007,15 +1041,15 @@ def serve_measure(rates=(200.0, 1000.0, 5000.0), n_requests=100, compare=True, f
         for r, (A, B) in zip(reqs, results):
             if np.dtype(r.dtype) != np.float32 or r.tsteps <= 1:
                 continue
-            shadow = Request(shape=r.shape, dtype=np.float64, tsteps=r.tsteps, seed=r.seed)
-            a64, b64 = _materialise(shadow, dev)
+            a64, b64 = _materialise(r, dev)
+            a64, b64 = a64.double(), b64.double()
             (stencils.jacobi_2d_kernel if a64.dim() == 2 else stencils.heat_3d_kernel)(
                 r.tsteps, a64, b64)
             pairs.append((r.tsteps, A, a64))
         torch.cuda.synchronize(dev)
         rep = _fp32_error_report(pairs)
-        rep["what"] = ("float32 requests of the stream against float64 runs of the same "
-                       "seeded draw (float32 inputs are roundings of it)")
+        rep["what"] = ("float32 requests of the stream (float64 guard on) against float64 "
+                       "runs of the same inputs, widened exactly")
         out["fp32_error_vs_fp64"] = rep
         del pairs, kept, results
         torch.cuda.empty_cache()
@@ -1043,15 +1077,30 @@ def serve_measure(rates=(200.0, 1000.0, 5000.0), n_requests=100, compare=True, f
     return out
 
 
+def _pinned_inputs(shape, dt, seed):
+    """Seeded U[0,1) inputs of one request in pinned host memory: A, and B for 2D."""
+    import torch
+    tdt = torch.float32 if dt == np.float32 else torch.float64
+    rng = np.random.default_rng(seed)
+    a = torch.empty(shape, dtype=tdt, pin_memory=True).numpy()
+    rng.random(shape, dtype=dt, out=a)
+    if len(shape) != 2:
+        return a, None
+    b = torch.empty(shape, dtype=tdt, pin_memory=True).numpy()
+    rng.random(shape, dtype=dt, out=b)
+    return a, b
+
+
 def run_serve(args):
     """Configuration 5 on its own line (``--workload serve``) at ``--rate``."""
     s = serve_measure(rates=(args.rate,), n_requests=args.requests, compare=args.compare,
-                      quantum=args.quantum, cpu=not args.no_cpu_baseline)
+                      cpu=not args.no_cpu_baseline)
     e = s["rates"][0]
     print(json.dumps(_base_line(
         args, e["served"]["updates_per_s"], e["served"]["span_s"] * 1e3, "f32+f64",
         SERVE_WORKLOAD.format(n=args.requests, rate=args.rate),
-        {"quantum_half_sweeps": args.quantum, "hbm_budget_gb": 150, "rounds": e["rounds"],
+        {"hbm_budget_gb": 150, "worker_launches": e["worker_launches"],
+         "float32_requests_run_in_float64": e["float32_requests_run_in_float64"],
          "peak_resident_gb": e["peak_resident_gb"]},
         latency={k: e["served"][k] for k in ("p50_ms", "p99_ms", "mean_ms")},
         comparator=e.get("sequential"), served_over_sequential=e.get("served_over_sequential"),

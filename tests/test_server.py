@@ -189,14 +189,17 @@ def test_server_rejects_oversized_and_cancels_on_stop():
     with pytest.raises(ValueError):
         srv.submit(big)
     srv.stop()
-    # a long queue behind a budget that holds one grid; stop without draining cancels the rest
-    srv = StencilServer(hbm_budget_bytes=big.nbytes, reserve_bytes=0).start()
-    futs = [srv.submit(Request(shape=(100, 100), dtype=np.float64, tsteps=400, seed=i))
+    # a long queue behind a budget that holds one grid (each takes tens of
+    # milliseconds); stop without draining cancels the rest
+    one = Request(shape=(1024, 1024), dtype=np.float64, tsteps=3000, seed=0)
+    srv = StencilServer(hbm_budget_bytes=one.nbytes, reserve_bytes=0).start()
+    futs = [srv.submit(Request(shape=(1024, 1024), dtype=np.float64, tsteps=3000, seed=i,
+                               return_host=False))
             for i in range(6)]
-    time.sleep(0.05)
+    time.sleep(0.02)
     srv.stop(drain=False)
     assert any(f.cancelled() for f in futs)
     for f in futs:
         if not f.cancelled():
             A, B = f.result(timeout=60)
-            assert A.shape == (100, 100)
+            assert tuple(A.shape) == (1024, 1024)
