@@ -318,27 +318,29 @@ class StencilServer:
         self.tq = TileQueue(max_slots=self.max_slots, tile_rows=self.tile_rows,
                             tile_planes=self.tile_planes, ctas_per_sm=self.ctas_per_sm,
                             idle_us=self.idle_us, device=self.device)
-        waiting = collections.deque()
         staging = []     # (request, upload event)
         resident = {}    # slot -> request
         returning = []   # (request, delivery event)
         try:
             while True:
                 with self._cv:
-                    while self._queue:
-                        waiting.append(self._queue.popleft())
-                    if self._stop and not (waiting or staging or resident or returning):
+                    if self._stop and not (self._queue or staging or resident or returning):
                         return
                 moved = False
                 # admission, oldest first; later requests wait behind one that does not fit
-                while waiting:
-                    req = waiting[0]
-                    if req.future.cancelled():
-                        waiting.popleft()
-                        continue
-                    if not self.admission.try_admit(req.nbytes):
-                        break
-                    waiting.popleft()
+                # (a request leaves the client queue only once admitted, so stop(drain=False)
+                # can still cancel the rest)
+                while True:
+                    with self._cv:
+                        if not self._queue:
+                            break
+                        req = self._queue[0]
+                        if req.future.cancelled():
+                            self._queue.popleft()
+                            continue
+                        if not self.admission.try_admit(req.nbytes):
+                            break
+                        self._queue.popleft()
                     req.t_admit = time.perf_counter()
                     self.promoted += int(req.promoted)
                     staging.append((req, self._upload(req)))
@@ -378,12 +380,12 @@ class StencilServer:
                 returning = still
                 if not moved:
                     with self._cv:
-                        if not self._queue and not self._stop:
+                        if not self._stop:
                             self._cv.wait(timeout=self.poll_s)
         except Exception as e:  # fail every outstanding request loudly
             self.error = e
             with self._cv:
-                pending = list(self._queue) + list(waiting) + [r for r, _ in staging] + \
+                pending = list(self._queue) + [r for r, _ in staging] + \
                     list(resident.values()) + [r for r, _ in returning]
                 self._queue.clear()
             for r in pending:
