@@ -90,6 +90,12 @@ extern "C" {
                                          also the halo width; an even number up to
                                          64, 0 (default) = the library's choice.
                                          Reading returns the value in effect. */
+#define NPBGB_CFG_HEAT_TB 16          /* heat3d binary32: half-sweeps per launch, 2
+                                         (default; temporal blocking, where the
+                                         arrays meet the TMA rules and TSTEPS >= 4)
+                                         or 1.  Results are identical either way. */
+#define NPBGB_CFG_HEAT_TB_CHUNK 17    /* heat3d binary32 two-step kernel: axis-0
+                                         planes per CTA; 0 (default) = automatic */
 
 /* Batch forms. */
 #define NPBGB_BATCH_PERSISTENT 1
@@ -154,6 +160,26 @@ NPBGB_API int32_t npbgb_device_status(void* stream);
  * npbgb_device_status then reports: a check of the timeout path that needs
  * no fault.  No counterpart in the reference. */
 NPBGB_API int32_t npbgb_selftest_wait_timeout(int64_t limit_ns, void* stream);
+
+/* Converts n elements: NPBGB_F32 -> NPBGB_F64 (exact) or NPBGB_F64 -> NPBGB_F32
+ * (round to nearest even, as NumPy's astype).  For binary32 requests that run
+ * in binary64 because their binary32 error would exceed NPBench's acceptance
+ * bound (npbench/infrastructure/utilities.py:154-180); the reference has no such
+ * step (it runs in the dtype it is given). */
+NPBGB_API int32_t npbgb_convert(void* dst, int32_t dst_dtype, const void* src, int32_t src_dtype,
+                                int64_t n, void* stream);
+
+/* Arithmetic pipe probe: launches `ctas` CTAs of 256 threads in which every
+ * thread runs 8 independent chains of `iters` operations of one kind
+ * (op: 0 binary64 add, 1 binary64 multiply, 2 binary64 fused multiply-add,
+ * 3 binary32 fused multiply-add, 4 32-bit three-input logic, 5 32-bit add,
+ * 6 32-bit multiply-add); the caller times it on `stream`, and
+ * ctas * 256 * 8 * iters / time is that pipe's throughput.  `sink` holds
+ * ctas * 256 doubles.  These are the compute roofs that the binary64 kernels,
+ * which GB300's binary64 pipe bounds rather than HBM, are measured against.
+ * No counterpart in the reference. */
+NPBGB_API int32_t npbgb_probe_pipe(int32_t op, int64_t iters, int32_t ctas, void* sink,
+                                   void* stream);
 
 /* 2D 5-point Jacobi, the whole time loop of
  *   kernel(TSTEPS, A, B)   polybench/jacobi_2d/jacobi_2d_numpy.py:4-10

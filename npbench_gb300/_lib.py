@@ -33,6 +33,8 @@ NPBGB_CFG_BATCH_MODE = 11
 NPBGB_CFG_HDIFF_EMU = 12
 NPBGB_CFG_JACOBI1D_CTAS = 14
 NPBGB_CFG_JACOBI1D_DEPTH = 15
+NPBGB_CFG_HEAT_TB = 16
+NPBGB_CFG_HEAT_TB_CHUNK = 17
 NPBGB_BATCH_PERSISTENT = 1
 NPBGB_BATCH_STEPPED = 2
 NPBGB_BATCH_QUEUE = 3
@@ -76,6 +78,8 @@ SIGNATURES = {
                                  ctypes.POINTER(_i64)]),
     "npbgb_queue_close": (_i32, [_vp]),
     "npbgb_queue_destroy": (_i32, [_vp]),
+    "npbgb_probe_pipe": (_i32, [_i32, _i64, _i32, _vp, _vp]),
+    "npbgb_convert": (_i32, [_vp, _i32, _vp, _i32, _i64, _vp]),
     "npbgb_jacobi2d": (_i32, [_vp, _vp, _i64, _i64, _i32, _i32, _vp]),
     "npbgb_heat3d": (_i32, [_vp, _vp, _i64, _i64, _i64, _i32, _i32, _vp]),
     "npbgb_hdiff": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i32, _vp]),
@@ -153,3 +157,15 @@ def device_status(stream=None):
 
 def version():
     return load().npbgb_version().decode()
+
+
+def convert(dst, src, stream=None):
+    """dst <- src between float32 and float64 CUDA tensors of one size (libnpbgb kernel)."""
+    import torch
+    codes = {torch.float64: NPBGB_F64, torch.float32: NPBGB_F32}
+    if dst.numel() != src.numel() or not (dst.is_contiguous() and src.is_contiguous()):
+        raise ValueError("convert: contiguous tensors of one size")
+    if stream is None:
+        stream = torch.cuda.current_stream(dst.device)
+    check(load().npbgb_convert(dst.data_ptr(), codes[dst.dtype], src.data_ptr(), codes[src.dtype],
+                               dst.numel(), stream.cuda_stream), "npbgb_convert")

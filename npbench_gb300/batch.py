@@ -9,7 +9,7 @@ half-sweep over all grids still active), smaller ones in the persistent form;
 ``mode="queue"`` runs the batch as one launch of the device-side tile work
 queue, and NPBGB_CFG_BATCH_MODE or ``mode`` forces any form.  ``guard=True``
 runs float32 grids whose float32 error would exceed NPBench's bound in float64
-(queue form).  Every entry (A, B, TSTEPS) is a pair of CUDA tensors of one dtype (float32 or
+(stepped or queue form).  Every entry (A, B, TSTEPS) is a pair of CUDA tensors of one dtype (float32 or
 float64) with its own step count: 2D pairs are Jacobi-2D grids, 3D pairs
 Heat-3D grids.  After a launch each pair holds what ``kernel(TSTEPS, A, B)``
 of polybench/jacobi_2d/jacobi_2d_numpy.py:4-10 or
@@ -50,8 +50,8 @@ class Batch:
 
         guard=True applies the float64 guard (``npbench_gb300.precision``): a
         float32 grid whose float32 error is predicted above NPBench's bound runs
-        in float64 (widened exactly, rounded back once at the end), which needs
-        the queue form; the batch then takes it."""
+        in float64 (widened exactly, rounded back once at the end), which the
+        stepped and queue forms do (by default such a batch is stepped)."""
         self._h = None
         self.guard = bool(guard)
         self.promoted = 0
@@ -83,10 +83,8 @@ class Batch:
         return precision.needs_fp64("jacobi2d" if A.dim() == 2 else "heat3d", int(entry[2]))
 
     def _guard_mode(self, grids, mode):
-        if any(self._promote(e[0], e) for e in grids):
-            if mode not in (None, "auto", "queue"):
-                raise ValueError("float32 grids promoted to float64 need the queue form")
-            return "queue"
+        if mode == "persistent" and any(self._promote(e[0], e) for e in grids):
+            raise ValueError("float32 grids promoted to float64 need the stepped or queue form")
         return mode
 
     def _structs(self, grids, band_rows_of):

@@ -81,6 +81,17 @@ struct StepGrid {
   int16_t dtype, kind;
 };
 
+// A share of one grid's arrays for the binary32 <-> binary64 conversions of a
+// stepped batch (grids run in binary64 for binary32 callers).
+struct ConvChunk {
+  double* a;
+  double* b;
+  float* a32;
+  float* b32;
+  int64_t off, count;
+};
+constexpr int64_t kConvChunk = 1 << 16;  // elements per conversion CTA
+
 __device__ unsigned int g_batch_error;  // bit 0: a CTA made no progress for the limit
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
@@ -260,6 +271,22 @@ batch_step(const StepGrid* __restrict__ grids, const int32_t* __restrict__ tile_
   }
 }
 
+// Widens (before the first half-sweep) or rounds back (after the last) the
+// binary32 arrays of the batch's binary64-promoted grids, one chunk per CTA.
+__global__ void __launch_bounds__(256) batch_convert(const ConvChunk* __restrict__ chunks, int widen) {
+  pdl_begin();
+  const ConvChunk c = chunks[blockIdx.x];
+  for (int64_t i = c.off + threadIdx.x; i < c.off + c.count; i += blockDim.x) {
+    if (widen) {
+      c.a[i] = double(c.a32[i]);
+      c.b[i] = double(c.b32[i]);
+    } else {
+      c.a32[i] = __double2float_rn(c.a[i]);
+      c.b32[i] = __double2float_rn(c.b[i]);
+    }
+  }
+}
+
 using PersistentFn = void (*)(const BandDesc*, uint32_t*, const int32_t*, const int32_t*, int, int,
                               uint32_t);
 
@@ -301,6 +328,8 @@ struct npbgb_batch {
   int32_t* d_tiles = nullptr;
   int64_t cap_step = 0, cap_tiles = 0, ntiles = 0;
   std::vector<int32_t> launch_tiles;  // CTAs of launch s = tiles of the grids active at s
+  npbgb::ConvChunk* d_conv = nullptr;  // stepped form: conversion chunks of promoted grids
+  int64_t cap_conv = 0, nconv = 0;
   // Queue form (mode NPBGB_BATCH_QUEUE).
   npbgb::qhost::StaticQueue* sq = nullptr;
 };
@@ -312,7 +341,7 @@ namespace {
 // Returns NPBGB_OK with *nbands_out = 0 for grids with nothing to do.
 template <typename Emit>
 int32_t plan_grid(const npbgb_grid& G, int64_t g, int32_t band_rows, int first, int64_t* nbands_out,
-                  int64_t* updates_out, Emit emit, bool heat_allowed) {
+                  int64_t* updates_out, Emit emit, bool heat_allowed, bool conv_allowed = false) {
   using namespace npbgb;
   *nbands_out = 0;
   *updates_out = 0;
@@ -326,9 +355,16 @@ int32_t plan_grid(const npbgb_grid& G, int64_t g, int32_t band_rows, int first, 
     return set_error(NPBGB_ERR_ARG, "batch: grid %lld: bad extents", (long long)g);
   if (G.step0 < 0 || G.nsteps < 0)
     return set_error(NPBGB_ERR_ARG, "batch: grid %lld: negative step0 or nsteps", (long long)g);
-  if (G.a32 || G.b32)
+  if ((G.a32 || G.b32) && !conv_allowed)
     return set_error(NPBGB_ERR_ARG,
-                     "batch: grid %lld: binary32 arrays for a binary64 run need the queue form",
+                     "batch: grid %lld: binary32 arrays for a binary64 run need the stepped or "
+                     "queue form",
+                     (long long)g);
+  if ((G.a32 || G.b32) &&
+      (!G.a32 || !G.b32 || G.a32 == G.b32 || G.dtype != NPBGB_F64 || G.a32 == G.a || G.a32 == G.b ||
+       G.b32 == G.a || G.b32 == G.b))
+    return set_error(NPBGB_ERR_ARG,
+                     "batch: grid %lld: binary32 arrays need a binary64 grid and two distinct arrays",
                      (long long)g);
   const int64_t total = G.tsteps > 1 ? 2 * int64_t(G.tsteps - 1) : 0;
   int64_t todo = total - G.step0;
@@ -371,6 +407,7 @@ void free_batch(npbgb_batch* b) {
   if (!b) return;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   npbgb::qhost::free_static(b->sq);
+  cudaFree(b->d_conv);
   cudaFree(b->d_step);
   cudaFree(b->d_tiles);
   cudaFree(b->d_bands);
@@ -385,9 +422,15 @@ int32_t launch_stepped(npbgb_batch* b, cudaStream_t st) {
   const int f64_emul = int(g_cfg_f64_emulation);
   const int hw_warps = jacobi_hw_warps();
   cudaError_t e = cudaSuccess;
+  if (b->nconv > 0)
+    e = launch_chained(batch_convert, dim3{unsigned(b->nconv)}, dim3{256u}, 0, st,
+                       static_cast<const ConvChunk*>(b->d_conv), 1);
   for (size_t s = 0; s < b->launch_tiles.size() && e == cudaSuccess; ++s)
     e = launch_chained(batch_step, dim3{unsigned(b->launch_tiles[s])}, dim3{unsigned(kBThreads)}, 0,
                        st, b->d_step, b->d_tiles, int32_t(s), f64_emul, hw_warps, 1u);
+  if (b->nconv > 0 && e == cudaSuccess)
+    e = launch_chained(batch_convert, dim3{unsigned(b->nconv)}, dim3{256u}, 0, st,
+                       static_cast<const ConvChunk*>(b->d_conv), 0);
   return cuda_status(e, "batch: stepped launch");
 }
 
@@ -456,6 +499,22 @@ int32_t plan_stepped(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int
     }
     sg.push_back(d);
   }
+  std::vector<ConvChunk> conv;
+  for (int64_t g = 0; g < count; ++g) {
+    const npbgb_grid& G = grids[g];
+    if (!G.a32) continue;
+    const bool heat = G.kind == NPBGB_KIND_HEAT3D;
+    const int64_t total = G.tsteps > 1 ? 2 * int64_t(G.tsteps - 1) : 0;
+    int64_t todo = total - G.step0;
+    if (G.nsteps > 0 && G.nsteps < todo) todo = G.nsteps;
+    if (todo <= 0 || G.n0 < 3 || G.n1 < 3 || (heat && G.n2 < 3)) continue;  // nothing to do
+    const int64_t cells = G.n0 * G.n1 * (heat ? G.n2 : 1);
+    for (int64_t off = 0; off < cells; off += kConvChunk)
+      conv.push_back(ConvChunk{static_cast<double*>(G.a), static_cast<double*>(G.b),
+                               static_cast<float*>(G.a32), static_cast<float*>(G.b32), off,
+                               std::min(kConvChunk, cells - off)});
+  }
+  if (int64_t(conv.size()) > 0x7fffffff) return set_error(NPBGB_ERR_NOMEM, "batch: too many chunks");
   std::stable_sort(sg.begin(), sg.end(),
                    [](const StepGrid& x, const StepGrid& y) { return x.count > y.count; });
   std::vector<int32_t> tiles;
@@ -500,6 +559,18 @@ int32_t plan_stepped(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int
       ((e = cudaMemcpy(b->d_step, sg.data(), sizeof(StepGrid) * sg.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
        (e = cudaMemcpy(b->d_tiles, tiles.data(), sizeof(int32_t) * tiles.size(), cudaMemcpyHostToDevice)) != cudaSuccess))
     return cuda_status(e, "batch: upload");
+  if (int64_t(conv.size()) > b->cap_conv) {
+    cudaFree(b->d_conv);
+    b->d_conv = nullptr;
+    b->cap_conv = 0;
+    if ((e = cudaMalloc(&b->d_conv, sizeof(ConvChunk) * conv.size())) != cudaSuccess)
+      return cuda_status(e, "batch: alloc");
+    b->cap_conv = int64_t(conv.size());
+  }
+  if (!conv.empty() &&
+      (e = cudaMemcpy(b->d_conv, conv.data(), sizeof(ConvChunk) * conv.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_status(e, "batch: upload");
+  b->nconv = int64_t(conv.size());
   b->mode = NPBGB_BATCH_STEPPED;
   b->ntiles = int64_t(tiles.size());
   b->launch_tiles = std::move(launch_tiles);
@@ -520,9 +591,14 @@ int32_t plan_into(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int32_
     const npbgb_grid& G = grids[g];
     cells += int64_t(G.n0) * G.n1 * (G.kind == NPBGB_KIND_HEAT3D ? G.n2 : 1);
   }
+  bool conv = false;
+  for (int64_t g = 0; g < count && !conv; ++g) conv = grids[g].a32 || grids[g].b32;
+  // Grids promoted to binary64 for binary32 callers need conversion launches,
+  // which the stepped and queue forms have; by default they take the stepped one.
   const int32_t mode = g_cfg_batch_mode != 0
                            ? int32_t(g_cfg_batch_mode)
-                           : (cells >= kSteppedCells ? NPBGB_BATCH_STEPPED : NPBGB_BATCH_PERSISTENT);
+                           : ((conv || cells >= kSteppedCells) ? NPBGB_BATCH_STEPPED
+                                                               : NPBGB_BATCH_PERSISTENT);
   if (mode == NPBGB_BATCH_QUEUE) {
     // The queue planner validates the grids itself (it also takes binary32
     // arrays of grids run in binary64).
@@ -550,7 +626,8 @@ int32_t plan_into(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int32_
   for (int64_t g = 0; g < count; ++g) {
     int64_t nb = 0, up = 0;
     const int32_t r = plan_grid(grids[g], g, band_rows, int(bands.size()), &nb, &up,
-                                [&](const BandDesc& d) { bands.push_back(d); }, true);
+                                [&](const BandDesc& d) { bands.push_back(d); }, true,
+                                mode == NPBGB_BATCH_STEPPED);
     if (r != NPBGB_OK) return r;
     if (int64_t(bands.size()) > 0x7fffffff) return set_error(NPBGB_ERR_NOMEM, "batch: too many bands");
     updates += up;
@@ -561,6 +638,7 @@ int32_t plan_into(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int32_
   }
   qhost::free_static(b->sq);
   b->sq = nullptr;
+  b->nconv = 0;
   if (mode == NPBGB_BATCH_STEPPED) return plan_stepped(b, grids, count, band_rows, updates);
   b->mode = NPBGB_BATCH_PERSISTENT;
   b->launch_tiles.clear();

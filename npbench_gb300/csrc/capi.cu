@@ -25,6 +25,8 @@ int64_t g_cfg_batch_mode = 0;
 int64_t g_cfg_hdiff_emu = -1;  // -1: default mask
 int64_t g_cfg_jacobi1d_ctas = 0;   // 0: default
 int64_t g_cfg_jacobi1d_depth = 0;  // 0: default
+int64_t g_cfg_heat_tb = 2;         // binary32 Heat-3D half-sweeps per launch
+int64_t g_cfg_heat_tb_chunk = 0;   // 0: automatic
 int64_t jacobi1d_effective_depth();  // jacobi1d.cu
 int64_t jacobi1d_effective_ctas();
 
@@ -32,6 +34,7 @@ uint32_t take_heat_device_error();
 uint32_t take_batch_device_error();
 uint32_t take_cfd_device_error();
 uint32_t take_queue_device_error();
+uint32_t take_heat_tb_device_error();
 int32_t launch_wait_timeout_selftest(uint64_t limit_ns, cudaStream_t st);
 
 int32_t set_error(int32_t code, const char* fmt, ...) {
@@ -159,6 +162,14 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       if (value < 0 || value > 8) return set_error(NPBGB_ERR_ARG, "jacobi1d CTAs per SM: 0 .. 8");
       g_cfg_jacobi1d_ctas = value;
       return NPBGB_OK;
+    case NPBGB_CFG_HEAT_TB:
+      if (value != 1 && value != 2) return set_error(NPBGB_ERR_ARG, "heat TB: 1 or 2");
+      g_cfg_heat_tb = value;
+      return NPBGB_OK;
+    case NPBGB_CFG_HEAT_TB_CHUNK:
+      if (value < 0 || value > 65535) return set_error(NPBGB_ERR_ARG, "heat TB chunk: 0 .. 65535");
+      g_cfg_heat_tb_chunk = value;
+      return NPBGB_OK;
     case NPBGB_CFG_JACOBI1D_DEPTH:
       if (value < 0 || value > 64 || (value & 1))
         return set_error(NPBGB_ERR_ARG, "jacobi1d depth: 0 or an even number up to 64");
@@ -187,6 +198,8 @@ int32_t npbgb_get_config(int32_t key, int64_t* value) {
     case NPBGB_CFG_HDIFF_EMU: *value = g_cfg_hdiff_emu; return NPBGB_OK;
     case NPBGB_CFG_JACOBI1D_CTAS: *value = jacobi1d_effective_ctas(); return NPBGB_OK;
     case NPBGB_CFG_JACOBI1D_DEPTH: *value = jacobi1d_effective_depth(); return NPBGB_OK;
+    case NPBGB_CFG_HEAT_TB: *value = g_cfg_heat_tb; return NPBGB_OK;
+    case NPBGB_CFG_HEAT_TB_CHUNK: *value = g_cfg_heat_tb_chunk; return NPBGB_OK;
     default: return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
   }
 }
@@ -195,7 +208,7 @@ int32_t npbgb_device_status(void* stream) {
   using namespace npbgb;
   cudaError_t e = stream ? cudaStreamSynchronize(as_stream(stream)) : cudaDeviceSynchronize();
   if (e != cudaSuccess) return cuda_status(e, "device status");
-  const uint32_t h = take_heat_device_error();
+  const uint32_t h = take_heat_device_error() | take_heat_tb_device_error();
   const uint32_t bt = take_batch_device_error();
   const uint32_t cf = take_cfd_device_error();
   const uint32_t qu = take_queue_device_error();

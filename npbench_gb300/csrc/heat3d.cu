@@ -37,6 +37,11 @@ extern int64_t g_cfg_heat_tma;
 extern int64_t g_cfg_heat_rows;
 extern int64_t g_cfg_heat_hw_rows;
 extern int64_t g_cfg_f64_cvt;
+extern int64_t g_cfg_heat_tb;
+
+int32_t heat3d_tb2_run(float* a, float* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps,
+                       cudaStream_t st, int32_t (*single_pairs)(float*, float*, int64_t, int64_t,
+                                                                int64_t, int32_t, cudaStream_t));
 
 namespace {
 
@@ -348,7 +353,7 @@ int32_t launch_ldg(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tstep
 }
 
 template <typename T, bool FX>
-int32_t run(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps, cudaStream_t st) {
+int32_t run_single(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps, cudaStream_t st) {
   if (tsteps <= 1 || n0 < 3 || n1 < 3 || n2 < 3) return NPBGB_OK;
   if (g_cfg_heat_tma) {
     // Tuned on GB300 (256^3): binary32 is memory-latency bound and wants more
@@ -368,6 +373,24 @@ int32_t run(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps, cuda
     if (r != NPBGB_ERR_STATE) return r;
   }
   return launch_ldg<T, FX>(a, b, n0, n1, n2, tsteps, st);
+}
+
+int32_t run_single_f32(float* a, float* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps,
+                       cudaStream_t st) {
+  return run_single<float, false>(a, b, n0, n1, n2, tsteps, st);
+}
+
+// Binary32 (HBM-bound) takes two half-sweeps per launch (heat_tb.cu) where
+// the arrays allow TMA; binary64 (bound by its arithmetic pipes) one.
+template <typename T, bool FX>
+int32_t run(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps, cudaStream_t st) {
+  if constexpr (sizeof(T) == 4) {
+    if (g_cfg_heat_tb == 2 && g_cfg_heat_tma && tsteps >= 4) {
+      const int32_t r = heat3d_tb2_run(a, b, n0, n1, n2, tsteps, st, run_single_f32);
+      if (r != NPBGB_ERR_STATE) return r;
+    }
+  }
+  return run_single<T, FX>(a, b, n0, n1, n2, tsteps, st);
 }
 
 // One CTA waits, with a short limit, on an mbarrier that nothing completes;

@@ -6,9 +6,10 @@
 // column tile streamed over `chunk` planes).  Segments sit in a ring in
 // device memory.  Every CTA of the worker kernel loops:
 //
-//   claim  the next tile of the segment at the ring's head (a 64-bit
-//          compare-and-swap on the entry's claim word, tagged with the ring
-//          position so that a late claimer of a recycled entry fails);
+//   claim  the next tiles of the segment at the ring's head: one 64-bit
+//          fetch-and-add on the entry's claim word, whose high half is the
+//          ring position (a claimer whose add lands on a recycled entry owns
+//          the tiles it counted there, so every add is a valid claim);
 //   sweep  that tile (the same per-point arithmetic as the single-grid
 //          kernels, loads and stores through L2);
 //   count  the tile into its grid's completion counter (acquire-release); the
@@ -20,7 +21,9 @@
 // half-sweep is complete, which orders both read-after-write and
 // write-after-read between the ping-pong buffers; tiles are claimed in ring
 // order, so a claimed tile never waits on anything and the kernel needs no
-// co-residency (plain launch, not cooperative).  Grids of different sizes,
+// co-residency (plain launch, not cooperative).  A claim takes several tiles
+// of a large segment at once (ntiles / (4 * CTAs), at least one).  Grids of
+// different sizes,
 // kinds and precisions interleave tile by tile, and a grid's next half-sweep
 // starts as soon as its own previous one is done.
 //
@@ -36,8 +39,8 @@
 //
 // The kernel ends when nothing is outstanding and the inbox is closed, or
 // has stayed empty for `idle_ns`; the host launches it again when new grids
-// arrive.  Every wait is bounded: with work outstanding, no tile completing
-// anywhere for kQueueLimitNs sets an error word and the kernel ends.
+// arrive.  Every wait is bounded: with work outstanding, a ring whose head and
+// tail stay unchanged for kQueueLimitNs sets an error word and the kernel ends.
 //
 // Per point the arithmetic is that of jacobi2d.cu / heat3d.cu (bit-identical
 // to polybench/jacobi_2d/jacobi_2d_numpy.py:6-10 and
@@ -65,7 +68,7 @@ using namespace qdev;
 
 constexpr int kQWarps = 8;
 constexpr int kQThreads = 32 * kQWarps;
-constexpr uint64_t kQueueLimitNs = 2000000000ull;  // two seconds without a completed tile
+constexpr uint64_t kQueueLimitNs = 2000000000ull;  // two seconds without the ring moving
 
 __device__ unsigned int g_queue_error;  // any launch's error bits, for npbgb_device_status
 
@@ -196,13 +199,17 @@ __device__ void record_error(const QArgs& q, uint32_t bits) {
 
 struct Waiting {
   uint64_t idle_since = 0;   // 0: not idle
-  uint64_t seen_t = 0;
-  uint32_t seen_progress = 0xffffffffu;
+  uint64_t seen_t = 0;       // when (seen_h, seen_t) was last seen to change
+  uint32_t seen_h = 0xffffffffu, seen_tail = 0xffffffffu;
 };
 
-// Thread 0: the next tile (slot >= 0), or slot = -1 when the launch ends.
-__device__ void next_tile(const QArgs& q, int32_t* o_slot, int32_t* o_s, int32_t* o_tile,
-                          Waiting& w) {
+struct Claim {
+  int32_t slot = -1, s = 0, t0 = 0, t1 = 0;  // tiles [t0, t1) of half-sweep segment s
+};
+
+// Thread 0: the next tiles (slot >= 0), or slot = -1 when the launch ends.
+__device__ void next_tiles(const QArgs& q, Claim* out, Waiting& w) {
+  const uint32_t div = 4u * gridDim.x;
   for (;;) {
     const uint32_t h = ld_acq_gpu(&q.st->head);
     const uint32_t t = ld_acq_gpu(&q.st->tail);
@@ -211,22 +218,47 @@ __device__ void next_tile(const QArgs& q, int32_t* o_slot, int32_t* o_s, int32_t
       const uint32_t seq = ld_acq_gpu(&e->seq);
       if (seq == h) {
         const int32_t nt = ld_rlx_gpu(&e->ntiles);
-        unsigned long long* cw = &q.claim[h % q.ring_size];
-        for (;;) {
-          const uint64_t c = ld_rlx_gpu64(cw);
-          if (uint32_t(c >> 32) != h) break;  // recycled: the head has moved on
-          const uint32_t n = uint32_t(c);
-          if (int64_t(n) >= int64_t(nt)) {     // exhausted: help the head along
-            atomicCAS(&q.st->head, h, h + 1u);
-            break;
-          }
-          if (atomicCAS(cw, (unsigned long long)c, (unsigned long long)(c + 1)) == c) {
-            *o_slot = ld_rlx_gpu(&e->slot);
-            *o_s = ld_rlx_gpu(&e->s);
-            *o_tile = int32_t(n);
+        const uint32_t per = max(1u, uint32_t(nt) / div);
+        const uint64_t old = atomicAdd(&q.claim[h % q.ring_size], (unsigned long long)per);
+        const uint32_t tag = uint32_t(old >> 32), n = uint32_t(old);
+        if (tag == h) {
+          if (n < uint32_t(nt)) {
+            out->slot = ld_rlx_gpu(&e->slot);
+            out->s = ld_rlx_gpu(&e->s);
+            out->t0 = int32_t(n);
+            out->t1 = int32_t(min(n + per, uint32_t(nt)));
             w.idle_since = 0;
             return;
           }
+          atomicCAS(&q.st->head, h, h + 1u);  // exhausted: help the head along
+          continue;
+        }
+        // The add landed on the entry recycled for position `tag` (> h): the
+        // tiles [n, n + per) of that segment are this claimer's.  Its producer
+        // wrote the claim word before publishing the entry; wait for that.
+        QSeg* r = &q.ring[tag % q.ring_size];
+        const uint64_t t_start = tma::globaltimer();
+        for (;;) {
+          const uint32_t rs = ld_acq_gpu(&r->seq);
+          if (rs == tag) break;
+          if ((rs != kSeqEmpty && int32_t(rs - tag) > 0) ||
+              tma::globaltimer() - t_start > kQueueLimitNs) {
+            // recycled again before this claim could be read, or never
+            // published: both mean lost tiles; end with an error
+            record_error(q, 1u);
+            out->slot = -1;
+            return;
+          }
+          __nanosleep(32);
+        }
+        const int32_t rn = ld_rlx_gpu(&r->ntiles);
+        if (n < uint32_t(rn)) {
+          out->slot = ld_rlx_gpu(&r->slot);
+          out->s = ld_rlx_gpu(&r->s);
+          out->t0 = int32_t(n);
+          out->t1 = int32_t(min(n + per, uint32_t(rn)));
+          w.idle_since = 0;
+          return;
         }
         continue;
       }
@@ -239,27 +271,27 @@ __device__ void next_tile(const QArgs& q, int32_t* o_slot, int32_t* o_s, int32_t
     if (activate(q)) continue;
     const uint64_t now = tma::globaltimer();
     if (ld_acq_gpu(&q.st->shutdown)) {
-      *o_slot = -1;
+      out->slot = -1;
       return;
     }
     const uint32_t active = ld_acq_gpu(&q.st->active);
+    if (h != w.seen_h || t != w.seen_tail) {
+      w.seen_h = h;
+      w.seen_tail = t;
+      w.seen_t = now;
+    }
     if (active == 0u && h == t) {
       if (w.idle_since == 0) w.idle_since = now;
       const bool closed = ld_acq_sys(&q.inbox_ctl[1]) != 0u;
       if ((closed || now - w.idle_since > q.idle_ns) && try_shutdown(q)) {
-        *o_slot = -1;
+        out->slot = -1;
         return;
       }
-      w.seen_progress = 0xffffffffu;
     } else {
       w.idle_since = 0;
-      const uint32_t pr = ld_rlx_gpu(&q.st->progress);
-      if (pr != w.seen_progress) {
-        w.seen_progress = pr;
-        w.seen_t = now;
-      } else if (now - w.seen_t > kQueueLimitNs) {
+      if (now - w.seen_t > kQueueLimitNs) {  // work outstanding, ring not moving
         record_error(q, 1u);
-        *o_slot = -1;
+        out->slot = -1;
         return;
       }
     }
@@ -267,12 +299,12 @@ __device__ void next_tile(const QArgs& q, int32_t* o_slot, int32_t* o_s, int32_t
   }
 }
 
-// Thread 0, after the CTA's barrier: counts the tile and hands on the grid.
-__device__ void complete_tile(const QArgs& q, int32_t slot, int32_t s, const QSlot& G) {
+// Thread 0, after the CTA's barrier: counts the tiles and hands on the grid.
+__device__ void complete_tiles(const QArgs& q, int32_t slot, int32_t s, int32_t count,
+                               const QSlot& G) {
   // bar.sync ordered the CTA's stores before this release, which is cumulative.
-  const uint32_t old = atom_add_acq_rel(&q.done[slot], 1u);
-  atomicAdd(&q.st->progress, 1u);
-  if (old + 1u == uint32_t(s + 1) * uint32_t(G.ntiles)) {
+  const uint32_t old = atom_add_acq_rel(&q.done[slot], uint32_t(count));
+  if (old + uint32_t(count) == uint32_t(s + 1) * uint32_t(G.ntiles)) {
     if (s + 1 < G.steps) {
       produce(q, slot, s + 1, G.ntiles);
     } else {
@@ -360,18 +392,20 @@ __device__ __forceinline__ void sweep_tile(const QArgs& q, const QSlot& G, int32
 
 template <int MINB>
 __global__ void __launch_bounds__(kQThreads, MINB) queue_worker(const QArgs q) {
-  __shared__ int32_t s_cmd[3];
+  __shared__ int32_t s_cmd[4];
   __shared__ __align__(16) QSlot s_slot;
   __shared__ hcore::PlaneBuf<double, true> plane;  // Heat-3D staging (largest element type)
   const int tid = threadIdx.x;
   Waiting w;
   for (;;) {
     if (tid == 0) {
-      int32_t slot = -1, s = 0, tile = 0;
-      next_tile(q, &slot, &s, &tile, w);
+      Claim c;
+      next_tiles(q, &c, w);
+      const int32_t slot = c.slot;
       s_cmd[0] = slot;
-      s_cmd[1] = s;
-      s_cmd[2] = tile;
+      s_cmd[1] = c.s;
+      s_cmd[2] = c.t0;
+      s_cmd[3] = c.t1;
       if (slot >= 0) {
         // The slot was written by the activating CTA before it published the
         // segment this thread acquired; read it through L2.
@@ -384,11 +418,11 @@ __global__ void __launch_bounds__(kQThreads, MINB) queue_worker(const QArgs q) {
     __syncthreads();
     const int32_t slot = s_cmd[0];
     if (slot < 0) return;
-    const int32_t s = s_cmd[1], tile = s_cmd[2];
+    const int32_t s = s_cmd[1], t0 = s_cmd[2], t1 = s_cmd[3];
     const QSlot G = s_slot;
-    sweep_tile(q, G, s, tile, plane);
+    for (int32_t tile = t0; tile < t1; ++tile) sweep_tile(q, G, s, tile, plane);
     __syncthreads();
-    if (tid == 0) complete_tile(q, slot, s, G);
+    if (tid == 0) complete_tiles(q, slot, s, t1 - t0, G);
   }
 }
 
@@ -474,10 +508,12 @@ int32_t describe(const npbgb_grid& G, int64_t g, int32_t tile_rows, int32_t tile
   return NPBGB_OK;
 }
 
+// CTAs per SM a worker launch uses: the requested count, at most what fits.
 int slots_per_sm(int ctas_per_sm, int* per_sm_out) {
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, worker_fn(ctas_per_sm), kQThreads, 0);
   if (per_sm <= 0) per_sm = 1;
+  per_sm = std::min(per_sm, std::max(1, ctas_per_sm));
   if (per_sm_out) *per_sm_out = per_sm;
   return per_sm;
 }

@@ -51,8 +51,8 @@ struct QState {
   uint32_t inbox_head;  // inbox entries taken in
   uint32_t lock;        // inbox lock (activation and shutdown)
   uint32_t shutdown;    // 1: every CTA leaves at its next idle moment
-  uint32_t error;       // bit 0: no tile completed within the limit; bit 1: bad inbox entry
-  uint32_t progress;    // tiles completed in this launch
+  uint32_t error;       // bit 0: the ring did not move within the limit; bit 1: bad inbox entry
+  uint32_t pad;
 };
 
 struct QArgs {

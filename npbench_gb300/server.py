@@ -12,18 +12,24 @@ without ever waiting for the GPU:
   arrays fit in the HBM budget (``AdmissionController``); their arrays are
   allocated and their inputs uploaded on a copy stream (an event marks the
   upload done);
-* **folding**: an uploaded grid is handed to the device-side tile work queue
-  (``npbench_gb300.queue``, libnpbgb's ``npbgb_queue_*``), whose persistent
-  worker kernel takes it in while it runs: its tiles interleave with those of
-  every other resident grid, whatever their sizes, kinds and precisions, and
-  its next half-sweep starts as soon as its own previous one is done;
+* **dispatch**: an uploaded grid below ``direct_cells`` cells is folded into
+  the device-side tile work queue (``npbench_gb300.queue``, libnpbgb's
+  ``npbgb_queue_*``), whose persistent worker kernel takes it in while it runs:
+  its tiles interleave with those of every other small grid, whatever their
+  sizes, kinds and precisions, and its next half-sweep starts as soon as its
+  own previous one is done.  A larger grid fills the GPU by itself and goes to
+  a big-grid lane (its own stream) that runs it with the tuned single-grid
+  kernels (TMA pipelines, two half-sweeps per launch in binary32 Heat-3D),
+  shortest job first; the queue's CTAs share the SMs with those launches;
 * **completion**: the worker writes a completion word to host memory when a
-  grid's last half-sweep is done; the serving thread polls those words;
+  grid's last half-sweep is done, and a lane records an event; the serving
+  thread polls both;
 * **return**: results are copied back on the copy stream (or handed over as
   device tensors), the budget is released and the future resolved.
 
 Arrivals never wait for a round to end: the worker kernel keeps running while
-new grids are folded in, and ends by itself only when it has nothing left.
+new grids are folded in (and ends by itself only when it has nothing left),
+and small requests never wait behind a large one.
 
 **Float64 guard.**  A float32 request whose float32 error against float64 is
 predicted to exceed NPBench's acceptance bound (``npbench_gb300.precision``)
@@ -186,8 +192,8 @@ class StencilServer:
     """Serving thread with an HBM admission budget, feeding the device-side tile queue."""
 
     def __init__(self, device=0, hbm_budget_bytes=150e9, max_slots=4096, tile_rows=0,
-                 tile_planes=0, ctas_per_sm=0, idle_us=500, fp64_guard=True,
-                 reserve_bytes=8 << 30, poll_s=2e-4):
+                 tile_planes=0, ctas_per_sm=1, idle_us=500, fp64_guard=True,
+                 reserve_bytes=8 << 30, poll_s=2e-4, direct_cells=1 << 20, big_lanes=1):
         import torch
         self.device = torch.device("cuda", device) if isinstance(device, int) else \
             torch.device(device)
@@ -198,6 +204,9 @@ class StencilServer:
         self.fp64_guard = bool(fp64_guard)
         self.reserve_bytes = int(min(reserve_bytes, hbm_budget_bytes))
         self.poll_s = float(poll_s)
+        self.direct_cells = int(direct_cells)
+        self.big_lanes = max(1, int(big_lanes))
+        self.queued_small = self.ran_big = 0
         self._queue = collections.deque()
         self._cv = threading.Condition()
         self._stop = False
@@ -273,6 +282,24 @@ class StencilServer:
             return self.tq.submit(d["A64"], d["B64"], req.tsteps, a32=d["A"], b32=d["B"])
         return self.tq.submit(d["A"], d["B"], req.tsteps)
 
+    def _run_big(self, req, stream):
+        """Queues a large grid's whole run on a big-grid lane; returns its end event."""
+        import torch
+        d = req.dev
+        fn = stencils.jacobi_2d_kernel if len(req.shape) == 2 else stencils.heat_3d_kernel
+        with torch.cuda.stream(stream):
+            if req.promoted:
+                _lib.convert(d["A64"], d["A"], stream)
+                _lib.convert(d["B64"], d["B"], stream)
+                fn(req.tsteps, d["A64"], d["B64"])
+                _lib.convert(d["A"], d["A64"], stream)
+                _lib.convert(d["B"], d["B64"], stream)
+            else:
+                fn(req.tsteps, d["A"], d["B"])
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        return ev
+
     def _deliver(self, req):
         """Starts returning a finished request's result; returns an event that marks it."""
         import torch
@@ -318,13 +345,18 @@ class StencilServer:
         self.tq = TileQueue(max_slots=self.max_slots, tile_rows=self.tile_rows,
                             tile_planes=self.tile_planes, ctas_per_sm=self.ctas_per_sm,
                             idle_us=self.idle_us, device=self.device)
+        lanes = [{"stream": torch.cuda.Stream(self.device), "req": None, "ev": None}
+                 for _ in range(self.big_lanes)]
         staging = []     # (request, upload event)
+        big_ready = []   # uploaded large grids waiting for a lane
         resident = {}    # slot -> request
         returning = []   # (request, delivery event)
         try:
             while True:
                 with self._cv:
-                    if self._stop and not (self._queue or staging or resident or returning):
+                    busy = any(ln["req"] is not None for ln in lanes)
+                    if self._stop and not (self._queue or staging or big_ready or resident or
+                                           returning or busy):
                         return
                 moved = False
                 # admission, oldest first; later requests wait behind one that does not fit
@@ -345,11 +377,15 @@ class StencilServer:
                     self.promoted += int(req.promoted)
                     staging.append((req, self._upload(req)))
                     moved = True
-                # folding: uploaded grids into the running queue
+                # dispatch: large grids to a lane, small ones into the running queue
                 still = []
                 for req, ev in staging:
                     if not ev.query():
                         still.append((req, ev))
+                        continue
+                    if req.cells >= self.direct_cells and req.updates > 0:
+                        big_ready.append(req)
+                        moved = True
                         continue
                     try:
                         slot = self._fold(req)
@@ -363,7 +399,19 @@ class StencilServer:
                         returning.append((req, self._deliver(req)))
                     else:
                         resident[slot] = req
+                        self.queued_small += 1
                 staging = still
+                for ln in lanes:
+                    if ln["req"] is not None and ln["ev"].query():
+                        returning.append((ln["req"], self._deliver(ln["req"])))
+                        ln["req"] = None
+                        moved = True
+                    if ln["req"] is None and big_ready:
+                        nxt = min(big_ready, key=lambda r: r.updates)  # shortest job first
+                        big_ready.remove(nxt)
+                        ln["req"], ln["ev"] = nxt, self._run_big(nxt, ln["stream"])
+                        self.ran_big += 1
+                        moved = True
                 if resident:
                     self.tq.kick(self._compute)
                     for slot in self.tq.poll():
@@ -385,8 +433,9 @@ class StencilServer:
         except Exception as e:  # fail every outstanding request loudly
             self.error = e
             with self._cv:
-                pending = list(self._queue) + [r for r, _ in staging] + \
-                    list(resident.values()) + [r for r, _ in returning]
+                pending = list(self._queue) + [r for r, _ in staging] + big_ready + \
+                    list(resident.values()) + [r for r, _ in returning] + \
+                    [ln["req"] for ln in lanes if ln["req"] is not None]
                 self._queue.clear()
             for r in pending:
                 if not r.future.done():

@@ -769,3 +769,41 @@ def test_fp32_form_error_against_fp64(bench, shape, tsteps):
     rel_l2 = float(diff.norm() / ref.norm())
     print(f"\nfp32-vs-fp64 {bench} {shape} TSTEPS={tsteps}: max_abs={max_abs:.3e} rel_l2={rel_l2:.3e}")
     assert rel_l2 <= 1e-5 and max_abs < 1e-4
+
+
+@pytest.mark.parametrize("shape", [(3, 3, 4), (4, 5, 8), (18, 34, 36), (40, 70, 68), (67, 33, 100),
+                                   (128, 130, 132), (9, 300, 44)])
+@pytest.mark.parametrize("tsteps", [4, 5, 6, 7, 12])
+def test_heat_f32_two_steps_per_launch(shape, tsteps):
+    """Binary32 Heat-3D with two half-sweeps per launch (temporal blocking) gives the
+    oracle's bits, also when A and B start with different faces (B's faces are the
+    odd steps' faces) and whatever the number of planes per CTA."""
+    from npbench_gb300 import _lib
+    rng = np.random.default_rng(sum(shape) + tsteps)
+    A = rng.random(shape).astype(np.float32)
+    B = rng.random(shape).astype(np.float32)  # distinct faces
+    ra, rb = A.copy(), B.copy()
+    cref.heat_3d_kernel(tsteps, ra, rb)
+    old = (_lib.get_config(_lib.NPBGB_CFG_HEAT_TB), _lib.get_config(_lib.NPBGB_CFG_HEAT_TB_CHUNK))
+    try:
+        for tb, chunk in ((2, 0), (2, 1), (2, 5), (1, 0)):
+            _lib.set_config(_lib.NPBGB_CFG_HEAT_TB, tb)
+            _lib.set_config(_lib.NPBGB_CFG_HEAT_TB_CHUNK, chunk)
+            dA, dB = _dev(A), _dev(B)
+            stencils.heat_3d_kernel(tsteps, dA, dB)
+            _lib.device_status()
+            assert bits_equal(_host(dA), ra), (tb, chunk, first_diff(_host(dA), ra))
+            assert bits_equal(_host(dB), rb), (tb, chunk, first_diff(_host(dB), rb))
+    finally:
+        _lib.set_config(_lib.NPBGB_CFG_HEAT_TB, old[0])
+        _lib.set_config(_lib.NPBGB_CFG_HEAT_TB_CHUNK, old[1])
+
+
+def test_heat_f32_two_steps_full_size_out_of_l2():
+    """384^3 binary32 (two 226 MB arrays, beyond L2): the two-step kernel against the oracle."""
+    A, B = workloads.uniform_heat((384, 384, 384), np.float32, seed=33)
+    dA, dB = _dev(A), _dev(B)
+    stencils.heat_3d_kernel(10, dA, dB)
+    cref.heat_3d_kernel(10, A, B)
+    assert bits_equal(_host(dA), A), first_diff(_host(dA), A)
+    assert bits_equal(_host(dB), B)

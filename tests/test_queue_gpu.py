@@ -163,10 +163,21 @@ def test_batch_guard_promotes_long_float32_grids():
         B = rng.random(shape).astype(dt) if len(shape) == 2 else A.copy()
         host.append((A, B, T))
         dev.append((torch.from_numpy(A).to(DEV), torch.from_numpy(B).to(DEV), T))
-    with Batch(dev, guard=True) as bt:
-        assert bt.promoted == 1 and bt.info()["mode"] == "queue"
-        bt.launch()
-        _lib.device_status()
+    init = [(a.clone(), b.clone()) for a, b, _ in dev]
+    for mode, name in ((None, "stepped"), ("queue", "queue"), ("stepped", "stepped")):
+        for (a0, b0), (a, b, _) in zip(init, dev):
+            a.copy_(a0)
+            b.copy_(b0)
+        with Batch(dev, guard=True, mode=mode) as bt:
+            assert bt.promoted == 1 and bt.info()["mode"] == name
+            bt.launch()
+            _lib.device_status()
+        _check_guarded(host, dev)
+    with pytest.raises(ValueError):
+        Batch(dev, guard=True, mode="persistent")
+
+
+def _check_guarded(host, dev):
     for n, ((A, B, T), (a, b, _)) in enumerate(zip(host, dev)):
         ga, gb = a.cpu().numpy(), b.cpu().numpy()
         oa, ob = A.astype(np.float64), B.astype(np.float64)

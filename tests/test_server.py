@@ -103,10 +103,11 @@ def _alone(r):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("tile_rows", [0, 5])
-def test_served_mix_equals_alone(tile_rows):
+@pytest.mark.parametrize("tile_rows,direct_cells", [(0, 1 << 20), (5, 1 << 20), (0, 3000)])
+def test_served_mix_equals_alone(tile_rows, direct_cells):
     """Requests arrive from three client threads while others run, wait for
-    memory under a small budget, and each result equals the request run alone."""
+    memory under a small budget, and each result equals the request run alone
+    (all through the tile queue, or the larger ones through a big-grid lane)."""
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -115,7 +116,7 @@ def test_served_mix_equals_alone(tile_rows):
     budget = max(2 * r.cells * 16 for r in reqs) * 3  # small: forces waiting for memory
     futures = []
     with StencilServer(hbm_budget_bytes=budget, tile_rows=tile_rows, tile_planes=tile_rows,
-                       reserve_bytes=budget) as srv:
+                       reserve_bytes=budget, direct_cells=direct_cells, big_lanes=2) as srv:
         def client(part):
             for r in part:
                 futures.append((r, srv.submit(r)))
@@ -127,7 +128,9 @@ def test_served_mix_equals_alone(tile_rows):
             t.join()
         results = [(r, f.result(timeout=300)) for r, f in futures]
     assert srv.admission.peak <= budget and srv.admission.in_use == 0
-    assert srv.launches >= 1
+    assert srv.queued_small + srv.ran_big <= len(reqs) and srv.queued_small >= 1
+    if direct_cells < 10000:
+        assert srv.ran_big >= 1
     for r, (A, B) in results:
         a, b = _alone(r)
         assert np.array_equal(a, A) and np.array_equal(b, B), (r.shape, r.dtype, r.tsteps)
