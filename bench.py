@@ -15,7 +15,10 @@ The two 128 MiB arrays exceed the 129 MB L2, so no L2 flush is needed.
 * ``roofline``  algorithmic bytes (16 B per float64 update: read one value,
                 write one) of one half-sweep launch over its measured duration;
 * ``fp64_roofline`` the reference's 13 binary64 operations per update at the
-                achieved rate against the binary64 pipe's measured rate;
+                achieved rate against the binary64 pipe's rate, measured in the
+                same run by a probe kernel (npbench_gb300.pipes);
+* ``compute_roofline`` the kernel's instructions per update on each pipe (ncu)
+                against each pipe's measured rate: the arithmetic ceiling;
 * ``fp32``      the same workload in float32 with its error against float64;
 * ``cpu_baseline`` the reference's arithmetic on the host: the C restatement
                 (oracle/stencils.c, bit-identical to the reference's NumPy code)
@@ -62,9 +65,6 @@ HALF_SWEEPS = 2 * (TSTEPS - 1)
 INTERIOR = (N_GRID - 2) ** 3
 UPDATES_PER_STEP = HALF_SWEEPS * INTERIOR
 FALLBACK_HBM_GBS = 6800.0
-# Rate of GB300's binary64 pipe for DADD / DMUL, measured with a probe kernel of
-# independent dependent chains on this hardware (ops/s, whole GPU).
-FP64_PIPE_OPS = 5.0e11
 # Separately rounded binary64 operations per Heat-3D update as the reference
 # writes it: 2*c once, then per axis a subtraction, an addition and the product
 # by 0.125, and three additions joining the axes.
@@ -114,14 +114,65 @@ def measured_peaks():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def ncu_traffic(kernel_key):
-    """DRAM bytes per launch recorded from an ncu capture (profiles/ncu_traffic.json)."""
+def _ncu_record(kernel_key):
     try:
         with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
-            d = json.load(f)
-        return d.get(kernel_key, {}).get("dram_bytes_per_launch")
+            return json.load(f).get(kernel_key, {})
     except Exception:
+        return {}
+
+
+def ncu_traffic(kernel_key):
+    """DRAM bytes per launch recorded from an ncu capture (profiles/ncu_traffic.json)."""
+    return _ncu_record(kernel_key).get("dram_bytes_per_launch")
+
+
+# Which probe measures each pipe's throughput (npbench_gb300.pipes): the integer
+# ALU pipe retires LOP3, the binary64 pipe DADD/DMUL/DFMA, the FMA pipes FFMA.
+PIPE_PROBES = {"alu": "lop3", "fp64": "dadd", "fma": "ffma"}
+
+
+def compute_roofline(kernel_key, achieved_ups, rates):
+    """The arithmetic roof of a binary64 kernel: thread instructions per lattice
+    update on each pipe (ncu's sm__inst_executed_pipe_*.sum of one launch x 32 /
+    updates per launch, profiles/ncu_traffic.json) against each pipe's throughput
+    measured in this run (pipe probes), and the issue rate of one instruction
+    per scheduler per clock.  The ceiling is the update rate at which the
+    busiest pipe (or issue) saturates."""
+    rec = _ncu_record(kernel_key).get("inst_per_update")
+    if not rec or not rates:
         return None
+    limits = {}
+    for pipe, probe in PIPE_PROBES.items():
+        n = rec.get(pipe, 0.0)
+        if n > 0 and rates.get(probe):
+            limits[pipe] = rates[probe] / n
+    if rec.get("issue") and rates.get("issue_slots"):
+        limits["issue"] = rates["issue_slots"] / rec["issue"]
+    if not limits:
+        return None
+    bound = min(limits, key=limits.get)
+    return {"bound": bound, "ceiling_updates_per_s": limits[bound], "achieved": achieved_ups,
+            "frac": achieved_ups / limits[bound], "unit": "updates/s",
+            "per_pipe_ceiling_updates_per_s": limits, "inst_per_update": rec,
+            "pipe_rates_ops_per_s": {k: rates.get(v) for k, v in PIPE_PROBES.items()},
+            "source": _ncu_record(kernel_key).get("inst_source")}
+
+
+def measure_pipes():
+    """Live pipe throughputs on this GPU (a fraction of a second), plus issue slots."""
+    import torch
+    from npbench_gb300 import pipes
+    rates = pipes.measure(target_ms=3.0, repeats=2)
+    props = torch.cuda.get_device_properties(0)
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            clk = float(json.load(f)["sm_max_mhz"]) * 1e6
+    except Exception:
+        clk = 2.07e9  # GB300's maximum SM clock
+    # one warp instruction per scheduler (4 per SM) per clock = 128 thread instructions
+    rates["issue_slots"] = props.multi_processor_count * 4 * 32 * clk
+    return rates
 
 
 class ClockSampler:
@@ -353,13 +404,19 @@ def run_gb300(args, world, rank, local):
                 "traffic": ncu_traffic("heat3d_f64_256"),
                 "kernel": "heat3d half-sweep float64", "alg_bytes_per_launch": alg_bytes,
                 "launch_ms": launch_ms}
-    # The binary64 arithmetic bound: the reference's operations per update at the
-    # achieved rate, against what the binary64 pipe alone retires.  Above 1 because
-    # most additions run exactly in fixed point on the integer pipes.
+    # The arithmetic bounds.  fp64_roofline: the reference's 13 binary64
+    # operations per update at the achieved rate, against what the binary64 pipe
+    # alone retires (measured now by the DADD probe); above 1 because most
+    # additions run exactly in fixed point on the integer pipes.
+    # compute_roofline: the kernel's own instruction mix against every pipe.
+    rates = measure_pipes() if rank == 0 else {}
     fp64_equiv = HEAT_FP64_OPS * INTERIOR / (launch_ms * 1e-3)
-    fp64_roof = {"ops_per_update": HEAT_FP64_OPS, "achieved_ops_per_s": fp64_equiv,
-                 "fp64_pipe_ops_per_s": FP64_PIPE_OPS, "frac": fp64_equiv / FP64_PIPE_OPS,
-                 "peak_kind": "probe of DADD/DMUL throughput on GB300"}
+    fp64_roof = None
+    if rates.get("dadd"):
+        fp64_roof = {"ops_per_update": HEAT_FP64_OPS, "achieved_ops_per_s": fp64_equiv,
+                     "fp64_pipe_ops_per_s": rates["dadd"], "frac": fp64_equiv / rates["dadd"],
+                     "peak_kind": "DADD pipe probe (npbench_gb300.pipes), measured in this run"}
+    comp_roof = compute_roofline("heat3d_f64_256", INTERIOR / (launch_ms * 1e-3), rates)
 
     # End to end through the public call with host buffers.
     hA = torch.from_numpy(A0).pin_memory()
@@ -431,6 +488,8 @@ def run_gb300(args, world, rank, local):
             "config": heat_config(world),
             "roofline": roofline,
             "fp64_roofline": fp64_roof,
+            "compute_roofline": comp_roof,
+            "pipe_rates_ops_per_s": dict(rates) if rates else None,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * A64.nbytes,
                     "d2h_bytes_per_step": 2 * A64.nbytes},
             "gpu_launches": HALF_SWEEPS * args.steps,
@@ -824,7 +883,7 @@ def _fp32_error_report(pairs):
     return out
 
 
-BATCH_FORM = "queue"
+BATCH_FORM = "stepped"
 BATCH_TILE_ROWS = 128
 
 

@@ -90,10 +90,12 @@ extern "C" {
                                          also the halo width; an even number up to
                                          64, 0 (default) = the library's choice.
                                          Reading returns the value in effect. */
-#define NPBGB_CFG_HEAT_TB 16          /* heat3d binary32: half-sweeps per launch, 2
-                                         (default; temporal blocking, where the
-                                         arrays meet the TMA rules and TSTEPS >= 4)
-                                         or 1.  Results are identical either way. */
+#define NPBGB_CFG_HEAT_TB 16          /* heat3d binary32: half-sweeps per launch.
+                                         2: two (temporal blocking) wherever the
+                                         arrays meet the TMA rules and TSTEPS >= 4;
+                                         1: one; 0 (default): two for arrays of
+                                         256 MiB and more, else one.  Results are
+                                         identical either way. */
 #define NPBGB_CFG_HEAT_TB_CHUNK 17    /* heat3d binary32 two-step kernel: axis-0
                                          planes per CTA; 0 (default) = automatic */
 
@@ -336,8 +338,9 @@ NPBGB_API int32_t npbgb_batch_destroy(npbgb_batch* batch);
  * runs one grid per call), so this is the serving counterpart of those calls.
  *
  * npbgb_queue_create: up to max_slots grids in flight; tile_rows / tile_planes
- *   are the Jacobi-2D rows and Heat-3D planes per tile (0 = 128 / 16; a grid's
- *   band_rows overrides); ctas_per_sm (2-4, 0 = 3) sizes the worker launch;
+ *   are the Jacobi-2D rows and Heat-3D planes per tile (0 = sized per grid for
+ *   about one tile per worker CTA, 8-256 rows or 4-64 planes; a grid's band_rows
+ *   overrides); ctas_per_sm (1-4, 0 = 3) sizes the worker launch;
  *   the worker ends after idle_us microseconds with nothing to do.  Device
  *   buffers and pinned host memory are allocated here, never later.
  * npbgb_queue_submit: takes a grid (npbgb_grid, step0/nsteps honoured) and

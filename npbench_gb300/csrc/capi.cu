@@ -25,7 +25,7 @@ int64_t g_cfg_batch_mode = 0;
 int64_t g_cfg_hdiff_emu = -1;  // -1: default mask
 int64_t g_cfg_jacobi1d_ctas = 0;   // 0: default
 int64_t g_cfg_jacobi1d_depth = 0;  // 0: default
-int64_t g_cfg_heat_tb = 2;         // binary32 Heat-3D half-sweeps per launch
+int64_t g_cfg_heat_tb = 0;         // binary32 Heat-3D half-sweeps per launch (0: by size)
 int64_t g_cfg_heat_tb_chunk = 0;   // 0: automatic
 int64_t jacobi1d_effective_depth();  // jacobi1d.cu
 int64_t jacobi1d_effective_ctas();
@@ -163,7 +163,7 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       g_cfg_jacobi1d_ctas = value;
       return NPBGB_OK;
     case NPBGB_CFG_HEAT_TB:
-      if (value != 1 && value != 2) return set_error(NPBGB_ERR_ARG, "heat TB: 1 or 2");
+      if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "heat TB: 0, 1 or 2");
       g_cfg_heat_tb = value;
       return NPBGB_OK;
     case NPBGB_CFG_HEAT_TB_CHUNK:

@@ -380,12 +380,18 @@ int32_t run_single_f32(float* a, float* b, int64_t n0, int64_t n1, int64_t n2, i
   return run_single<float, false>(a, b, n0, n1, n2, tsteps, st);
 }
 
-// Binary32 (HBM-bound) takes two half-sweeps per launch (heat_tb.cu) where
-// the arrays allow TMA; binary64 (bound by its arithmetic pipes) one.
+// Binary32 arrays well beyond L2 take two half-sweeps per launch (heat_tb.cu)
+// where the arrays allow TMA: measured on GB300, 512^3 17.6 -> 13.6 ms for
+// TSTEPS=30, no change at 384^3, and slower at 256^3, whose pair L2 largely
+// holds.  Binary64 (bound by its arithmetic pipes, not HBM) takes one.
+constexpr int64_t kTwoStepBytes = int64_t(256) << 20;  // per array, automatic choice
+
 template <typename T, bool FX>
 int32_t run(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps, cudaStream_t st) {
   if constexpr (sizeof(T) == 4) {
-    if (g_cfg_heat_tb == 2 && g_cfg_heat_tma && tsteps >= 4) {
+    const bool big = n0 * n1 * n2 * int64_t(sizeof(T)) >= kTwoStepBytes;
+    const bool two = g_cfg_heat_tb == 2 || (g_cfg_heat_tb == 0 && big);
+    if (two && g_cfg_heat_tma && tsteps >= 4) {
       const int32_t r = heat3d_tb2_run(a, b, n0, n1, n2, tsteps, st, run_single_f32);
       if (r != NPBGB_ERR_STATE) return r;
     }

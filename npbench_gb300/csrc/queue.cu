@@ -447,8 +447,10 @@ uint32_t take_queue_device_error() {
 // ---------------------------------------------------------------------------
 namespace qhost {
 
+// target_tiles: tiles per half-sweep the automatic tile extent aims at (about
+// the worker's CTA count, so that one grid alone still spreads over the GPU).
 int32_t describe(const npbgb_grid& G, int64_t g, int32_t tile_rows, int32_t tile_planes,
-                 QSlot* out, int64_t* updates) {
+                 QSlot* out, int64_t* updates, int64_t target_tiles) {
   *updates = 0;
   if (G.kind != NPBGB_KIND_JACOBI2D && G.kind != NPBGB_KIND_HEAT3D)
     return set_error(NPBGB_ERR_ARG, "queue: grid %lld: kind %d", (long long)g, G.kind);
@@ -488,17 +490,24 @@ int32_t describe(const npbgb_grid& G, int64_t g, int32_t tile_rows, int32_t tile
   out->steps = int32_t(todo) + (conv ? 2 : 0);
   out->cells = G.n0 * G.n1 * n2;
   int64_t ntiles;
+  const int64_t target = std::max<int64_t>(1, target_tiles);
   if (heat) {
-    const int32_t c = G.band_rows > 0 ? G.band_rows : (tile_planes > 0 ? tile_planes : 16);
-    out->chunk = c;
     out->tx = int32_t(cdiv(n2 - 2, hcore::kTK));
     out->ty = int32_t(cdiv(G.n1 - 2, hcore::kTJ));
+    // automatic: planes for about `target` tiles, 4 .. 64 (a tile streams them)
+    const int64_t autoc = std::min<int64_t>(64, std::max<int64_t>(
+        4, cdiv((G.n0 - 2) * out->tx * out->ty, target)));
+    const int32_t c = G.band_rows > 0 ? G.band_rows : (tile_planes > 0 ? tile_planes : int32_t(autoc));
+    out->chunk = c;
     ntiles = int64_t(out->tx) * out->ty * cdiv(G.n0 - 2, c);
   } else {
-    const int32_t c = G.band_rows > 0 ? G.band_rows : (tile_rows > 0 ? tile_rows : 128);
-    out->chunk = c;
     out->tx = int32_t(cdiv(G.n1 - 2, 32 * kQWarps));
     out->ty = 1;
+    // automatic: rows for about `target` tiles, 8 .. 256
+    const int64_t autoc = std::min<int64_t>(256, std::max<int64_t>(
+        8, cdiv((G.n0 - 2) * out->tx, target)));
+    const int32_t c = G.band_rows > 0 ? G.band_rows : (tile_rows > 0 ? tile_rows : int32_t(autoc));
+    out->chunk = c;
     ntiles = int64_t(out->tx) * cdiv(G.n0 - 2, c);
   }
   if (ntiles * (todo + 2) >= (int64_t(1) << 32))
@@ -534,6 +543,7 @@ struct npbgb_queue {
   int32_t max_slots = 0;
   uint32_t ring_size = 0, inbox_cap = 0;
   int32_t tile_rows = 0, tile_planes = 0, ctas_per_sm = 3;
+  int64_t target_tiles = 1;
   uint64_t idle_ns = 0;
   // device memory
   npbgb::qdev::QSlot* d_slots = nullptr;
@@ -632,6 +642,11 @@ int32_t npbgb_queue_create(int32_t max_slots, int32_t tile_rows, int32_t tile_pl
   q->tile_planes = tile_planes;
   q->ctas_per_sm = ctas_per_sm > 0 ? ctas_per_sm : 3;
   q->idle_ns = uint64_t(idle_us) * 1000ull;
+  {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, q->device);
+    q->target_tiles = int64_t(std::max(1, sms)) * qhost::slots_per_sm(q->ctas_per_sm, nullptr);
+  }
   cudaError_t e;
   const unsigned mapped = cudaHostAllocMapped | cudaHostAllocPortable;
   if ((e = cudaMalloc(&q->d_slots, sizeof(qdev::QSlot) * size_t(max_slots))) != cudaSuccess ||
@@ -665,7 +680,8 @@ int32_t npbgb_queue_submit(npbgb_queue* q, const npbgb_grid* grid, int32_t* slot
   qdev::QSlot d;
   int64_t updates = 0;
   std::lock_guard<std::mutex> lock(q->mu);
-  const int32_t r = qhost::describe(*grid, 0, q->tile_rows, q->tile_planes, &d, &updates);
+  const int32_t r = qhost::describe(*grid, 0, q->tile_rows, q->tile_planes, &d, &updates,
+                                    q->target_tiles);
   if (r != NPBGB_OK) return r;
   if (d.total == 0) return NPBGB_OK;  // nothing to do: finished at once
   if (load_acquire(q->h_ctl + 3) != 0u)
@@ -821,11 +837,16 @@ int32_t plan_static(const npbgb_grid* grids, int64_t count, int32_t tile_rows, i
   *out = nullptr;
   *updates = 0;
   *tiles = 0;
+  int sms0 = 0, dev0 = 0;
+  cudaGetDevice(&dev0);
+  cudaDeviceGetAttribute(&sms0, cudaDevAttrMultiProcessorCount, dev0);
+  const int64_t target = int64_t(std::max(1, sms0)) *
+                         slots_per_sm(ctas_per_sm > 0 ? ctas_per_sm : 3, nullptr);
   std::vector<qdev::QSlot> slots;
   for (int64_t g = 0; g < count; ++g) {
     qdev::QSlot d;
     int64_t up = 0;
-    const int32_t r = describe(grids[g], g, tile_rows, tile_rows, &d, &up);
+    const int32_t r = describe(grids[g], g, tile_rows, tile_rows, &d, &up, target);
     if (r != NPBGB_OK) return r;
     if (d.total == 0) continue;
     d.gen = 1;

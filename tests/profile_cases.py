@@ -23,6 +23,14 @@ batch_step 256 mixed grids, stepped form, one pass        batch_step, -s 20
 jacobi_f64_1000  Jacobi-2D 1000^2 float64, TSTEPS=3       jacobi2d_strip, -s 2
 jacobi1d   Jacobi-1D N=32000 float64, TSTEPS=64           jacobi1d_block, -s 2
 fdtd       FDTD-2D 1000x1200 float64, TMAX=3 (6 launches) fdtd_e / fdtd_h, -s 1
+heat_f32_tb Heat-3D 416^3 float32, TSTEPS=6: 4 two-step   heat3d_tb2, -s 1
+           launches, then one single-step pair
+heat_f32_384 Heat-3D 384^3 float32, TSTEPS=3, one step    heat3d_tma, -s 2
+           per launch
+batch1024  the first 1024 grids of the 4096-grid batch,   batch_step, -s 100
+           stepped form, TSTEPS as drawn (about 4 GB)
+queue_mix  240 small mixed grids through the tile queue   queue_worker, -c 1
+pipes      the seven pipe-rate probes                     pipe_probe, -c 7
 ========== ============================================== ===================
 """
 import os
@@ -102,6 +110,43 @@ def run(case):
         with Batch(work, band_rows=64) as bt:
             bt.launch()
             bt.launch()
+    elif case in ("heat_f32_tb", "heat_f32_384"):
+        n, T = (416, 6) if case == "heat_f32_tb" else (384, 3)
+        A, B = workloads.uniform_heat((n,) * 3, np.float32, seed=0)
+        a, b = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+        stencils.heat_3d_kernel(T, a, b)
+    elif case == "batch1024":
+        from npbench_gb300.batch import Batch
+        specs = workloads.batch_jacobi_specs(4096, seed=0)[:1024]
+        g = torch.Generator(device=dev)
+        g.manual_seed(0)
+        work = []
+        for (ny, nx), dtp, T in specs:
+            tdt = torch.float64 if dtp == np.float64 else torch.float32
+            work.append((torch.rand((ny, nx), dtype=tdt, device=dev, generator=g),
+                         torch.rand((ny, nx), dtype=tdt, device=dev, generator=g), T))
+        with Batch(work, band_rows=128, mode="stepped") as bt:
+            bt.launch()
+    elif case == "queue_mix":
+        from npbench_gb300.queue import TileQueue
+        rng = np.random.default_rng(0)
+        grids = []
+        for n in range(240):
+            dtp = torch.float32 if n % 3 else torch.float64
+            if n % 2:
+                shape = tuple(int(x) for x in rng.integers(64, 700, 2))
+            else:
+                shape = tuple(int(x) for x in rng.integers(16, 90, 3))
+            a = torch.rand(shape, dtype=dtp, device=dev)
+            grids.append((a, a.clone(), int(rng.integers(20, 200))))
+        with TileQueue(max_slots=256, ctas_per_sm=1) as q:
+            pending = {q.submit(a, b, T) for a, b, T in grids} - {-1}
+            while pending:
+                q.kick()
+                pending -= set(q.poll())
+    elif case == "pipes":
+        from npbench_gb300 import pipes
+        pipes.measure(target_ms=1.0, repeats=0)
     else:
         raise SystemExit(f"unknown case {case!r}")
     torch.cuda.synchronize()

@@ -799,11 +799,19 @@ def test_heat_f32_two_steps_per_launch(shape, tsteps):
         _lib.set_config(_lib.NPBGB_CFG_HEAT_TB_CHUNK, old[1])
 
 
-def test_heat_f32_two_steps_full_size_out_of_l2():
-    """384^3 binary32 (two 226 MB arrays, beyond L2): the two-step kernel against the oracle."""
-    A, B = workloads.uniform_heat((384, 384, 384), np.float32, seed=33)
+@pytest.mark.parametrize("n,tb", [(384, 2), (416, 0)])
+def test_heat_f32_two_steps_full_size_out_of_l2(n, tb):
+    """Binary32 grids beyond L2 against the oracle: 384^3 with the two-step kernel
+    forced, 416^3 (275 MB per array) where the automatic choice takes it."""
+    from npbench_gb300 import _lib
+    A, B = workloads.uniform_heat((n, n, n), np.float32, seed=33)
     dA, dB = _dev(A), _dev(B)
-    stencils.heat_3d_kernel(10, dA, dB)
+    old = _lib.set_config(_lib.NPBGB_CFG_HEAT_TB, tb)
+    try:
+        stencils.heat_3d_kernel(10, dA, dB)
+        _lib.device_status()
+    finally:
+        _lib.set_config(_lib.NPBGB_CFG_HEAT_TB, old)
     cref.heat_3d_kernel(10, A, B)
     assert bits_equal(_host(dA), A), first_diff(_host(dA), A)
     assert bits_equal(_host(dB), B)
