@@ -930,16 +930,18 @@ def batch_measure(n_grids=4096, steps=2, warmup=1, compare=True, compare_steps=1
             a.copy_(a0)
             b.copy_(b0)
 
-    from npbench_gb300 import precision
+    from npbench_gb300 import autotune, precision
     form = form or BATCH_FORM
-    rows = tile_rows or BATCH_TILE_ROWS
+    tuned = autotune.batch_settings([(s, dt) for s, dt, _ in specs])
+    rows = tile_rows or tuned.get("rows") or BATCH_TILE_ROWS
     promoted = [guard and dt == np.float32 and precision.needs_fp64("jacobi2d", T)
                 for _, dt, T in specs]
     ups = sum(2 * (T - 1) * (s[0] - 2) * (s[1] - 2) for s, _, T in specs)
     # algorithmic bytes: 2 x the element size per update, in the precision it runs in
     alg = sum(2 * (T - 1) * (s[0] - 2) * (s[1] - 2) * 2 * (8 if p else np.dtype(dt).itemsize)
               for (s, dt, T), p in zip(specs, promoted))
-    with Batch(work, band_rows=rows, mode=form, guard=guard) as batch:
+    with autotune.batch_applied(tuned), Batch(work, band_rows=rows, mode=form,
+                                              guard=guard) as batch:
         info = batch.info()
         with ClockSampler(0) as clk:
             ms = _timed_steps(torch, dev, stream, lambda: batch.launch(graph=True), reset,
@@ -954,6 +956,8 @@ def batch_measure(n_grids=4096, steps=2, warmup=1, compare=True, compare_steps=1
            "tiles" if info["mode"] != "persistent" else "bands": info["bands"],
            "launches" if info["mode"] == "stepped" else "ctas": info["ctas"],
            "rows_per_tile": rows, "graph": True,
+           "tuned": {"class": autotune.batch_key([(s, dt) for s, dt, _ in specs]),
+                     "settings": dict(tuned, rows=rows)},
            "fp64_guard": {"on": bool(guard), "float32_grids_run_in_float64": int(sum(promoted)),
                           "float32_grids": int(sum(dt == np.float32 for _, dt, _ in specs))},
            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
@@ -1048,7 +1052,9 @@ def serve_measure(rates=(200.0, 1000.0, 5000.0), n_requests=100, compare=True, f
                                       _materialise)
     with StencilServer() as warm:
         warm.submit(Request(shape=(64, 64), dtype=np.float32, tsteps=5, seed=1)).result()
+    from npbench_gb300 import autotune
     out = {"requests_per_rate": n_requests, "hbm_budget_gb": 150, "rates": [],
+           "tuned": {"class": autotune.server_key(), "settings": autotune.server_settings()},
            "inputs": "seeded U[0,1) host arrays in pinned memory, uploaded by the server "
                      "(and by the comparator) inside the measured span; results stay on "
                      "the device"}

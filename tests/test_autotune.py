@@ -26,11 +26,17 @@ def cache(tmp_path, monkeypatch):
     autotune.load_cache(refresh=True)
 
 
-def test_keys_name_benchmark_dtype_and_shape():
-    assert autotune.key("jacobi_2d", (2800, 2800), np.float64) == "jacobi_2d/float64/2800x2800"
-    assert autotune.key("heat_3d", [120, 120, 120], "float32") == "heat_3d/float32/120x120x120"
+def test_keys_name_benchmark_dtype_and_shape_class():
+    assert autotune.shape_class((2800, 2800)) == (11, 11)
+    assert autotune.key("jacobi_2d", (2800, 2800), np.float64) == "jacobi_2d/float64/c11x11"
+    assert autotune.key("heat_3d", [120, 120, 120], "float32") == "heat_3d/float32/c6x6x6"
+    # grids within a factor of two share a class
+    assert autotune.key("heat_3d", (256,) * 3, "float64") == autotune.key("heat_3d", (511, 300, 257),
+                                                                         "float64")
+    assert autotune.key("heat_3d", (256,) * 3, "float64") != autotune.key("heat_3d", (255, 256, 256),
+                                                                         "float64")
     torch = pytest.importorskip("torch")
-    assert autotune.key("heat_3d", (4, 5, 6), torch.float64) == "heat_3d/float64/4x5x6"
+    assert autotune.key("heat_3d", (4, 5, 6), torch.float64) == "heat_3d/float64/c2x2x2"
 
 
 def test_search_spaces():
@@ -38,6 +44,9 @@ def test_search_spaces():
     assert {"JACOBI_HW_WARPS": 4, "JACOBI_CHUNK": 3} in sp and len(sp) == 49
     assert all(c["JACOBI_HW_WARPS"] == -1 for c in autotune._space("jacobi_2d", np.float32))
     heat = autotune._space("heat_3d", np.float64)
+    assert all("HEAT_TB" not in c for c in heat)
+    f32 = autotune._space("heat_3d", np.float32)
+    assert {c["HEAT_TB"] for c in f32} == {1, 2}  # temporal depth is a knob in binary32
     assert {"HEAT_ROWS": 2, "HEAT_HW_ROWS": 4, "HEAT_CHUNK": 8} in heat
     assert {"HEAT_ROWS": 2, "HEAT_HW_ROWS": 5, "HEAT_CHUNK": 8} in heat
     assert {"HEAT_ROWS": 2, "HEAT_HW_ROWS": 7, "HEAT_CHUNK": 8} in heat
@@ -46,7 +55,7 @@ def test_search_spaces():
 
 
 def test_cached_setting_applies_for_the_call_only(cache):
-    cache.write_text(json.dumps({"jacobi_2d/float64/40x50": {
+    cache.write_text(json.dumps({"jacobi_2d/float64/c5x5": {
         "config": {"JACOBI_HW_WARPS": 6, "JACOBI_CHUNK": 5}, "ms": 1.0, "default_ms": 2.0}}))
     autotune.load_cache(refresh=True)
     before = (_lib.get_config(_lib.NPBGB_CFG_JACOBI_HW_WARPS),
@@ -59,10 +68,55 @@ def test_cached_setting_applies_for_the_call_only(cache):
         assert cfg == {"JACOBI_HW_WARPS": 6, "JACOBI_CHUNK": 5}
         assert _lib.get_config(_lib.NPBGB_CFG_JACOBI_HW_WARPS) == 6
         assert _lib.get_config(_lib.NPBGB_CFG_JACOBI_CHUNK) == 5
-    with autotune.applied("jacobi_2d", (41, 50), np.float64) as cfg:  # other shape: nothing
+    # an unseen shape of the same class gets the setting; another class does not
+    with autotune.applied("jacobi_2d", (61, 33), np.float64) as cfg:
+        assert cfg == {"JACOBI_HW_WARPS": 6, "JACOBI_CHUNK": 5}
+        assert _lib.get_config(_lib.NPBGB_CFG_JACOBI_CHUNK) == 5
+    with autotune.applied("jacobi_2d", (64, 50), np.float64) as cfg:
         assert cfg is None
     assert (_lib.get_config(_lib.NPBGB_CFG_JACOBI_HW_WARPS),
             _lib.get_config(_lib.NPBGB_CFG_JACOBI_CHUNK)) == before
+
+
+def test_batch_and_server_settings_by_class(cache):
+    """The batch's tile rows and the server's split come from the class of the batch
+    (grid count, median size, dtype mix) and of the stream; an unseen batch of the
+    same class gets the tuned rows."""
+    batch = [((100 + i, 200), np.float32 if i % 2 else np.float64) for i in range(300)]
+    k = autotune.batch_key(batch)
+    assert k == "batch/mixed/n8/m15"
+    cache.write_text(json.dumps({
+        k: {"config": {"rows": 64, "JACOBI_HW_WARPS": 6}},
+        "serve/mixed": {"config": {"direct_cells": 262144, "ctas_per_sm": 2, "big_lanes": 1}}}))
+    autotune.load_cache(refresh=True)
+    autotune.enable()
+    other = [((120, 150 + i), np.float64 if i % 3 else np.float32) for i in range(400)]
+    assert autotune.batch_key(other) == k
+    got = autotune.batch_settings(other)
+    assert got == {"rows": 64, "JACOBI_HW_WARPS": 6}
+    before = _lib.get_config(_lib.NPBGB_CFG_JACOBI_HW_WARPS)
+    with autotune.batch_applied(got):
+        assert _lib.get_config(_lib.NPBGB_CFG_JACOBI_HW_WARPS) == 6
+    assert _lib.get_config(_lib.NPBGB_CFG_JACOBI_HW_WARPS) == before
+    assert autotune.batch_settings([((10, 10), np.float32)])["rows"] == 128  # no entry: default
+    assert autotune.server_settings() == {"direct_cells": 262144, "ctas_per_sm": 2,
+                                          "big_lanes": 1}
+    autotune.disable()
+    assert autotune.server_settings()["direct_cells"] == 1 << 20
+
+
+def test_shipped_table_is_consulted_after_the_user_cache(cache, monkeypatch, tmp_path):
+    shipped = tmp_path / "shipped.json"
+    shipped.write_text(json.dumps({"heat_3d/float64/c8x8x8": {"config": {"HEAT_CHUNK": 8}},
+                                   "heat_3d/float32/c8x8x8": {"config": {"HEAT_TB": 2}}}))
+    original = autotune.SHIPPED_PATH
+    monkeypatch.setattr(autotune, "SHIPPED_PATH", str(shipped))
+    cache.write_text(json.dumps({"heat_3d/float32/c8x8x8": {"config": {"HEAT_TB": 1}}}))
+    autotune.load_cache(refresh=True)
+    assert autotune.lookup("heat_3d/float64/c8x8x8")["config"] == {"HEAT_CHUNK": 8}
+    assert autotune.lookup("heat_3d/float32/c8x8x8")["config"] == {"HEAT_TB": 1}
+    monkeypatch.setattr(autotune, "SHIPPED_PATH", original)
+    autotune.load_cache(refresh=True)
 
 
 def test_store_merges_entries(cache):
