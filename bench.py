@@ -128,8 +128,9 @@ def ncu_traffic(kernel_key):
 
 
 # Which probe measures each pipe's throughput (npbench_gb300.pipes): the integer
-# ALU pipe retires LOP3, the binary64 pipe DADD/DMUL/DFMA, the FMA pipes FFMA.
-PIPE_PROBES = {"alu": "lop3", "fp64": "dadd", "fma": "ffma"}
+# ALU pipe retires LOP3, the binary64 pipe DADD/DMUL/DFMA; the stencils' FMA-pipe
+# instructions are integer multiply-adds on its heavy half, whose rate IMAD measures.
+PIPE_PROBES = {"alu": "lop3", "fp64": "dadd", "fma": "imad"}
 
 
 def compute_roofline(kernel_key, achieved_ups, rates):
@@ -962,7 +963,9 @@ def batch_measure(n_grids=4096, steps=2, warmup=1, compare=True, compare_steps=1
                           "float32_grids": int(sum(dt == np.float32 for _, dt, _ in specs))},
            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                         "frac": ach / peak, "peak_kind": kind,
-                        "traffic": ncu_traffic("batch_4096")},
+                        "traffic": ncu_traffic("batch_4096"),
+                        "traffic_over_algorithmic":
+                            _ncu_record("batch_4096").get("traffic_over_algorithmic")},
            "clocks": clk.summary()}
     if compare:
         ms_pg = _timed_steps(torch, dev, stream, lambda: _per_grid_guarded(work, guard), reset,

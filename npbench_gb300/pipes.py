@@ -35,7 +35,7 @@ def measure(ops=tuple(OPS), target_ms=5.0, ctas_per_sm=8, repeats=3):
         best = None
         for attempt in range(8):
             times = []
-            for _ in range(repeats + 1):
+            for _ in range(max(1, repeats) + 1):
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
                 _lib.check(lib.npbgb_probe_pipe(op, iters, ctas, sink.data_ptr(),
