@@ -108,6 +108,7 @@ class Request:
     t_admit: float = 0.0
     t_done: float = 0.0
     promoted: bool = False
+    path: str = ""        # "queue" (tile queue) or "lane" (big-grid lane)
     dev: dict = field(default=None, repr=False)
     out: tuple = field(default=None, repr=False)
     future: concurrent.futures.Future = field(default=None, repr=False)
@@ -193,7 +194,8 @@ class StencilServer:
 
     def __init__(self, device=0, hbm_budget_bytes=150e9, max_slots=4096, tile_rows=0,
                  tile_planes=0, ctas_per_sm=None, idle_us=500, fp64_guard=True,
-                 reserve_bytes=8 << 30, poll_s=2e-4, direct_cells=None, big_lanes=None):
+                 reserve_bytes=8 << 30, poll_s=2e-4, direct_cells=None, big_lanes=None,
+                 lane_order="sjf"):
         """direct_cells (grids from this many cells go to a big-grid lane),
         ctas_per_sm (the queue worker's CTAs per SM) and big_lanes default to the
         tuned settings of the serving loop (``autotune.server_settings``)."""
@@ -214,6 +216,9 @@ class StencilServer:
         self.poll_s = float(poll_s)
         self.direct_cells = int(direct_cells)
         self.big_lanes = max(1, int(big_lanes))
+        if lane_order not in ("sjf", "fifo"):
+            raise ValueError("lane_order: 'sjf' (shortest job first) or 'fifo'")
+        self.lane_order = lane_order
         self.queued_small = self.ran_big = 0
         self._queue = collections.deque()
         self._cv = threading.Condition()
@@ -392,6 +397,7 @@ class StencilServer:
                         still.append((req, ev))
                         continue
                     if req.cells >= self.direct_cells and req.updates > 0:
+                        req.path = "lane"
                         big_ready.append(req)
                         moved = True
                         continue
@@ -407,6 +413,7 @@ class StencilServer:
                         returning.append((req, self._deliver(req)))
                     else:
                         resident[slot] = req
+                        req.path = "queue"
                         self.queued_small += 1
                 staging = still
                 for ln in lanes:
@@ -415,7 +422,8 @@ class StencilServer:
                         ln["req"] = None
                         moved = True
                     if ln["req"] is None and big_ready:
-                        nxt = min(big_ready, key=lambda r: r.updates)  # shortest job first
+                        nxt = (min(big_ready, key=lambda r: r.updates)  # shortest job first
+                               if self.lane_order == "sjf" else big_ready[0])
                         big_ready.remove(nxt)
                         ln["req"], ln["ev"] = nxt, self._run_big(nxt, ln["stream"])
                         self.ran_big += 1
