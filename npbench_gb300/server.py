@@ -195,15 +195,18 @@ class StencilServer:
     def __init__(self, device=0, hbm_budget_bytes=150e9, max_slots=4096, tile_rows=0,
                  tile_planes=0, ctas_per_sm=None, idle_us=500, fp64_guard=True,
                  reserve_bytes=8 << 30, poll_s=2e-4, direct_cells=None, big_lanes=None,
-                 lane_order="sjf"):
+                 lane_order=None):
         """direct_cells (grids from this many cells go to a big-grid lane),
-        ctas_per_sm (the queue worker's CTAs per SM) and big_lanes default to the
-        tuned settings of the serving loop (``autotune.server_settings``)."""
+        ctas_per_sm (the queue worker's CTAs per SM), big_lanes (big grids run
+        concurrently, one per lane) and lane_order ("sjf": shortest job first,
+        or "fifo") default to the tuned settings of the serving loop
+        (``autotune.server_settings``)."""
         from . import autotune
         tuned = autotune.server_settings()
         direct_cells = tuned["direct_cells"] if direct_cells is None else direct_cells
         ctas_per_sm = tuned["ctas_per_sm"] if ctas_per_sm is None else ctas_per_sm
         big_lanes = tuned["big_lanes"] if big_lanes is None else big_lanes
+        lane_order = tuned.get("lane_order", "sjf") if lane_order is None else lane_order
         import torch
         self.device = torch.device("cuda", device) if isinstance(device, int) else \
             torch.device(device)

@@ -102,7 +102,7 @@ def test_batch_and_server_settings_by_class(cache):
     assert autotune.server_settings() == {"direct_cells": 262144, "ctas_per_sm": 2,
                                           "big_lanes": 1}
     autotune.disable()
-    assert autotune.server_settings()["direct_cells"] == 1 << 20
+    assert autotune.server_settings()["direct_cells"] == 1 << 18
 
 
 def test_shipped_table_is_consulted_after_the_user_cache(cache, monkeypatch, tmp_path):
