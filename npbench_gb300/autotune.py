@@ -363,7 +363,7 @@ def tune_batch(n_grids=512, seed=0, rows=(32, 64, 128, 256), hw_warps=(-1, 2, 6)
 # ---------------------------------------------------------------------------
 # The server
 # ---------------------------------------------------------------------------
-_SERVER_DEFAULT = {"direct_cells": 1 << 18, "ctas_per_sm": 1, "big_lanes": 2, "lane_order": "sjf"}
+_SERVER_DEFAULT = {"direct_cells": 1 << 18, "ctas_per_sm": 1, "big_lanes": 3, "lane_order": "fifo"}
 
 
 def server_key(stream="mixed"):

@@ -48,21 +48,14 @@ constexpr int kYOff = 2;              // tile row jj lives at box row jj + kYOff
 constexpr int kPlaneBytes = kBoxX * kBoxY * 4;                 // 5760
 constexpr int kStageStride = (kPlaneBytes + 127) / 128 * 128;  // 5760
 constexpr int kStages = 6;
-constexpr int kS1 = kTile + 2;        // step t+1 region (34 rows of tile rows -1 .. 32)
-constexpr int kS1Pitch = 36;          // row pitch of a step t+1 plane; tile column kk at kk + 2
+constexpr int kS1 = kTile + 2;        // step t+1 region (34)
+constexpr int kS1Pitch = 36;          // row pitch of a step t+1 plane
 constexpr int kS1Planes = 4;
 constexpr int kThreads = 256;
 constexpr size_t kSmemBytes = size_t(kStages) * kStageStride +
                               size_t(kS1Planes) * kS1 * kS1Pitch * 4 + kStages * 8;
 
 __device__ unsigned int g_heat_tb_error;  // bit 0: an mbarrier wait timed out
-
-// 64-bit shared-memory load of an aligned pair of floats, as an f32x2 operand.
-__device__ __forceinline__ F2 lds2(uint32_t addr) {
-  F2 r;
-  asm volatile("ld.shared.b64 %0, [%1];" : "=l"(r.v) : "r"(addr));
-  return r;
-}
 
 __global__ void __launch_bounds__(kThreads)
 heat3d_tb2(const __grid_constant__ CUtensorMap src_map, const float* __restrict__ odd_faces,
@@ -72,7 +65,7 @@ heat3d_tb2(const __grid_constant__ CUtensorMap src_map, const float* __restrict_
   float* s1 = reinterpret_cast<float*>(smem + kStages * kStageStride);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kStages * kStageStride +
                                                kS1Planes * kS1 * kS1Pitch * 4);
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t k0 = 1 + int64_t(blockIdx.x) * kTile, j0 = 1 + int64_t(blockIdx.y) * kTile;
   const int64_t ib = 1 + int64_t(blockIdx.z) * chunk;
   const int64_t ie = (ib + chunk < n0 - 1) ? ib + chunk : n0 - 1;  // output planes [ib, ie)
@@ -85,6 +78,9 @@ heat3d_tb2(const __grid_constant__ CUtensorMap src_map, const float* __restrict_
   // or past the end read as zeros and are never used.
   const int x0 = int(k0) - kXOff, y0 = int(j0) - kYOff;
 
+  auto stage = [&](int64_t q) -> const float* {
+    return reinterpret_cast<const float*>(smem + int((q - qlo) % kStages) * kStageStride);
+  };
   auto issue = [&](int64_t q) {
     const int st = int((q - qlo) % kStages);
     uint64_t* bar = &bars[st];
@@ -111,17 +107,6 @@ heat3d_tb2(const __grid_constant__ CUtensorMap src_map, const float* __restrict_
   bool ok = true;
 
   // Step t+1 planes p = ib-1 .. ie; after each, step t+2 plane p-1.
-  //
-  // Both steps work on pairs of adjacent columns: one 64-bit shared load gives
-  // a pair's centre values as the f32x2 operand, its neighbours along axis 2
-  // come from the pairs either side, and each packed instruction rounds both
-  // points exactly as the scalar operator would.  Step t+1 covers the 34 x 34
-  // region (tile plus a halo of one) as 34 rows of 17 pairs, starting at an
-  // odd tile column (box columns are even there); step t+2 the 32 x 32 tile as
-  // 32 rows of 16 pairs.  Both are spread over all 256 threads.
-  const uint32_t sbase = tma::smem_u32(smem);
-  const uint32_t s1base = tma::smem_u32(s1);
-  constexpr int kS1Items = kS1 * 17, kS2Items = kTile * 16;
   for (int64_t p = ib - 1; p <= ie; ++p) {
     float* out1 = s1p(p);
     if (p == 0 || p == n0 - 1) {
@@ -130,7 +115,7 @@ heat3d_tb2(const __grid_constant__ CUtensorMap src_map, const float* __restrict_
       for (int e = tid; e < kS1 * kS1; e += kThreads) {
         const int jj = e / kS1 - 1, kk = e % kS1 - 1;
         const int64_t j = j0 + jj, k = k0 + kk;
-        out1[(jj + 1) * kS1Pitch + kk + 2] = (j < n1 && k < n2) ? __ldg(fp + j * n2 + k) : 0.0f;
+        out1[(jj + 1) * kS1Pitch + kk + 1] = (j < n1 && k < n2) ? __ldg(fp + j * n2 + k) : 0.0f;
       }
     } else {
       while (waited < p + 1 && ok) {
@@ -138,29 +123,61 @@ heat3d_tb2(const __grid_constant__ CUtensorMap src_map, const float* __restrict_
         ok = wait(waited);
       }
       if (ok) {
-        const uint32_t pm = sbase + uint32_t((p - 1 - qlo) % kStages) * kStageStride;
-        const uint32_t pc = sbase + uint32_t((p - qlo) % kStages) * kStageStride;
-        const uint32_t pn = sbase + uint32_t((p + 1 - qlo) % kStages) * kStageStride;
-        const float* fp = odd_faces + p * s0;
-        for (int q = tid; q < kS1Items; q += kThreads) {
-          const int r = q / 17, b = 4 + 2 * (q - r * 17);  // box column of the pair (even)
-          const int jj = r - 1, kk = b - kXOff;              // tile position of its first cell
-          const uint32_t o = uint32_t(((jj + kYOff) * kBoxX + b) * 4);
-          const F2 c = lds2(pc + o), vl = lds2(pc + o - 8), vr = lds2(pc + o + 8);
-          const F2 v = hcore::heat_point2(c, lds2(pn + o), lds2(pm + o), lds2(pc + o + 4 * kBoxX),
-                                          lds2(pc + o - 4 * kBoxX), f2(f2y(c), f2x(vr)),
-                                          f2(f2y(vl), f2x(c)));
-          float x = f2x(v), y = f2y(v);
-          if (edge) {
-            // cells of the odd step on a face along axis 1 or 2 keep B's value
-            const int64_t j = j0 + jj, k = k0 + kk;
-            const bool jface = j == 0 || j == n1 - 1;
-            if (j < n1 && k < n2 && (jface || k == 0 || k == n2 - 1)) x = __ldg(fp + j * n2 + k);
-            if (j < n1 && k + 1 < n2 && (jface || k + 1 == n2 - 1)) y = __ldg(fp + j * n2 + k + 1);
+        const float* pm = stage(p - 1);
+        const float* pc = stage(p);
+        const float* pn = stage(p + 1);
+        // main 32 x 32: warp rows 4w .. 4w+3, lane = column; rows in packed pairs
+#pragma unroll
+        for (int r = 0; r < 4; r += 2) {
+          const int jj = warp * 4 + r, kk = lane;
+          const int o = (jj + kYOff) * kBoxX + kk + kXOff;
+          const F2 v = hcore::heat_point2(f2(pc[o], pc[o + kBoxX]), f2(pn[o], pn[o + kBoxX]),
+                                          f2(pm[o], pm[o + kBoxX]),
+                                          f2(pc[o + kBoxX], pc[o + 2 * kBoxX]),
+                                          f2(pc[o - kBoxX], pc[o]), f2(pc[o + 1], pc[o + 1 + kBoxX]),
+                                          f2(pc[o - 1], pc[o - 1 + kBoxX]));
+          out1[(jj + 1) * kS1Pitch + kk + 1] = f2x(v);
+          out1[(jj + 2) * kS1Pitch + kk + 1] = f2y(v);
+        }
+        // the ring around it: rows -1 and 32 (34 each), columns -1 and 32 (32 each)
+        if (tid < 132) {
+          int jj, kk;
+          if (tid < 68) {
+            jj = tid < 34 ? -1 : kTile;
+            kk = (tid % 34) - 1;
+          } else {
+            const int t = tid - 68;
+            kk = t < 32 ? -1 : kTile;
+            jj = t % 32;
           }
-          float* w = out1 + (jj + 1) * kS1Pitch + kk + 2;
-          w[0] = x;
-          w[1] = y;
+          const int o = (jj + kYOff) * kBoxX + kk + kXOff;
+          out1[(jj + 1) * kS1Pitch + kk + 1] =
+              hcore::heat_point<float>(pc[o], pn[o], pm[o], pc[o + kBoxX], pc[o - kBoxX], pc[o + 1],
+                                pc[o - 1]);
+        }
+        if (edge) {
+          // Cells of the odd step on a face along axis 1 or 2 keep B's value;
+          // this CTA's own evaluations there must not be used.  Each thread
+          // fixes the cells it wrote above.
+          const float* fp = odd_faces + p * s0;
+          auto fix = [&](int jj, int kk) {
+            const int64_t j = j0 + jj, k = k0 + kk;
+            if (j < n1 && k < n2 && (j == 0 || k == 0 || j == n1 - 1 || k == n2 - 1))
+              out1[(jj + 1) * kS1Pitch + kk + 1] = __ldg(fp + j * n2 + k);
+          };
+          for (int r = 0; r < 4; ++r) fix(warp * 4 + r, lane);
+          if (tid < 132) {
+            int jj, kk;
+            if (tid < 68) {
+              jj = tid < 34 ? -1 : kTile;
+              kk = (tid % 34) - 1;
+            } else {
+              const int t = tid - 68;
+              kk = t < 32 ? -1 : kTile;
+              jj = t % 32;
+            }
+            fix(jj, kk);
+          }
         }
       }
     }
@@ -172,24 +189,26 @@ heat3d_tb2(const __grid_constant__ CUtensorMap src_map, const float* __restrict_
     // Input plane p-1 is no longer needed: refill its buffer kStages planes on.
     if (tid == 0 && p - 1 >= qlo && p - 1 + kStages <= qhi) issue(p - 1 + kStages);
     // Step t+2, plane p-1, from step t+1 planes p-2, p-1, p.
-    const int64_t op = p - 1;
-    if (op >= ib) {
-      const uint32_t qm = s1base + uint32_t((op - 1) & 3) * (kS1 * kS1Pitch * 4);
-      const uint32_t qc = s1base + uint32_t(op & 3) * (kS1 * kS1Pitch * 4);
-      const uint32_t qn = s1base + uint32_t((op + 1) & 3) * (kS1 * kS1Pitch * 4);
-      float* drow = dst + op * s0;
-      for (int q = tid; q < kS2Items; q += kThreads) {
-        const int jj = q >> 4, kk = (q & 15) * 2;
-        const uint32_t o = uint32_t(((jj + 1) * kS1Pitch + kk + 2) * 4);
-        const F2 c = lds2(qc + o), vl = lds2(qc + o - 8), vr = lds2(qc + o + 8);
-        const F2 v = hcore::heat_point2(c, lds2(qn + o), lds2(qm + o), lds2(qc + o + 4 * kS1Pitch),
-                                        lds2(qc + o - 4 * kS1Pitch), f2(f2y(c), f2x(vr)),
-                                        f2(f2y(vl), f2x(c)));
-        const int64_t j = j0 + jj, k = k0 + kk;
-        if (j < n1 - 1) {
-          float* g = drow + j * n2 + k;
-          if (k < n2 - 1) g[0] = f2x(v);
-          if (k + 1 < n2 - 1) g[1] = f2y(v);
+    const int64_t o = p - 1;
+    if (o >= ib) {
+      const float* qm = s1p(o - 1);
+      const float* qc = s1p(o);
+      const float* qn = s1p(o + 1);
+      const int kk = lane;
+      const int64_t k = k0 + kk;
+#pragma unroll
+      for (int r = 0; r < 4; r += 2) {
+        const int jj = warp * 4 + r;
+        const int c = (jj + 1) * kS1Pitch + kk + 1;
+        const F2 v = hcore::heat_point2(f2(qc[c], qc[c + kS1Pitch]), f2(qn[c], qn[c + kS1Pitch]),
+                                        f2(qm[c], qm[c + kS1Pitch]),
+                                        f2(qc[c + kS1Pitch], qc[c + 2 * kS1Pitch]),
+                                        f2(qc[c - kS1Pitch], qc[c]), f2(qc[c + 1], qc[c + 1 + kS1Pitch]),
+                                        f2(qc[c - 1], qc[c - 1 + kS1Pitch]));
+        const int64_t j = j0 + jj;
+        if (k < n2 - 1) {
+          if (j < n1 - 1) dst[o * s0 + j * n2 + k] = f2x(v);
+          if (j + 1 < n1 - 1) dst[o * s0 + (j + 1) * n2 + k] = f2y(v);
         }
       }
     }
