@@ -98,6 +98,12 @@ extern "C" {
                                          identical either way. */
 #define NPBGB_CFG_HEAT_TB_CHUNK 17    /* heat3d binary32 two-step kernel: axis-0
                                          planes per CTA; 0 (default) = automatic */
+#define NPBGB_CFG_JACOBI_BANDS 18     /* jacobi2d: the whole time loop in one launch with
+                                         bands of rows resident in shared memory.
+                                         0 (default): when the bands fit, the grid has
+                                         2^18 cells or more and 16 half-sweeps or more;
+                                         1: never; 2: whenever the bands fit.  Results
+                                         are identical either way. */
 
 /* Batch forms. */
 #define NPBGB_BATCH_PERSISTENT 1
@@ -189,7 +195,10 @@ NPBGB_API int32_t npbgb_probe_pipe(int32_t op, int64_t iters, int32_t ctas, void
  * A -> B and then B -> A over the interior [1, ny-1) x [1, nx-1):
  *   dst = 0.2 * ((((c + w) + e) + s) + n)
  * Boundary rows and columns are never written.  On return A holds the newest
- * field and B the previous one, as in the reference.  tsteps <= 1 is a no-op. */
+ * field and B the previous one, as in the reference.  tsteps <= 1 is a no-op.
+ * Grids whose bands of rows fit in shared memory run the whole loop in one
+ * cooperative launch (NPBGB_CFG_JACOBI_BANDS; its exchange rows come from a
+ * stream-ordered pool), others one chained launch per half-sweep. */
 NPBGB_API int32_t npbgb_jacobi2d(void* A, void* B, int64_t ny, int64_t nx, int32_t tsteps,
                        int32_t dtype, void* stream);
 

@@ -27,6 +27,7 @@ int64_t g_cfg_jacobi1d_ctas = 0;   // 0: default
 int64_t g_cfg_jacobi1d_depth = 0;  // 0: default
 int64_t g_cfg_heat_tb = 0;         // binary32 Heat-3D half-sweeps per launch (0: by size)
 int64_t g_cfg_heat_tb_chunk = 0;   // 0: automatic
+int64_t g_cfg_jacobi_bands = 0;    // 0: automatic, 1: off, 2: whenever the bands fit
 int64_t jacobi1d_effective_depth();  // jacobi1d.cu
 int64_t jacobi1d_effective_ctas();
 
@@ -35,6 +36,7 @@ uint32_t take_batch_device_error();
 uint32_t take_cfd_device_error();
 uint32_t take_queue_device_error();
 uint32_t take_heat_tb_device_error();
+uint32_t take_jacobi_bands_device_error();
 int32_t launch_wait_timeout_selftest(uint64_t limit_ns, cudaStream_t st);
 
 int32_t set_error(int32_t code, const char* fmt, ...) {
@@ -170,6 +172,10 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       if (value < 0 || value > 65535) return set_error(NPBGB_ERR_ARG, "heat TB chunk: 0 .. 65535");
       g_cfg_heat_tb_chunk = value;
       return NPBGB_OK;
+    case NPBGB_CFG_JACOBI_BANDS:
+      if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "jacobi bands: 0, 1 or 2");
+      g_cfg_jacobi_bands = value;
+      return NPBGB_OK;
     case NPBGB_CFG_JACOBI1D_DEPTH:
       if (value < 0 || value > 64 || (value & 1))
         return set_error(NPBGB_ERR_ARG, "jacobi1d depth: 0 or an even number up to 64");
@@ -200,6 +206,7 @@ int32_t npbgb_get_config(int32_t key, int64_t* value) {
     case NPBGB_CFG_JACOBI1D_DEPTH: *value = jacobi1d_effective_depth(); return NPBGB_OK;
     case NPBGB_CFG_HEAT_TB: *value = g_cfg_heat_tb; return NPBGB_OK;
     case NPBGB_CFG_HEAT_TB_CHUNK: *value = g_cfg_heat_tb_chunk; return NPBGB_OK;
+    case NPBGB_CFG_JACOBI_BANDS: *value = g_cfg_jacobi_bands; return NPBGB_OK;
     default: return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
   }
 }
@@ -210,13 +217,13 @@ int32_t npbgb_device_status(void* stream) {
   if (e != cudaSuccess) return cuda_status(e, "device status");
   const uint32_t h = take_heat_device_error() | take_heat_tb_device_error();
   const uint32_t bt = take_batch_device_error();
-  const uint32_t cf = take_cfd_device_error();
+  const uint32_t cf = take_cfd_device_error() | take_jacobi_bands_device_error();
   const uint32_t qu = take_queue_device_error();
   if (h == 0xffffffffu || bt == 0xffffffffu || cf == 0xffffffffu || qu == 0xffffffffu)
     return set_error(NPBGB_ERR_CUDA, "reading the device error words");
   if (h) return set_error(NPBGB_ERR_TIMEOUT, "a bounded device wait gave up (heat3d)");
   if (bt) return set_error(NPBGB_ERR_TIMEOUT, "a batch CTA made no progress within its limit");
-  if (cf) return set_error(NPBGB_ERR_TIMEOUT, "a cavity_flow band waited on its neighbours past its limit");
+  if (cf) return set_error(NPBGB_ERR_TIMEOUT, "a band waited on its neighbours past its limit");
   if (qu & 1u) return set_error(NPBGB_ERR_TIMEOUT, "a queue worker saw no tile complete within its limit");
   if (qu) return set_error(NPBGB_ERR_STATE, "a queue worker found an invalid inbox entry");
   return NPBGB_OK;

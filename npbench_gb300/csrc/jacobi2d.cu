@@ -22,6 +22,9 @@ extern int64_t g_cfg_f64_emulation;
 extern int64_t g_cfg_jacobi_chunk;
 extern int64_t g_cfg_jacobi_hw_warps;
 
+template <typename T>
+int32_t jacobi2d_bands_run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st);
+
 namespace {
 
 constexpr int kWarps = 8;
@@ -64,6 +67,10 @@ int pick_chunk(int64_t ny, int64_t col_blocks) {
 template <typename T, bool FX>
 int32_t run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st) {
   if (tsteps <= 1 || ny < 3 || nx < 3) return NPBGB_OK;
+  {
+    const int32_t r = jacobi2d_bands_run<T>(a, b, ny, nx, tsteps, st);
+    if (r != NPBGB_ERR_STATE) return r;
+  }
   const int64_t gx = cdiv(nx - 2, 32 * kWarps);
   const int chunk = pick_chunk(ny, gx);
   const int64_t gy = cdiv(ny - 2, chunk);

@@ -195,11 +195,12 @@ class StencilServer:
     def __init__(self, device=0, hbm_budget_bytes=150e9, max_slots=4096, tile_rows=0,
                  tile_planes=0, ctas_per_sm=None, idle_us=500, fp64_guard=True,
                  reserve_bytes=8 << 30, poll_s=2e-4, direct_cells=None, big_lanes=None,
-                 lane_order=None):
+                 lane_order=None, age_s=0.25):
         """direct_cells (grids from this many cells go to a big-grid lane),
         ctas_per_sm (the queue worker's CTAs per SM), big_lanes (big grids run
-        concurrently, one per lane) and lane_order ("sjf": shortest job first,
-        or "fifo") default to the tuned settings of the serving loop
+        concurrently, one per lane) and lane_order ("sjf": shortest job first;
+        "fifo"; "aged": shortest first unless the oldest has waited longer than
+        age_s) default to the tuned settings of the serving loop
         (``autotune.server_settings``)."""
         from . import autotune
         tuned = autotune.server_settings()
@@ -219,9 +220,11 @@ class StencilServer:
         self.poll_s = float(poll_s)
         self.direct_cells = int(direct_cells)
         self.big_lanes = max(1, int(big_lanes))
-        if lane_order not in ("sjf", "fifo"):
-            raise ValueError("lane_order: 'sjf' (shortest job first) or 'fifo'")
+        if lane_order not in ("sjf", "fifo", "aged"):
+            raise ValueError("lane_order: 'sjf' (shortest job first), 'fifo' or 'aged' "
+                             "(shortest first, but a job waiting longer than age_s goes first)")
         self.lane_order = lane_order
+        self.age_s = float(age_s)
         self.queued_small = self.ran_big = 0
         self._queue = collections.deque()
         self._cv = threading.Condition()
@@ -297,6 +300,16 @@ class StencilServer:
         if req.promoted:
             return self.tq.submit(d["A64"], d["B64"], req.tsteps, a32=d["A"], b32=d["B"])
         return self.tq.submit(d["A"], d["B"], req.tsteps)
+
+    def _pick(self, ready):
+        """The next large grid for a free lane (``ready`` is in arrival order)."""
+        if self.lane_order == "fifo":
+            return ready[0]
+        if self.lane_order == "aged":
+            now = time.perf_counter()
+            if now - ready[0].t_submit > self.age_s:
+                return ready[0]  # the oldest has waited long enough: it goes first
+        return min(ready, key=lambda r: r.updates)  # shortest job first
 
     def _run_big(self, req, stream):
         """Queues a large grid's whole run on a big-grid lane; returns its end event."""
@@ -425,8 +438,7 @@ class StencilServer:
                         ln["req"] = None
                         moved = True
                     if ln["req"] is None and big_ready:
-                        nxt = (min(big_ready, key=lambda r: r.updates)  # shortest job first
-                               if self.lane_order == "sjf" else big_ready[0])
+                        nxt = self._pick(big_ready)
                         big_ready.remove(nxt)
                         ln["req"], ln["ev"] = nxt, self._run_big(nxt, ln["stream"])
                         self.ran_big += 1

@@ -815,3 +815,28 @@ def test_heat_f32_two_steps_full_size_out_of_l2(n, tb):
     cref.heat_3d_kernel(10, A, B)
     assert bits_equal(_host(dA), A), first_diff(_host(dA), A)
     assert bits_equal(_host(dB), B)
+
+
+@pytest.mark.parametrize("shape", [(5, 5), (300, 7), (7, 300), (157, 1000), (1000, 1000),
+                                   (1500, 900), (160, 2053)])
+@pytest.mark.parametrize("tsteps", [2, 3, 9, 60])
+def test_jacobi_bands_in_shared_memory(shape, tsteps):
+    """The whole Jacobi-2D time loop in one launch, bands of rows resident in shared
+    memory (forced on), against the oracle and against the chained launches (forced
+    off), in both precisions; A and B start with different faces."""
+    from npbench_gb300 import _lib
+    old = _lib.get_config(_lib.NPBGB_CFG_JACOBI_BANDS)
+    try:
+        for dtype in (np.float64, np.float32):
+            A, B = workloads.uniform_pair(shape, dtype, seed=sum(shape) + tsteps)
+            ra, rb = A.copy(), B.copy()
+            cref.jacobi_2d_kernel(tsteps, ra, rb)
+            for mode in (2, 1):
+                _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS, mode)
+                dA, dB = _dev(A), _dev(B)
+                stencils.jacobi_2d_kernel(tsteps, dA, dB)
+                _lib.device_status()
+                assert bits_equal(_host(dA), ra), (mode, dtype, first_diff(_host(dA), ra))
+                assert bits_equal(_host(dB), rb), (mode, dtype, first_diff(_host(dB), rb))
+    finally:
+        _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS, old)
