@@ -104,6 +104,8 @@ extern "C" {
                                          2^18 cells or more and 16 half-sweeps or more;
                                          1: never; 2: whenever the bands fit.  Results
                                          are identical either way. */
+#define NPBGB_CFG_JACOBI_BANDS_WARPS 19 /* warps per CTA of that kernel: 8, 16 or 32
+                                           (default) */
 
 /* Batch forms. */
 #define NPBGB_BATCH_PERSISTENT 1

@@ -36,6 +36,7 @@ NPBGB_CFG_JACOBI1D_DEPTH = 15
 NPBGB_CFG_HEAT_TB = 16
 NPBGB_CFG_HEAT_TB_CHUNK = 17
 NPBGB_CFG_JACOBI_BANDS = 18
+NPBGB_CFG_JACOBI_BANDS_WARPS = 19
 NPBGB_BATCH_PERSISTENT = 1
 NPBGB_BATCH_STEPPED = 2
 NPBGB_BATCH_QUEUE = 3

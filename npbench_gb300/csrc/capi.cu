@@ -28,6 +28,7 @@ int64_t g_cfg_jacobi1d_depth = 0;  // 0: default
 int64_t g_cfg_heat_tb = 0;         // binary32 Heat-3D half-sweeps per launch (0: by size)
 int64_t g_cfg_heat_tb_chunk = 0;   // 0: automatic
 int64_t g_cfg_jacobi_bands = 0;    // 0: automatic, 1: off, 2: whenever the bands fit
+int64_t g_cfg_jacobi_bands_warps = 32;
 int64_t jacobi1d_effective_depth();  // jacobi1d.cu
 int64_t jacobi1d_effective_ctas();
 
@@ -176,6 +177,11 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "jacobi bands: 0, 1 or 2");
       g_cfg_jacobi_bands = value;
       return NPBGB_OK;
+    case NPBGB_CFG_JACOBI_BANDS_WARPS:
+      if (value != 8 && value != 16 && value != 32)
+        return set_error(NPBGB_ERR_ARG, "jacobi bands warps: 8, 16 or 32");
+      g_cfg_jacobi_bands_warps = value;
+      return NPBGB_OK;
     case NPBGB_CFG_JACOBI1D_DEPTH:
       if (value < 0 || value > 64 || (value & 1))
         return set_error(NPBGB_ERR_ARG, "jacobi1d depth: 0 or an even number up to 64");
@@ -207,6 +213,7 @@ int32_t npbgb_get_config(int32_t key, int64_t* value) {
     case NPBGB_CFG_HEAT_TB: *value = g_cfg_heat_tb; return NPBGB_OK;
     case NPBGB_CFG_HEAT_TB_CHUNK: *value = g_cfg_heat_tb_chunk; return NPBGB_OK;
     case NPBGB_CFG_JACOBI_BANDS: *value = g_cfg_jacobi_bands; return NPBGB_OK;
+    case NPBGB_CFG_JACOBI_BANDS_WARPS: *value = g_cfg_jacobi_bands_warps; return NPBGB_OK;
     default: return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
   }
 }

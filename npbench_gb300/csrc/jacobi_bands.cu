@@ -35,11 +35,10 @@ namespace npbgb {
 
 extern int64_t g_cfg_f64_emulation;
 extern int64_t g_cfg_jacobi_bands;
+extern int64_t g_cfg_jacobi_bands_warps;
 
 namespace {
 
-constexpr int kJWarps = 8;
-constexpr int kJThreads = 32 * kJWarps;
 constexpr uint64_t kJLimitNs = 2000000000ull;
 
 __device__ unsigned int g_jbands_error;  // bit 0: a neighbour wait gave up
@@ -55,24 +54,26 @@ __device__ __forceinline__ void red_release_add_u32(uint32_t* p, uint32_t v) {
 
 // Half-sweep of buffer rows [ra, rb) of one band: every warp takes strips of
 // 32 columns in turn; with FX the first hw_warps warps use hardware binary64.
-template <typename T, bool FX>
+template <typename T, bool FX, int W>
 __device__ __forceinline__ void band_rows(const T* src, T* dst, int64_t nx, int ra, int rb,
                                           int hw_warps, uint32_t one) {
   if (ra >= rb) return;
   const int warp = threadIdx.x >> 5;
-  for (int64_t k0 = 1 + int64_t(warp) * 32; k0 < nx - 1; k0 += 32 * kJWarps) {
-    if (FX && warp < hw_warps)
+  for (int64_t k0 = 1 + int64_t(warp) * 32; k0 < nx - 1; k0 += 32 * W) {
+    if (FX && (warp % 8) < hw_warps)
       jcore::strip_rows<T, false, false, 1>(src, dst, nx, k0, ra, rb, one);
     else
       jcore::strip_rows<T, FX, false, FX ? 1 : 4>(src, dst, nx, k0, ra, rb, one);
   }
 }
 
-template <typename T, bool FX>
-__global__ void __launch_bounds__(kJThreads, 1)
+// W warps per CTA; with FX, warps w with w % 8 < hw_warps use hardware binary64.
+template <typename T, bool FX, int W>
+__global__ void __launch_bounds__(32 * W, 1)
 jacobi2d_bands(T* __restrict__ A, T* __restrict__ B, int64_t ny, int64_t nx, int32_t halfsweeps,
                int rpb, T* __restrict__ exch, uint32_t* __restrict__ counters, int hw_warps,
                uint32_t one) {
+  constexpr int kJThreads = 32 * W;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_ok;
   const int tid = threadIdx.x;
@@ -98,8 +99,8 @@ jacobi2d_bands(T* __restrict__ A, T* __restrict__ B, int64_t ny, int64_t nx, int
     const T* src = buf[s & 1];
     T* dst = buf[(s + 1) & 1];
     // Edge rows first, then publish them.
-    band_rows<T, FX>(src, dst, nx, 1, 2, hw_warps, one);
-    if (rows > 1) band_rows<T, FX>(src, dst, nx, rows, rows + 1, hw_warps, one);
+    band_rows<T, FX, W>(src, dst, nx, 1, 2, hw_warps, one);
+    if (rows > 1) band_rows<T, FX, W>(src, dst, nx, rows, rows + 1, hw_warps, one);
     __syncthreads();
     T* top = slot(s & 1, b, 0);
     T* bot = slot(s & 1, b, 1);
@@ -110,7 +111,7 @@ jacobi2d_bands(T* __restrict__ A, T* __restrict__ B, int64_t ny, int64_t nx, int
     __syncthreads();  // the CTA's stores before thread 0's release, which is cumulative
     if (tid == 0) red_release_add_u32(counters + b, 1u);
     // The interior hides the neighbours' hand-off.
-    band_rows<T, FX>(src, dst, nx, 2, rows, hw_warps, one);
+    band_rows<T, FX, W>(src, dst, nx, 2, rows, hw_warps, one);
     if (tid == 0) {
       const uint32_t want = uint32_t(s + 1);
       const uint64_t t0 = tma::globaltimer();
@@ -188,7 +189,7 @@ cudaError_t scratch_pool(cudaMemPool_t* out) {
 // caller then uses the chained kernels).
 template <typename T>
 int32_t jacobi2d_bands_run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st) {
-  if (g_cfg_jacobi_bands == 1) return NPBGB_ERR_STATE;
+  if (g_cfg_jacobi_bands != 2) return NPBGB_ERR_STATE;  // off unless forced (see the header)
   if (tsteps <= 1 || ny < 3 || nx < 3) return NPBGB_ERR_STATE;
   const int32_t hs = 2 * (tsteps - 1);
   if (g_cfg_jacobi_bands == 0 && (hs < 16 || ny * nx < (int64_t(1) << 18))) return NPBGB_ERR_STATE;
@@ -203,7 +204,13 @@ int32_t jacobi2d_bands_run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, c
   const size_t smem = 2 * size_t(rpb + 2) * size_t(nx) * sizeof(T);
   if (smem + 1024 > size_t(smem_max)) return NPBGB_ERR_STATE;
   const bool fx = sizeof(T) == 8 && g_cfg_f64_emulation;
-  auto kern = fx ? jacobi2d_bands<T, true> : jacobi2d_bands<T, false>;
+  const int warps = g_cfg_jacobi_bands_warps == 8 || g_cfg_jacobi_bands_warps == 16 ?
+                        int(g_cfg_jacobi_bands_warps) : 32;
+  using Kern = void (*)(T*, T*, int64_t, int64_t, int32_t, int, T*, uint32_t*, int, uint32_t);
+  Kern kern = warps == 8 ? (fx ? jacobi2d_bands<T, true, 8> : jacobi2d_bands<T, false, 8>)
+            : warps == 16 ? (fx ? jacobi2d_bands<T, true, 16> : jacobi2d_bands<T, false, 16>)
+                          : (fx ? jacobi2d_bands<T, true, 32> : jacobi2d_bands<T, false, 32>);
+  const int kJThreads = 32 * warps;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e != cudaSuccess) return cuda_status(e, "jacobi2d_bands: smem attribute");
   int per_sm = 0;

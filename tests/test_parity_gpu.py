@@ -825,18 +825,21 @@ def test_jacobi_bands_in_shared_memory(shape, tsteps):
     memory (forced on), against the oracle and against the chained launches (forced
     off), in both precisions; A and B start with different faces."""
     from npbench_gb300 import _lib
-    old = _lib.get_config(_lib.NPBGB_CFG_JACOBI_BANDS)
+    old = (_lib.get_config(_lib.NPBGB_CFG_JACOBI_BANDS),
+           _lib.get_config(_lib.NPBGB_CFG_JACOBI_BANDS_WARPS))
     try:
         for dtype in (np.float64, np.float32):
             A, B = workloads.uniform_pair(shape, dtype, seed=sum(shape) + tsteps)
             ra, rb = A.copy(), B.copy()
             cref.jacobi_2d_kernel(tsteps, ra, rb)
-            for mode in (2, 1):
+            for mode, warps in ((2, 32), (2, 8), (1, 32)):
                 _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS, mode)
+                _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS_WARPS, warps)
                 dA, dB = _dev(A), _dev(B)
                 stencils.jacobi_2d_kernel(tsteps, dA, dB)
                 _lib.device_status()
-                assert bits_equal(_host(dA), ra), (mode, dtype, first_diff(_host(dA), ra))
-                assert bits_equal(_host(dB), rb), (mode, dtype, first_diff(_host(dB), rb))
+                assert bits_equal(_host(dA), ra), (mode, warps, dtype, first_diff(_host(dA), ra))
+                assert bits_equal(_host(dB), rb), (mode, warps, dtype, first_diff(_host(dB), rb))
     finally:
-        _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS, old)
+        _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS, old[0])
+        _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS_WARPS, old[1])
