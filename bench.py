@@ -96,6 +96,9 @@ def parse():
                     help="batch/serve: also time the per-grid / sequential comparator")
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--rate", type=float, default=1000.0)
+    ap.add_argument("--stream", choices=["mixed", "small"], default="mixed",
+                    help="serve workload: the mixed stream of configuration 5, or grids "
+                         "small enough for the tile queue")
     return ap.parse_args()
 
 
@@ -373,6 +376,7 @@ def run_gb300(args, world, rank, local):
             stencils.heat_3d_kernel(TSTEPS, A, B)
         torch.cuda.synchronize(dev)
         barrier()
+        n0 = _library_launches()
         ev = []
         for _ in range(args.steps):
             reset()
@@ -384,12 +388,14 @@ def run_gb300(args, world, rank, local):
             ev.append((e0, e1))
         torch.cuda.synchronize(dev)
         barrier()
+        _LAUNCHES["last"] = _library_launches() - n0
         ms = sum(a.elapsed_time(b) for a, b in ev)
         return ms, A, B, A0
 
     with ClockSampler(local) as clk:
         ms64, A64, B64, A0 = timed(np.float64)
     clocks = clk.summary()
+    launches = _LAUNCHES["last"]
     from npbench_gb300 import replicas
     ms_max = replicas.max_over_ranks(ms64, device=dev)
     ms_per_step = ms_max / args.steps
@@ -479,6 +485,9 @@ def run_gb300(args, world, rank, local):
         serve_block = serve_measure()
         serve_block["workload"] = SERVE_WORKLOAD.format(n=100, rate=0).replace(
             "Poisson 0 req/s", "Poisson arrivals at each rate")
+        small = serve_measure(rates=(SMALL_RATE,), n_requests=SMALL_REQUESTS, stream=SMALL_STREAM)
+        small["workload"] = SMALL_WORKLOAD.format(n=SMALL_REQUESTS, rate=SMALL_RATE)
+        serve_block["small_grids"] = small
 
     if rank == 0:
         line = {
@@ -493,7 +502,7 @@ def run_gb300(args, world, rank, local):
             "pipe_rates_ops_per_s": dict(rates) if rates else None,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * A64.nbytes,
                     "d2h_bytes_per_step": 2 * A64.nbytes},
-            "gpu_launches": HALF_SWEEPS * args.steps,
+            "gpu_launches": launches,
             "clocks": clocks,
             "fp32": fp32,
             "cpu_baseline": cpu,
@@ -506,12 +515,23 @@ def run_gb300(args, world, rank, local):
         dist.destroy_process_group()
 
 
+_LAUNCHES = {"last": None}
+
+
+def _library_launches():
+    """Kernels libnpbgb has put on a stream so far (its own counter)."""
+    from npbench_gb300 import _lib
+    return _lib.launches()
+
+
 def _timed_steps(torch, dev, stream, step, reset, steps, warmup, flush=None):
-    """Event time (ms) of `steps` calls of step(); reset() and flush() run untimed."""
+    """Event time (ms) of `steps` calls of step(); reset() and flush() run untimed.
+    The library's kernel launches inside the timed calls land in _LAUNCHES["last"]."""
     for _ in range(warmup):
         reset()
         step()
     torch.cuda.synchronize(dev)
+    n0 = _library_launches()
     ev = []
     for _ in range(steps):
         reset()
@@ -524,6 +544,7 @@ def _timed_steps(torch, dev, stream, step, reset, steps, warmup, flush=None):
         e1.record(stream)
         ev.append((e0, e1))
     torch.cuda.synchronize(dev)
+    _LAUNCHES["last"] = _library_launches() - n0
     return sum(a.elapsed_time(b) for a, b in ev)
 
 
@@ -577,7 +598,7 @@ def run_jacobi2d(args):
         roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                   "peak_kind": kind, "traffic": ncu_traffic("jacobi2d_f64_1000"),
                   "note": "inputs live in L2 within a step; frac may exceed what HBM alone allows"},
-        gpu_launches=hs * args.steps, clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
+        gpu_launches=_LAUNCHES["last"], clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
 
 
 def run_hdiff(args):
@@ -613,7 +634,7 @@ def run_hdiff(args):
         roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                   "peak_kind": kind, "traffic": ncu_traffic("hdiff_f64_256"),
                   "alg_bytes_per_launch": alg},
-        gpu_launches=args.steps, clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
+        gpu_launches=_LAUNCHES["last"], clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
 
 
 def run_jacobi1d(args):
@@ -655,7 +676,7 @@ def run_jacobi1d(args):
                   "peak_kind": kind, "traffic": None,
                   "note": f"16 B per update; {depth} half-sweeps per launch run in shared "
                           "memory, so the binary64 pipe, not HBM, bounds it"},
-        gpu_launches=(2 * (T - 1) + depth - 1) // depth * args.steps, clocks=clk.summary(),
+        gpu_launches=_LAUNCHES["last"], clocks=clk.summary(),
         cpu_baseline=cpu)), flush=True)
 
 
@@ -699,7 +720,7 @@ def run_vadv(args):
         roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                   "peak_kind": kind, "traffic": ncu_traffic("vadv_f64_256"),
                   "alg_bytes_per_launch": alg},
-        gpu_launches=args.steps, clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
+        gpu_launches=_LAUNCHES["last"], clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
 
 
 def run_cavity(args):
@@ -755,7 +776,7 @@ def run_cavity(args):
                   "peak_kind": kind, "traffic": None,
                   "note": "36,400 dependent sweeps of a 10K-point grid in one launch: bound by "
                           "the latency of each sweep's neighbour hand-off, not by bytes"},
-        gpu_launches=args.steps, clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
+        gpu_launches=_LAUNCHES["last"], clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
 
 
 def run_channel(args):
@@ -811,7 +832,7 @@ def run_channel(args):
                   "peak_kind": kind, "traffic": None,
                   "note": "dependent sweeps of a 10K-point grid in one launch: bound by the "
                           "latency of each sweep's neighbour hand-off, not by bytes"},
-        gpu_launches=args.steps, clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
+        gpu_launches=_LAUNCHES["last"], clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
 
 
 def run_fdtd2d(args):
@@ -853,7 +874,7 @@ def run_fdtd2d(args):
         roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                   "peak_kind": kind, "traffic": None,
                   "note": "48 B per cell-step (ex, ey, hz read and written once)"},
-        gpu_launches=2 * T * args.steps, clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
+        gpu_launches=_LAUNCHES["last"], clocks=clk.summary(), cpu_baseline=cpu)), flush=True)
 
 
 def _rel_err(low, ref):
@@ -947,6 +968,7 @@ def batch_measure(n_grids=4096, steps=2, warmup=1, compare=True, compare_steps=1
         with ClockSampler(0) as clk:
             ms = _timed_steps(torch, dev, stream, lambda: batch.launch(graph=True), reset,
                               steps, warmup)
+        launches = _LAUNCHES["last"]
         _lib.device_status()
     ms_step = ms / steps
     peak, kind = measured_peaks()
@@ -966,17 +988,17 @@ def batch_measure(n_grids=4096, steps=2, warmup=1, compare=True, compare_steps=1
                         "traffic": ncu_traffic("batch_4096"),
                         "traffic_over_algorithmic":
                             _ncu_record("batch_4096").get("traffic_over_algorithmic")},
-           "clocks": clk.summary()}
+           "clocks": clk.summary(), "gpu_launches": launches}
     if compare:
         ms_pg = _timed_steps(torch, dev, stream, lambda: _per_grid_guarded(work, guard), reset,
                              compare_steps, compare_warmup)
         ms_pg /= compare_steps
         out["per_grid"] = {"value": ups / (ms_pg * 1e-3), "ms_per_step": ms_pg,
                            "steps": compare_steps, "warmup": compare_warmup,
-                           "kernel_launches": sum(2 * (T - 1) for _, _, T in specs),
-                           "what": "one jacobi_2d_kernel call per grid (chained launches, "
-                                   "tuned single-grid kernels), same inputs, steps and "
-                                   "float64 guard"}
+                           "kernel_launches": _LAUNCHES["last"],
+                           "what": "one jacobi_2d_kernel call per grid (tuned single-grid "
+                                   "kernels: chained launches, or one launch with the bands "
+                                   "in shared memory), same inputs, steps and float64 guard"}
         out["batched_over_per_grid"] = ms_pg / ms_step
     if fp32_error:
         # The float32 grids (as the batch left them, guard included) against float64
@@ -1036,19 +1058,28 @@ def run_batch(args):
         dict(extra, l2=f"{b['cells'] * 6 * 2 / 1e9:.1f} GB resident, far above L2"),
         roofline=b["roofline"], comparator=b.get("per_grid"),
         batched_over_per_grid=b.get("batched_over_per_grid"),
-        fp32_error_vs_fp64=b.get("fp32_error_vs_fp64"), gpu_launches=args.steps,
+        fp32_error_vs_fp64=b.get("fp32_error_vs_fp64"), gpu_launches=b["gpu_launches"],
         clocks=b["clocks"], cpu_baseline=b.get("cpu_baseline"))), flush=True)
 
 
 SERVE_WORKLOAD = ("served stream: {n} requests, Poisson {rate:g} req/s, 2D Jacobi 128^2-4096^2 "
                   "and 3D heat 32^3-384^3 (log-uniform per axis), 70% float32, TSTEPS 20-1000")
 
+# A stream of grids small enough for the tile queue: every request is folded
+# into the running worker kernel, none takes a big-grid lane.
+SMALL_STREAM = {"side2d": (32, 224), "side3d": (12, 36)}
+SMALL_REQUESTS, SMALL_RATE = 1000, 20000.0
+SMALL_WORKLOAD = ("small-grid stream: {n} requests, Poisson {rate:g} req/s, 2D Jacobi 32^2-224^2 "
+                  "and 3D heat 12^3-36^3 (log-uniform per axis), 70% float32, TSTEPS 20-1000")
+
 
 def serve_measure(rates=(200.0, 1000.0, 5000.0), n_requests=100, compare=True, fp32_error=True,
-                  cpu=False):
+                  cpu=False, stream=None):
     """Configuration 5: Poisson arrivals of mixed solves through the continuous-batching
     server at each rate, beside the same requests run one at a time with per-grid
-    launches.  Returns {"rates": [...], "fp32_error_vs_fp64": ...}."""
+    launches.  `stream` overrides the request sizes (workloads.served_requests keywords).
+    Returns {"rates": [...], "fp32_error_vs_fp64": ...}."""
+    stream = dict(stream or {})
     import torch
     from npbench_gb300 import stencils, workloads
     from npbench_gb300.server import (Request, StencilServer, latency_stats, run_sequential,
@@ -1063,15 +1094,17 @@ def serve_measure(rates=(200.0, 1000.0, 5000.0), n_requests=100, compare=True, f
                      "the device"}
     kept = None
     # The same requests at every rate (only the arrival times scale).
-    _, specs = workloads.served_requests(n_requests, rates[0], seed=0)
+    _, specs = workloads.served_requests(n_requests, rates[0], seed=0, **stream)
     host = [_pinned_inputs(s, dt, sd) for s, dt, T, sd in specs]
     for rate in rates:
-        arrivals, _ = workloads.served_requests(n_requests, rate, seed=0)
+        arrivals, _ = workloads.served_requests(n_requests, rate, seed=0, **stream)
 
         def make():
             return [Request(shape=s, dtype=dt, tsteps=T, a=h[0], b=h[1], return_host=False)
                     for (s, dt, T, sd), h in zip(specs, host)]
         reqs = make()
+        torch.cuda.synchronize()
+        n_launch0 = _library_launches()
         srv = StencilServer(hbm_budget_bytes=150e9).start()
         t0 = time.perf_counter()
         futs = []
@@ -1083,10 +1116,14 @@ def serve_measure(rates=(200.0, 1000.0, 5000.0), n_requests=100, compare=True, f
                 futs.append(srv.submit(r))
             results = [f.result() for f in futs]
             srv.stop()
+        torch.cuda.synchronize()
+        n_launch = _library_launches() - n_launch0
         st = latency_stats(reqs)
         entry = {"rate_hz": rate, "served": {k: st[k] for k in ("updates_per_s", "p50_ms",
                                                                   "p99_ms", "mean_ms", "span_s")},
                  "worker_launches": srv.launches, "float32_requests_run_in_float64": srv.promoted,
+                 "paths": {"tile_queue": srv.queued_small, "big_grid_lanes": srv.ran_big},
+                 "gpu_launches": n_launch,
                  "peak_resident_gb": srv.admission.peak / 1e9, "clocks": clk.summary()}
         if compare:
             seq = make()
@@ -1125,7 +1162,7 @@ def serve_measure(rates=(200.0, 1000.0, 5000.0), n_requests=100, compare=True, f
         # The stream's requests in arrival order, up to about 2e10 updates,
         # through the C restatement on all host threads.
         from oracle import cref
-        _, specs = workloads.served_requests(n_requests, rates[0], seed=0)
+        _, specs = workloads.served_requests(n_requests, rates[0], seed=0, **stream)
         rng = np.random.default_rng(2)
         done_ups, t_cpu, n = 0, 0.0, 0
         for shape, dt, T, _ in specs:
@@ -1161,13 +1198,14 @@ def _pinned_inputs(shape, dt, seed):
 
 def run_serve(args):
     """Configuration 5 on its own line (``--workload serve``) at ``--rate``."""
+    small = args.stream == "small"
     s = serve_measure(rates=(args.rate,), n_requests=args.requests, compare=args.compare,
-                      cpu=not args.no_cpu_baseline)
+                      cpu=not args.no_cpu_baseline, stream=SMALL_STREAM if small else None)
     e = s["rates"][0]
     print(json.dumps(_base_line(
         args, e["served"]["updates_per_s"], e["served"]["span_s"] * 1e3, "f32+f64",
-        SERVE_WORKLOAD.format(n=args.requests, rate=args.rate),
-        {"hbm_budget_gb": 150, "worker_launches": e["worker_launches"],
+        (SMALL_WORKLOAD if small else SERVE_WORKLOAD).format(n=args.requests, rate=args.rate),
+        {"hbm_budget_gb": 150, "worker_launches": e["worker_launches"], "paths": e["paths"],
          "float32_requests_run_in_float64": e["float32_requests_run_in_float64"],
          "peak_resident_gb": e["peak_resident_gb"]},
         latency={k: e["served"][k] for k in ("p50_ms", "p99_ms", "mean_ms")},

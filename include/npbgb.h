@@ -93,19 +93,29 @@ extern "C" {
 #define NPBGB_CFG_HEAT_TB 16          /* heat3d binary32: half-sweeps per launch.
                                          2: two (temporal blocking) wherever the
                                          arrays meet the TMA rules and TSTEPS >= 4;
-                                         1: one; 0 (default): two for arrays of
-                                         256 MiB and more, else one.  Results are
+                                         0 (default) or 1: one (the single-step
+                                         kernel with short plane chunks measured
+                                         faster at every size).  Results are
                                          identical either way. */
 #define NPBGB_CFG_HEAT_TB_CHUNK 17    /* heat3d binary32 two-step kernel: axis-0
                                          planes per CTA; 0 (default) = automatic */
 #define NPBGB_CFG_JACOBI_BANDS 18     /* jacobi2d: the whole time loop in one launch with
                                          bands of rows resident in shared memory.
-                                         0 (default): when the bands fit, the grid has
-                                         2^18 cells or more and 16 half-sweeps or more;
-                                         1: never; 2: whenever the bands fit.  Results
-                                         are identical either way. */
-#define NPBGB_CFG_JACOBI_BANDS_WARPS 19 /* warps per CTA of that kernel: 8, 16 or 32
-                                           (default) */
+                                         0 (default): binary64 runs of 16 half-sweeps or
+                                         more whose bands fit; 1: never; 2: whenever the
+                                         bands fit (binary32 too).  Results are
+                                         identical either way. */
+#define NPBGB_CFG_JACOBI_BANDS_WARPS 19 /* warps per CTA of that kernel: 8, 16 or 32;
+                                           0 (default): one 32-column strip per warp,
+                                           8 to 32 warps */
+#define NPBGB_CFG_HEAT_STAGES 20      /* heat3d binary32 TMA kernel: depth of the
+                                         shared-memory plane ring, 4, 6 or 8;
+                                         0 (default) = automatic */
+#define NPBGB_CFG_LAUNCHES 21         /* read: kernels the library has put on a
+                                         stream, each batch graph replay counting the
+                                         kernels it holds (a launch recorded into a
+                                         caller's graph counts once, when recorded);
+                                         set 0 to reset */
 
 /* Batch forms. */
 #define NPBGB_BATCH_PERSISTENT 1

@@ -37,6 +37,8 @@ NPBGB_CFG_HEAT_TB = 16
 NPBGB_CFG_HEAT_TB_CHUNK = 17
 NPBGB_CFG_JACOBI_BANDS = 18
 NPBGB_CFG_JACOBI_BANDS_WARPS = 19
+NPBGB_CFG_HEAT_STAGES = 20
+NPBGB_CFG_LAUNCHES = 21
 NPBGB_BATCH_PERSISTENT = 1
 NPBGB_BATCH_STEPPED = 2
 NPBGB_BATCH_QUEUE = 3
@@ -150,6 +152,11 @@ def get_config(key):
     v = _i64(0)
     check(load().npbgb_get_config(key, ctypes.byref(v)), "npbgb_get_config")
     return v.value
+
+
+def launches():
+    """Kernels the library has put on a stream so far (NPBGB_CFG_LAUNCHES)."""
+    return get_config(NPBGB_CFG_LAUNCHES)
 
 
 def device_status(stream=None):

@@ -7,8 +7,9 @@
     python -m npbench_gb300.autotune --ship FILE      # all of the above into FILE
 
 The kernels take knobs that change speed, never results (``NPBGB_CFG_*``): for
-binary64 Jacobi-2D the warps per CTA on the hardware binary64 path and the
-rows per CTA; for Heat-3D the tile rows per warp, the rows on hardware
+binary64 Jacobi-2D the warps per CTA on the hardware binary64 path, the
+rows per CTA and whether the whole loop runs in one launch with bands of rows
+in shared memory; for Heat-3D the tile rows per warp, the rows on hardware
 binary64, the planes per CTA and, in binary32, the half-sweeps per launch
 (temporal depth, 1 or 2).  Batches have their tile rows and hardware warps;
 the server its split between the tile queue and the big-grid lanes.
@@ -57,6 +58,7 @@ _KNOBS = {
     "HEAT_HW_ROWS": _lib.NPBGB_CFG_HEAT_HW_ROWS,
     "HEAT_CHUNK": _lib.NPBGB_CFG_HEAT_CHUNK,
     "HEAT_TB": _lib.NPBGB_CFG_HEAT_TB,
+    "JACOBI_BANDS": _lib.NPBGB_CFG_JACOBI_BANDS,
 }
 
 
@@ -67,13 +69,18 @@ def _space(bench, dtype):
     if bench == "jacobi_2d":
         for hw in ((0, 2, 3, 4, 5, 6, 8) if f64 else (-1,)):
             for ch in (0, 3, 4, 6, 8, 16, 32):
-                out.append({"JACOBI_HW_WARPS": hw, "JACOBI_CHUNK": ch})
+                cfg = {"JACOBI_HW_WARPS": hw, "JACOBI_CHUNK": ch}
+                if f64:
+                    cfg["JACOBI_BANDS"] = 1  # chained launches
+                out.append(cfg)
+            if f64:  # the whole loop in one launch where the bands fit
+                out.append({"JACOBI_HW_WARPS": hw, "JACOBI_CHUNK": 0, "JACOBI_BANDS": 0})
     elif bench == "heat_3d":
         for rows in (1, 2, 4):
             tj = 8 * rows
             for hw in (sorted({0, tj // 8, tj // 4, 5 * tj // 16, 3 * tj // 8, 7 * tj // 16})
                        if f64 else (-1,)):
-                for ch in (0, 4, 8, 16, 32):
+                for ch in (0, 4, 5, 8, 16, 32):
                     for tb in ((1,) if f64 else (1, 2)):
                         cfg = {"HEAT_ROWS": rows, "HEAT_HW_ROWS": hw, "HEAT_CHUNK": ch}
                         if not f64:
@@ -179,9 +186,11 @@ def applied(bench, shape, dtype):
 
 
 def _defaults(bench, dtype=np.float64):
-    names = ("JACOBI_HW_WARPS", "JACOBI_CHUNK") if bench == "jacobi_2d" else \
-        ("HEAT_ROWS", "HEAT_HW_ROWS", "HEAT_CHUNK") + \
-        (("HEAT_TB",) if np.dtype(dtype) == np.float32 else ())
+    f64 = np.dtype(dtype) == np.float64
+    if bench == "jacobi_2d":
+        names = ("JACOBI_HW_WARPS", "JACOBI_CHUNK") + (("JACOBI_BANDS",) if f64 else ())
+    else:
+        names = ("HEAT_ROWS", "HEAT_HW_ROWS", "HEAT_CHUNK") + (() if f64 else ("HEAT_TB",))
     return {n: _lib.get_config(_KNOBS[n]) for n in names}
 
 

@@ -321,6 +321,7 @@ struct npbgb_batch {
   int64_t cap_ctas = 0;   // allocated capacity of d_cta_off
   int ctas_per_sm = 2;  // persistent kernel variant chosen when planned
   cudaGraphExec_t graph = nullptr;
+  int64_t graph_kernels = 0;  // kernel launches in the graph, counted at each replay
   cudaStream_t graph_stream = nullptr;
   // Stepped form (mode NPBGB_BATCH_STEPPED).
   int32_t mode = NPBGB_BATCH_PERSISTENT;
@@ -453,7 +454,7 @@ int32_t launch_batch(npbgb_batch* b, cudaStream_t st) {
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  e = cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(persistent_kernel(b->ctas_per_sm)), args);
+  e = counted(cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(persistent_kernel(b->ctas_per_sm)), args));
   if (e != cudaSuccess) return cuda_status(e, "batch: cooperative launch");
   return NPBGB_OK;
 }
@@ -753,7 +754,11 @@ int32_t npbgb_batch_launch(npbgb_batch* b, int32_t use_graph, void* stream) {
       cudaStreamDestroy(cap);
       return cuda_status(e, "batch: begin capture");
     }
+    const int64_t before = add_launches(0);
     const int32_t r = launch_batch(b, cap);
+    const int64_t recorded = add_launches(0) - before;
+    add_launches(-recorded);  // counted at each replay instead
+    b->graph_kernels = recorded;
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(cap, &graph);
     cudaStreamDestroy(cap);
@@ -771,6 +776,7 @@ int32_t npbgb_batch_launch(npbgb_batch* b, int32_t use_graph, void* stream) {
   }
   cudaError_t e = cudaGraphLaunch(b->graph, st);
   if (e != cudaSuccess) return cuda_status(e, "batch: graph launch");
+  add_launches(b->graph_kernels);
   return NPBGB_OK;
 }
 
@@ -961,7 +967,7 @@ extern "C" int32_t npbgb_batch_run_noalloc(const npbgb_grid* grids, int64_t coun
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  e = cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(batch_persistent<2>), args);
+  e = counted(cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(batch_persistent<2>), args));
   if (e != cudaSuccess) return cuda_status(e, "batch(no-alloc): cooperative launch");
   return NPBGB_OK;
 }

@@ -1,4 +1,5 @@
 // Library-wide C ABI helpers: version, status strings, per-thread last error.
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 
@@ -28,7 +29,14 @@ int64_t g_cfg_jacobi1d_depth = 0;  // 0: default
 int64_t g_cfg_heat_tb = 0;         // binary32 Heat-3D half-sweeps per launch (0: by size)
 int64_t g_cfg_heat_tb_chunk = 0;   // 0: automatic
 int64_t g_cfg_jacobi_bands = 0;    // 0: automatic, 1: off, 2: whenever the bands fit
-int64_t g_cfg_jacobi_bands_warps = 32;
+int64_t g_cfg_jacobi_bands_warps = 0;  // 0: by the grid's width
+int64_t g_cfg_heat_stages = 0;         // 0: automatic (8)
+
+namespace {
+std::atomic<int64_t> g_launches{0};
+}  // namespace
+
+int64_t add_launches(int64_t n) { return g_launches.fetch_add(n, std::memory_order_relaxed) + n; }
 int64_t jacobi1d_effective_depth();  // jacobi1d.cu
 int64_t jacobi1d_effective_ctas();
 
@@ -177,9 +185,18 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "jacobi bands: 0, 1 or 2");
       g_cfg_jacobi_bands = value;
       return NPBGB_OK;
+    case NPBGB_CFG_LAUNCHES:
+      if (value != 0) return set_error(NPBGB_ERR_ARG, "launch count: only 0 (reset) may be set");
+      g_launches.store(0, std::memory_order_relaxed);
+      return NPBGB_OK;
+    case NPBGB_CFG_HEAT_STAGES:
+      if (value != 0 && value != 4 && value != 6 && value != 8)
+        return set_error(NPBGB_ERR_ARG, "heat stages: 0 (automatic), 4, 6 or 8");
+      g_cfg_heat_stages = value;
+      return NPBGB_OK;
     case NPBGB_CFG_JACOBI_BANDS_WARPS:
-      if (value != 8 && value != 16 && value != 32)
-        return set_error(NPBGB_ERR_ARG, "jacobi bands warps: 8, 16 or 32");
+      if (value != 0 && value != 8 && value != 16 && value != 32)
+        return set_error(NPBGB_ERR_ARG, "jacobi bands warps: 0, 8, 16 or 32");
       g_cfg_jacobi_bands_warps = value;
       return NPBGB_OK;
     case NPBGB_CFG_JACOBI1D_DEPTH:
@@ -214,6 +231,8 @@ int32_t npbgb_get_config(int32_t key, int64_t* value) {
     case NPBGB_CFG_HEAT_TB_CHUNK: *value = g_cfg_heat_tb_chunk; return NPBGB_OK;
     case NPBGB_CFG_JACOBI_BANDS: *value = g_cfg_jacobi_bands; return NPBGB_OK;
     case NPBGB_CFG_JACOBI_BANDS_WARPS: *value = g_cfg_jacobi_bands_warps; return NPBGB_OK;
+    case NPBGB_CFG_HEAT_STAGES: *value = g_cfg_heat_stages; return NPBGB_OK;
+    case NPBGB_CFG_LAUNCHES: *value = g_launches.load(std::memory_order_relaxed); return NPBGB_OK;
     default: return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
   }
 }

@@ -582,7 +582,7 @@ extern "C" int32_t npbgb_cavity_flow(void* u, void* v, void* p, int64_t ny, int6
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     void* args[] = {&a};
-    e = cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(cfd_bands<false>), args);
+    e = counted(cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(cfd_bands<false>), args));
   }
   if (e != cudaSuccess) status = cuda_status(e, "cavity_flow: cooperative launch");
   if (workspace == nullptr) cudaFreeAsync(ws, st);
@@ -763,7 +763,7 @@ extern "C" int32_t npbgb_channel_flow(void* u, void* v, void* p, int64_t ny, int
   if (e == cudaSuccess) {
     if (ny < 3) {
       channel_small<<<1, kCThreads, 0, st>>>(a);
-      e = cudaGetLastError();
+      e = counted(cudaGetLastError());
     } else {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3{unsigned(l.nb), 1, 1};
@@ -775,7 +775,7 @@ extern "C" int32_t npbgb_channel_flow(void* u, void* v, void* p, int64_t ny, int
       cfg.attrs = attr;
       cfg.numAttrs = 1;
       void* args[] = {&a};
-      e = cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(cfd_bands<true>), args);
+      e = counted(cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(cfd_bands<true>), args));
     }
   }
   if (e == cudaSuccess && steps != nullptr) {

@@ -22,6 +22,7 @@
 // bit, and a point whose seven inputs are all clean is evaluated with exact
 // integer adds and round53; any other point is evaluated with hardware
 // binary64 from global memory.  Both give the IEEE result bit for bit.
+#include <algorithm>
 #include <type_traits>
 
 #include "fx64.cuh"
@@ -38,6 +39,7 @@ extern int64_t g_cfg_heat_rows;
 extern int64_t g_cfg_heat_hw_rows;
 extern int64_t g_cfg_f64_cvt;
 extern int64_t g_cfg_heat_tb;
+extern int64_t g_cfg_heat_stages;
 
 int32_t heat3d_tb2_run(float* a, float* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps,
                        cudaStream_t st, int32_t (*single_pairs)(float*, float*, int64_t, int64_t,
@@ -91,7 +93,7 @@ struct TmaGeom {
   static constexpr int kStride = (kBytes + 127) / 128 * 128;  // stage pitch, 128-byte aligned
 };
 
-constexpr int kStages = 8;
+constexpr int kStages = 8;  // ring depth of the binary64 kernels (binary32: NPBGB_CFG_HEAT_STAGES)
 // Output planes per CTA barrier: fixed point (the barrier also publishes the
 // conversion of the staged planes; 3 measured 3% faster than 1 at 256^3) and
 // plain binary32/binary64.  The prologue stages kStages - kSync planes and
@@ -107,7 +109,7 @@ static_assert(kSyncFx >= 1 && 2 * kSyncFx + 2 <= kStages && kSyncPlain >= 1 &&
 // conversions through the binary64 conversion path.  hw_rows: the last
 // hw_rows tile rows are evaluated with hardware binary64 (from global memory)
 // so that the binary64 pipe works alongside the integer pipe.  one == 1.
-template <typename T, bool FX, int R, bool CVT>
+template <typename T, bool FX, int R, bool CVT, int NS>
 __global__ void __launch_bounds__(kThreads)
 heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ src,
            T* __restrict__ dst, int64_t n0, int64_t n1, int64_t n2, int chunk, int hw_rows,
@@ -116,6 +118,8 @@ heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ sr
   using G = TmaGeom<T, R>;
   using S = typename std::conditional<FX, int64_t, T>::type;
   constexpr int kSync = FX ? kSyncFx : kSyncPlain;
+  constexpr int kStages = NS;
+  static_assert(2 * kSync + 2 <= kStages, "staging ring too short for the planes per barrier");
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kStages * G::kStride);
 
@@ -285,9 +289,22 @@ int auto_chunk(int64_t n0, int64_t tiles, int ctas_per_sm, int waves) {
   return int(c);
 }
 
-template <typename T, bool FX, int R, bool CVT>
+// Binary32 planes per CTA.  A CTA whose chunk's planes (chunk + 2) all fit in
+// the ring's first copies (kStages - 1) issues every copy at once, so short
+// chunks keep many CTAs' copies in flight.  Measured on GB300 (TSTEPS=21, 4
+// tile rows per warp, 8-deep ring, fraction of the measured copy bandwidth at
+// 8 bytes per update): 5 planes give 0.77, 0.80, 0.83 and 0.86 at 384^3,
+// 416^3, 512^3 and 640^3 (4 planes: 0.76-0.83; 6: 0.75-0.79), against 0.62,
+// 0.60, 0.55 and 0.50 for the 2-wave chunks; at 256^3, whose pair L2 largely
+// holds, 8 planes give 0.71 (5: 0.69, 2-wave: 0.70).
+int f32_chunk_cap(int64_t array_bytes) {
+  return array_bytes >= (int64_t(128) << 20) ? 5 : 8;
+}
+
+template <typename T, bool FX, int R, bool CVT, int NS = kStages>
 int32_t launch_tma(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps, cudaStream_t st) {
   using G = TmaGeom<T, R>;
+  constexpr int kStages = NS;
   const size_t smem = size_t(kStages) * G::kStride + kStages * sizeof(uint64_t);
   CUtensorMap map_a, map_b;
   const uint64_t dims[3] = {uint64_t(n2), uint64_t(n1), uint64_t(n0)};
@@ -297,16 +314,18 @@ int32_t launch_tma(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tstep
     return NPBGB_ERR_STATE;  // caller falls back to plain staging
   static bool attr_done = false;
   if (!attr_done) {
-    cudaError_t e = cudaFuncSetAttribute(heat3d_tma<T, FX, R, CVT>,
+    cudaError_t e = cudaFuncSetAttribute(heat3d_tma<T, FX, R, CVT, NS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return cuda_status(e, "heat3d: smem attribute");
     attr_done = true;
   }
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heat3d_tma<T, FX, R, CVT>, kThreads, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heat3d_tma<T, FX, R, CVT, NS>, kThreads, smem);
   const int64_t gx = cdiv(n2 - 2, kTK), gy = cdiv(n1 - 2, G::TJ);
-  const int chunk = g_cfg_heat_chunk > 0 ? int(g_cfg_heat_chunk)
-                                         : auto_chunk(n0, gx * gy, per_sm, FX ? 16 : 2);
+  int chunk = g_cfg_heat_chunk > 0 ? int(g_cfg_heat_chunk)
+                                   : auto_chunk(n0, gx * gy, per_sm, FX ? 16 : 2);
+  if (g_cfg_heat_chunk <= 0 && sizeof(T) == 4)
+    chunk = std::min(chunk, f32_chunk_cap(n0 * n1 * n2 * int64_t(sizeof(T))));
   const int64_t gz = cdiv(n0 - 2, chunk);
   if (gy > 65535 || gz > 65535 || gx > 0x7fffffff)
     return set_error(NPBGB_ERR_ARG, "heat3d: extent too large");
@@ -322,10 +341,10 @@ int32_t launch_tma(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tstep
   const dim3 block{unsigned(kThreads)};
   cudaError_t e = cudaSuccess;
   for (int32_t t = 1; t < tsteps && e == cudaSuccess; ++t) {
-    e = launch_chained(heat3d_tma<T, FX, R, CVT>, grid, block, smem, st, map_a, a, b, n0, n1, n2,
+    e = launch_chained(heat3d_tma<T, FX, R, CVT, NS>, grid, block, smem, st, map_a, a, b, n0, n1, n2,
                        chunk, hw, 1u);
     if (e == cudaSuccess)
-      e = launch_chained(heat3d_tma<T, FX, R, CVT>, grid, block, smem, st, map_b, b, a, n0, n1,
+      e = launch_chained(heat3d_tma<T, FX, R, CVT, NS>, grid, block, smem, st, map_b, b, a, n0, n1,
                          n2, chunk, hw, 1u);
   }
   return cuda_status(e, "heat3d_tma");
@@ -361,7 +380,18 @@ int32_t run_single(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tstep
     const int rows = g_cfg_heat_rows > 0 ? int(g_cfg_heat_rows) : (sizeof(T) == 4 ? 4 : 2);
     const bool cvt = g_cfg_f64_cvt != 0;
     int32_t r;
-    if (rows >= 4)
+    if constexpr (sizeof(T) == 4 && !FX) {
+      // binary32: the depth of the plane ring is a knob (no conversion step)
+      const int64_t ns = g_cfg_heat_stages;
+      if (rows >= 4)
+        r = ns == 4   ? launch_tma<T, FX, 4, false, 4>(a, b, n0, n1, n2, tsteps, st)
+            : ns == 6 ? launch_tma<T, FX, 4, false, 6>(a, b, n0, n1, n2, tsteps, st)
+                      : launch_tma<T, FX, 4, false, 8>(a, b, n0, n1, n2, tsteps, st);
+      else if (rows == 2)
+        r = launch_tma<T, FX, 2, false>(a, b, n0, n1, n2, tsteps, st);
+      else
+        r = launch_tma<T, FX, 1, false>(a, b, n0, n1, n2, tsteps, st);
+    } else if (rows >= 4)
       r = cvt ? launch_tma<T, FX, 4, true>(a, b, n0, n1, n2, tsteps, st)
               : launch_tma<T, FX, 4, false>(a, b, n0, n1, n2, tsteps, st);
     else if (rows == 2)
@@ -380,18 +410,16 @@ int32_t run_single_f32(float* a, float* b, int64_t n0, int64_t n1, int64_t n2, i
   return run_single<float, false>(a, b, n0, n1, n2, tsteps, st);
 }
 
-// Binary32 arrays well beyond L2 take two half-sweeps per launch (heat_tb.cu)
-// where the arrays allow TMA: measured on GB300, 512^3 17.6 -> 13.6 ms for
-// TSTEPS=30, no change at 384^3, and slower at 256^3, whose pair L2 largely
-// holds.  Binary64 (bound by its arithmetic pipes, not HBM) takes one.
-constexpr int64_t kTwoStepBytes = int64_t(256) << 20;  // per array, automatic choice
-
+// Binary32 takes two half-sweeps per launch (heat_tb.cu) only when asked
+// (NPBGB_CFG_HEAT_TB = 2).  Measured on GB300 at TSTEPS=21, the single-step
+// kernel with 5-plane chunks reaches 0.77-0.86 of the measured copy bandwidth
+// at 384^3 to 640^3, and the two-step kernel at most 0.62-0.69 over its chunk
+// sizes: the two-step kernel halves the HBM bytes but is bound by its
+// instruction issue.  Binary64 (bound by its arithmetic pipes) takes one.
 template <typename T, bool FX>
 int32_t run(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps, cudaStream_t st) {
   if constexpr (sizeof(T) == 4) {
-    const bool big = n0 * n1 * n2 * int64_t(sizeof(T)) >= kTwoStepBytes;
-    const bool two = g_cfg_heat_tb == 2 || (g_cfg_heat_tb == 0 && big);
-    if (two && g_cfg_heat_tma && tsteps >= 4) {
+    if (g_cfg_heat_tb == 2 && g_cfg_heat_tma && tsteps >= 4) {
       const int32_t r = heat3d_tb2_run(a, b, n0, n1, n2, tsteps, st, run_single_f32);
       if (r != NPBGB_ERR_STATE) return r;
     }

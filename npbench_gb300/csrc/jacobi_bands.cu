@@ -181,18 +181,34 @@ cudaError_t scratch_pool(cudaMemPool_t* out) {
   return cudaSuccess;
 }
 
+// Warps per CTA: by default one 32-column strip per warp and row, at least 8
+// and at most 32 warps.  Measured on GB300 (binary64, TSTEPS=100): 1000^2
+// takes 2.02 ms with 32 warps against 3.68 with 8, 500^2 1.01 ms with 16
+// against 1.06 with 32, and 150^2 (TSTEPS=50) 0.315 ms with 8.
+int bands_warps(int64_t nx) {
+  const int64_t w = g_cfg_jacobi_bands_warps;
+  if (w == 8 || w == 16 || w == 32) return int(w);
+  const int64_t strips = cdiv(nx - 2, int64_t(32));
+  return strips <= 8 ? 8 : strips <= 16 ? 16 : 32;
+}
+
 }  // namespace
 
 // Runs the whole time loop of Jacobi-2D in one cooperative launch when the
 // bands fit in shared memory (about 1.4 M binary64 cells or 2.8 M binary32
-// cells on 152 SMs) and the run is long enough; NPBGB_ERR_STATE otherwise (the
-// caller then uses the chained kernels).
+// cells on 152 SMs); NPBGB_ERR_STATE otherwise (the caller then uses the
+// chained kernels).  Automatic for binary64 runs of 16 half-sweeps or more:
+// with the warps above it measured 3-20% faster than the chained launches
+// (1000^2: 2.02 against 2.09 ms; 150^2 TSTEPS=50: 0.315 against 0.394 ms).
+// Binary32 stays on the chained launches, which measured faster at every
+// size tried (1000^2: 0.71 against 1.03 ms), because the binary32 half-sweep
+// is short enough that the band hand-off costs more than a launch boundary.
 template <typename T>
 int32_t jacobi2d_bands_run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st) {
-  if (g_cfg_jacobi_bands != 2) return NPBGB_ERR_STATE;  // off unless forced (see the header)
+  if (g_cfg_jacobi_bands == 1) return NPBGB_ERR_STATE;
   if (tsteps <= 1 || ny < 3 || nx < 3) return NPBGB_ERR_STATE;
   const int32_t hs = 2 * (tsteps - 1);
-  if (g_cfg_jacobi_bands == 0 && (hs < 16 || ny * nx < (int64_t(1) << 18))) return NPBGB_ERR_STATE;
+  if (g_cfg_jacobi_bands == 0 && (sizeof(T) != 8 || hs < 16)) return NPBGB_ERR_STATE;
   int dev = 0, sms = 0, smem_max = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -204,8 +220,7 @@ int32_t jacobi2d_bands_run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, c
   const size_t smem = 2 * size_t(rpb + 2) * size_t(nx) * sizeof(T);
   if (smem + 1024 > size_t(smem_max)) return NPBGB_ERR_STATE;
   const bool fx = sizeof(T) == 8 && g_cfg_f64_emulation;
-  const int warps = g_cfg_jacobi_bands_warps == 8 || g_cfg_jacobi_bands_warps == 16 ?
-                        int(g_cfg_jacobi_bands_warps) : 32;
+  const int warps = bands_warps(nx);
   using Kern = void (*)(T*, T*, int64_t, int64_t, int32_t, int, T*, uint32_t*, int, uint32_t);
   Kern kern = warps == 8 ? (fx ? jacobi2d_bands<T, true, 8> : jacobi2d_bands<T, false, 8>)
             : warps == 16 ? (fx ? jacobi2d_bands<T, true, 16> : jacobi2d_bands<T, false, 16>)
@@ -244,7 +259,7 @@ int32_t jacobi2d_bands_run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, c
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    e = cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(kern), args);
+    e = counted(cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(kern), args));
   }
   cudaFreeAsync(scratch, st);
   return cuda_status(e, "jacobi2d_bands");

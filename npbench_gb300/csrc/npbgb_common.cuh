@@ -13,6 +13,11 @@ namespace npbgb {
 // Records a message for npbgb_last_error() and returns `code`.
 int32_t set_error(int32_t code, const char* fmt, ...);
 
+// Adds n to the count of kernels the library has put on a stream
+// (NPBGB_CFG_LAUNCHES; a batch graph's kernels count at each replay, a launch
+// recorded into a caller's graph once, when recorded) and returns the new count.
+int64_t add_launches(int64_t n);
+
 // Maps a CUDA error to a status, recording the CUDA message.
 inline int32_t cuda_status(cudaError_t e, const char* where) {
   if (e == cudaSuccess) return NPBGB_OK;
@@ -23,6 +28,7 @@ inline int32_t cuda_status(cudaError_t e, const char* where) {
   do {                                                                 \
     cudaError_t _e = cudaGetLastError();                               \
     if (_e != cudaSuccess) return ::npbgb::cuda_status(_e, where);     \
+    ::npbgb::add_launches(1);                                          \
   } while (0)
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
@@ -93,6 +99,12 @@ __device__ __forceinline__ void pdl_begin() {
 }
 
 extern int64_t g_cfg_pdl;  // NPBGB_CFG_PDL
+
+// Passes a launch's status through, counting the launch when it succeeded.
+inline cudaError_t counted(cudaError_t e) {
+  if (e == cudaSuccess) add_launches(1);
+  return e;
+}
 extern int64_t g_cfg_hdiff_emu;  // NPBGB_CFG_HDIFF_EMU
 
 // allow_pdl = false launches in plain stream order whatever NPBGB_CFG_PDL says
@@ -110,7 +122,7 @@ cudaError_t launch_chained_if(bool allow_pdl, void (*kernel)(KArgs...), dim3 gri
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = (allow_pdl && g_cfg_pdl) ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+  return counted(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
 }
 
 template <typename... KArgs, typename... Args>

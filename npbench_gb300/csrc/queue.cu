@@ -529,7 +529,7 @@ int slots_per_sm(int ctas_per_sm, int* per_sm_out) {
 
 cudaError_t launch_worker(const QArgs& args, int nctas, int ctas_per_sm, cudaStream_t st) {
   worker_fn(ctas_per_sm)<<<dim3(unsigned(nctas)), dim3(kQThreads), 0, st>>>(args);
-  return cudaGetLastError();
+  return counted(cudaGetLastError());
 }
 
 }  // namespace qhost

@@ -372,7 +372,7 @@ extern "C" int32_t npbgb_vadv(void* utens_stage, const void* u_stage, const void
         static_cast<double*>(utens_stage), static_cast<const double*>(u_stage),
         static_cast<const double*>(wcon), static_cast<const double*>(u_pos),
         static_cast<const double*>(utens), dtr_stage, ncol, J, K, static_cast<double*>(ws));
-  cudaError_t le = cudaGetLastError();
+  cudaError_t le = counted(cudaGetLastError());
   if (workspace == nullptr) cudaFreeAsync(ws, st);
   return cuda_status(le, "vadv_columns");
 }

@@ -86,6 +86,24 @@ def test_argument_errors_are_status_codes_not_crashes():
     for key, bad in ((_lib.NPBGB_CFG_JACOBI1D_CTAS, 9), (_lib.NPBGB_CFG_JACOBI1D_DEPTH, 33),
                      (_lib.NPBGB_CFG_JACOBI1D_DEPTH, 66), (_lib.NPBGB_CFG_JACOBI1D_CTAS, -1)):
         assert lib.npbgb_set_config(key, bad) == _lib.NPBGB_ERR_ARG
+    for key, bad in ((_lib.NPBGB_CFG_HEAT_STAGES, 5), (_lib.NPBGB_CFG_HEAT_STAGES, 2),
+                     (_lib.NPBGB_CFG_JACOBI_BANDS_WARPS, 12), (_lib.NPBGB_CFG_JACOBI_BANDS, 3),
+                     (_lib.NPBGB_CFG_LAUNCHES, 7)):
+        assert lib.npbgb_set_config(key, bad) == _lib.NPBGB_ERR_ARG
+    assert _lib.get_config(_lib.NPBGB_CFG_HEAT_STAGES) == 0
+    assert _lib.get_config(_lib.NPBGB_CFG_JACOBI_BANDS_WARPS) == 0
+
+
+def test_launch_counter_counts_only_launched_kernels():
+    """The library's launch counter resets to 0 and does not move for calls that
+    launch nothing (no-op sizes and argument errors)."""
+    lib = _lib.load()
+    _lib.set_config(_lib.NPBGB_CFG_LAUNCHES, 0)
+    assert _lib.launches() == 0
+    assert lib.npbgb_jacobi2d(None, None, 100, 100, 1, _lib.NPBGB_F64, None) == _lib.NPBGB_OK
+    assert lib.npbgb_heat3d(None, None, 100, 2, 100, 50, _lib.NPBGB_F64, None) == _lib.NPBGB_OK
+    assert lib.npbgb_set_config(_lib.NPBGB_CFG_PDL, 2) == _lib.NPBGB_ERR_ARG
+    assert _lib.launches() == 0
 
 
 def test_noop_sizes_return_ok_without_touching_memory():

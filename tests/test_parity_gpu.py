@@ -802,19 +802,50 @@ def test_heat_f32_two_steps_per_launch(shape, tsteps):
 @pytest.mark.parametrize("n,tb", [(384, 2), (416, 0)])
 def test_heat_f32_two_steps_full_size_out_of_l2(n, tb):
     """Binary32 grids beyond L2 against the oracle: 384^3 with the two-step kernel
-    forced, 416^3 (275 MB per array) where the automatic choice takes it."""
+    forced; 416^3 (275 MB per array) with the automatic choice (one step, 4-plane
+    chunks) at each depth of the shared-memory plane ring."""
     from npbench_gb300 import _lib
-    A, B = workloads.uniform_heat((n, n, n), np.float32, seed=33)
-    dA, dB = _dev(A), _dev(B)
-    old = _lib.set_config(_lib.NPBGB_CFG_HEAT_TB, tb)
-    try:
-        stencils.heat_3d_kernel(10, dA, dB)
-        _lib.device_status()
-    finally:
-        _lib.set_config(_lib.NPBGB_CFG_HEAT_TB, old)
+    A0, B0 = workloads.uniform_heat((n, n, n), np.float32, seed=33)
+    A, B = A0.copy(), B0.copy()
     cref.heat_3d_kernel(10, A, B)
-    assert bits_equal(_host(dA), A), first_diff(_host(dA), A)
-    assert bits_equal(_host(dB), B)
+    old = (_lib.set_config(_lib.NPBGB_CFG_HEAT_TB, tb),
+           _lib.get_config(_lib.NPBGB_CFG_HEAT_STAGES))
+    try:
+        for stages in ((0,) if tb == 2 else (0, 4, 6, 8)):
+            _lib.set_config(_lib.NPBGB_CFG_HEAT_STAGES, stages)
+            dA, dB = _dev(A0), _dev(B0)
+            stencils.heat_3d_kernel(10, dA, dB)
+            _lib.device_status()
+            assert bits_equal(_host(dA), A), (stages, first_diff(_host(dA), A))
+            assert bits_equal(_host(dB), B), stages
+            del dA, dB
+    finally:
+        _lib.set_config(_lib.NPBGB_CFG_HEAT_TB, old[0])
+        _lib.set_config(_lib.NPBGB_CFG_HEAT_STAGES, old[1])
+
+
+@pytest.mark.parametrize("stages", [4, 6, 8])
+@pytest.mark.parametrize("chunk", [0, 1, 3, 4, 9])
+def test_heat_f32_plane_ring_depths(stages, chunk):
+    """The binary32 TMA kernel at each ring depth and plane chunk, ragged shapes, against
+    the oracle."""
+    from npbench_gb300 import _lib
+    old = (_lib.get_config(_lib.NPBGB_CFG_HEAT_STAGES), _lib.get_config(_lib.NPBGB_CFG_HEAT_CHUNK))
+    try:
+        _lib.set_config(_lib.NPBGB_CFG_HEAT_STAGES, stages)
+        _lib.set_config(_lib.NPBGB_CFG_HEAT_CHUNK, chunk)
+        for shape in ((5, 6, 8), (37, 45, 68), (70, 33, 100)):
+            A = workloads.uniform_heat(shape, np.float32, seed=stages + chunk)[0]
+            ra, rb = A.copy(), A.copy()
+            cref.heat_3d_kernel(7, ra, rb)
+            dA, dB = _dev(A), _dev(A)
+            stencils.heat_3d_kernel(7, dA, dB)
+            _lib.device_status()
+            assert bits_equal(_host(dA), ra), (shape, first_diff(_host(dA), ra))
+            assert bits_equal(_host(dB), rb), shape
+    finally:
+        _lib.set_config(_lib.NPBGB_CFG_HEAT_STAGES, old[0])
+        _lib.set_config(_lib.NPBGB_CFG_HEAT_CHUNK, old[1])
 
 
 @pytest.mark.parametrize("shape", [(5, 5), (300, 7), (7, 300), (157, 1000), (1000, 1000),
@@ -822,8 +853,9 @@ def test_heat_f32_two_steps_full_size_out_of_l2(n, tb):
 @pytest.mark.parametrize("tsteps", [2, 3, 9, 60])
 def test_jacobi_bands_in_shared_memory(shape, tsteps):
     """The whole Jacobi-2D time loop in one launch, bands of rows resident in shared
-    memory (forced on), against the oracle and against the chained launches (forced
-    off), in both precisions; A and B start with different faces."""
+    memory (forced on, with the warps per CTA by width and forced to 8 and 32; and
+    automatic), against the oracle and against the chained launches (forced off), in
+    both precisions; A and B start with different faces."""
     from npbench_gb300 import _lib
     old = (_lib.get_config(_lib.NPBGB_CFG_JACOBI_BANDS),
            _lib.get_config(_lib.NPBGB_CFG_JACOBI_BANDS_WARPS))
@@ -832,7 +864,7 @@ def test_jacobi_bands_in_shared_memory(shape, tsteps):
             A, B = workloads.uniform_pair(shape, dtype, seed=sum(shape) + tsteps)
             ra, rb = A.copy(), B.copy()
             cref.jacobi_2d_kernel(tsteps, ra, rb)
-            for mode, warps in ((2, 32), (2, 8), (1, 32)):
+            for mode, warps in ((2, 0), (2, 8), (2, 32), (0, 0), (1, 0)):
                 _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS, mode)
                 _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS_WARPS, warps)
                 dA, dB = _dev(A), _dev(B)
@@ -843,3 +875,30 @@ def test_jacobi_bands_in_shared_memory(shape, tsteps):
     finally:
         _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS, old[0])
         _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS_WARPS, old[1])
+
+
+def test_launch_counter_matches_the_paths_taken():
+    """The library's launch counter: binary64 Jacobi-2D 1000^2 at TSTEPS=100 is one
+    launch (bands in shared memory), binary32 198 chained launches, and a batch graph
+    counts its kernels at each replay."""
+    import torch
+    from npbench_gb300 import _lib
+    from npbench_gb300.batch import Batch
+    for dt, want in ((np.float64, 1), (np.float32, 198)):
+        A, B = workloads.uniform_pair((1000, 1000), dt, seed=5)
+        dA, dB = _dev(A), _dev(B)
+        torch.cuda.synchronize()
+        n0 = _lib.launches()
+        stencils.jacobi_2d_kernel(100, dA, dB)
+        torch.cuda.synchronize()
+        assert _lib.launches() - n0 == want, dt
+    grids = [_dev(x) for x in workloads.uniform_pair((100, 90), np.float64, seed=6)]
+    with Batch([(grids[0], grids[1], 5)], mode="stepped") as b:
+        b.launch(graph=True)
+        torch.cuda.synchronize()
+        n0 = _lib.launches()
+        b.launch(graph=True)
+        b.launch(graph=True)
+        torch.cuda.synchronize()
+        assert b.info()["ctas"] == 8  # stepped form: one launch per half-sweep
+        assert _lib.launches() - n0 == 2 * 8
