@@ -101,10 +101,11 @@ extern "C" {
                                          planes per CTA; 0 (default) = automatic */
 #define NPBGB_CFG_JACOBI_BANDS 18     /* jacobi2d: the whole time loop in one launch with
                                          bands of rows resident in shared memory.
-                                         0 (default): binary64 runs of 16 half-sweeps or
-                                         more whose bands fit; 1: never; 2: whenever the
-                                         bands fit (binary32 too).  Results are
-                                         identical either way. */
+                                         2: whenever the bands fit; 0 (default) or 1:
+                                         chained launches (measured faster over mixed
+                                         shapes and under concurrent streams; the
+                                         autotuner picks 2 per shape class where it
+                                         wins).  Results are identical either way. */
 #define NPBGB_CFG_JACOBI_BANDS_WARPS 19 /* warps per CTA of that kernel: 8, 16 or 32;
                                            0 (default): one 32-column strip per warp,
                                            8 to 32 warps */
@@ -116,6 +117,14 @@ extern "C" {
                                          kernels it holds (a launch recorded into a
                                          caller's graph counts once, when recorded);
                                          set 0 to reset */
+#define NPBGB_CFG_HEAT_MAD_ROWS 22    /* heat3d binary64 TMA kernel: fixed-point tile
+                                         rows (the first ones) whose 64-bit adds run as
+                                         multiply-adds on the FMA pipe; 0 (default) */
+#define NPBGB_CFG_QUEUE_WHOLE_CELLS 23 /* tile queue: grids of at most this many cells
+                                          per array run whole (one CTA sweeps every
+                                          tile of a half-sweep and runs on to the next
+                                          ones, up to 256, before returning the grid
+                                          to the ring); 0 = never; default 65536 */
 
 /* Batch forms. */
 #define NPBGB_BATCH_PERSISTENT 1
@@ -208,9 +217,9 @@ NPBGB_API int32_t npbgb_probe_pipe(int32_t op, int64_t iters, int32_t ctas, void
  *   dst = 0.2 * ((((c + w) + e) + s) + n)
  * Boundary rows and columns are never written.  On return A holds the newest
  * field and B the previous one, as in the reference.  tsteps <= 1 is a no-op.
- * Grids whose bands of rows fit in shared memory run the whole loop in one
- * cooperative launch (NPBGB_CFG_JACOBI_BANDS; its exchange rows come from a
- * stream-ordered pool), others one chained launch per half-sweep. */
+ * One chained launch per half-sweep; with NPBGB_CFG_JACOBI_BANDS = 2, grids
+ * whose bands of rows fit in shared memory run the whole loop in one
+ * cooperative launch (its exchange rows come from a stream-ordered pool). */
 NPBGB_API int32_t npbgb_jacobi2d(void* A, void* B, int64_t ny, int64_t nx, int32_t tsteps,
                        int32_t dtype, void* stream);
 

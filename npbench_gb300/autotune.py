@@ -71,10 +71,10 @@ def _space(bench, dtype):
             for ch in (0, 3, 4, 6, 8, 16, 32):
                 cfg = {"JACOBI_HW_WARPS": hw, "JACOBI_CHUNK": ch}
                 if f64:
-                    cfg["JACOBI_BANDS"] = 1  # chained launches
+                    cfg["JACOBI_BANDS"] = 0  # chained launches
                 out.append(cfg)
             if f64:  # the whole loop in one launch where the bands fit
-                out.append({"JACOBI_HW_WARPS": hw, "JACOBI_CHUNK": 0, "JACOBI_BANDS": 0})
+                out.append({"JACOBI_HW_WARPS": hw, "JACOBI_CHUNK": 0, "JACOBI_BANDS": 2})
     elif bench == "heat_3d":
         for rows in (1, 2, 4):
             tj = 8 * rows
@@ -477,6 +477,8 @@ def main(argv=None):
     ap.add_argument("--batch", action="store_true")
     ap.add_argument("--server", action="store_true")
     ap.add_argument("--ship", metavar="FILE", help="tune the benchmark classes into FILE")
+    ap.add_argument("--out", metavar="FILE",
+                    help="store a --bench/--batch/--server result in FILE, not the user cache")
     a = ap.parse_args(argv)
     if a.ship:
         grids = [("heat_3d", (256,) * 3, "float64"), ("heat_3d", (256,) * 3, "float32"),
@@ -490,10 +492,10 @@ def main(argv=None):
         print(json.dumps({"server": tune_server(path=a.ship)}), flush=True)
         return
     if a.batch:
-        print(json.dumps(tune_batch()))
+        print(json.dumps(tune_batch(path=a.out)))
         return
     if a.server:
-        print(json.dumps(tune_server()))
+        print(json.dumps(tune_server(path=a.out)))
         return
     if not a.bench:
         ap.error("give --bench, --batch, --server or --ship")
@@ -504,7 +506,7 @@ def main(argv=None):
         shape = (n, n) if a.bench == "jacobi_2d" else (n, n, n)
     else:
         ap.error("give --preset or --shape")
-    entry = tune(a.bench, shape, a.dtype)
+    entry = tune(a.bench, shape, a.dtype, path=a.out)
     print(json.dumps({key(a.bench, shape, a.dtype): entry}))
 
 

@@ -28,9 +28,11 @@ int64_t g_cfg_jacobi1d_ctas = 0;   // 0: default
 int64_t g_cfg_jacobi1d_depth = 0;  // 0: default
 int64_t g_cfg_heat_tb = 0;         // binary32 Heat-3D half-sweeps per launch (0: by size)
 int64_t g_cfg_heat_tb_chunk = 0;   // 0: automatic
-int64_t g_cfg_jacobi_bands = 0;    // 0: automatic, 1: off, 2: whenever the bands fit
+int64_t g_cfg_jacobi_bands = 0;    // 0, 1: chained launches; 2: bands whenever they fit
 int64_t g_cfg_jacobi_bands_warps = 0;  // 0: by the grid's width
 int64_t g_cfg_heat_stages = 0;         // 0: automatic (8)
+int64_t g_cfg_heat_mad_rows = 0;
+int64_t g_cfg_queue_whole_cells = 65536;
 
 namespace {
 std::atomic<int64_t> g_launches{0};
@@ -185,6 +187,15 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "jacobi bands: 0, 1 or 2");
       g_cfg_jacobi_bands = value;
       return NPBGB_OK;
+    case NPBGB_CFG_QUEUE_WHOLE_CELLS:
+      if (value < 0 || value > (int64_t(1) << 40))
+        return set_error(NPBGB_ERR_ARG, "queue whole cells: 0 .. 2^40");
+      g_cfg_queue_whole_cells = value;
+      return NPBGB_OK;
+    case NPBGB_CFG_HEAT_MAD_ROWS:
+      if (value < 0 || value > 64) return set_error(NPBGB_ERR_ARG, "heat mad rows: 0 .. 64");
+      g_cfg_heat_mad_rows = value;
+      return NPBGB_OK;
     case NPBGB_CFG_LAUNCHES:
       if (value != 0) return set_error(NPBGB_ERR_ARG, "launch count: only 0 (reset) may be set");
       g_launches.store(0, std::memory_order_relaxed);
@@ -232,6 +243,8 @@ int32_t npbgb_get_config(int32_t key, int64_t* value) {
     case NPBGB_CFG_JACOBI_BANDS: *value = g_cfg_jacobi_bands; return NPBGB_OK;
     case NPBGB_CFG_JACOBI_BANDS_WARPS: *value = g_cfg_jacobi_bands_warps; return NPBGB_OK;
     case NPBGB_CFG_HEAT_STAGES: *value = g_cfg_heat_stages; return NPBGB_OK;
+    case NPBGB_CFG_QUEUE_WHOLE_CELLS: *value = g_cfg_queue_whole_cells; return NPBGB_OK;
+    case NPBGB_CFG_HEAT_MAD_ROWS: *value = g_cfg_heat_mad_rows; return NPBGB_OK;
     case NPBGB_CFG_LAUNCHES: *value = g_launches.load(std::memory_order_relaxed); return NPBGB_OK;
     default: return set_error(NPBGB_ERR_ARG, "unknown config key %d", key);
   }

@@ -40,6 +40,7 @@ extern int64_t g_cfg_heat_hw_rows;
 extern int64_t g_cfg_f64_cvt;
 extern int64_t g_cfg_heat_tb;
 extern int64_t g_cfg_heat_stages;
+extern int64_t g_cfg_heat_mad_rows;
 
 int32_t heat3d_tb2_run(float* a, float* b, int64_t n0, int64_t n1, int64_t n2, int32_t tsteps,
                        cudaStream_t st, int32_t (*single_pairs)(float*, float*, int64_t, int64_t,
@@ -113,7 +114,7 @@ template <typename T, bool FX, int R, bool CVT, int NS>
 __global__ void __launch_bounds__(kThreads)
 heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ src,
            T* __restrict__ dst, int64_t n0, int64_t n1, int64_t n2, int chunk, int hw_rows,
-           uint32_t one) {
+           int mad_rows, uint32_t one) {
   pdl_begin();
   using G = TmaGeom<T, R>;
   using S = typename std::conditional<FX, int64_t, T>::type;
@@ -245,7 +246,8 @@ heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ sr
             const uint32_t tag =
                 hi32(c) | hi32(ip) | hi32(im) | hi32(jp) | hi32(jm) | hi32(kp) | hi32(km);
             if (!(tag & kPoisonHi))
-              out = heat_point_fxm<CVT, false>(c, ip, im, jp, jm, kp, km, one);
+              out = row < mad_rows ? heat_point_fxm<CVT, true>(c, ip, im, jp, jm, kp, km, one)
+                                   : heat_point_fxm<CVT, false>(c, ip, im, jp, jm, kp, km, one);
             else
               out = heat_point<T>(q[0], q[s0], q[-s0], q[s1], q[-s1], q[1], q[-1]);
           }
@@ -338,14 +340,17 @@ int32_t launch_tma(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tstep
   const int hw_default = R == 2 ? 7 : (R == 1 ? 3 : G::TJ / 4);
   int hw = g_cfg_heat_hw_rows >= 0 ? int(g_cfg_heat_hw_rows) : (FX ? hw_default : 0);
   if (hw > G::TJ) hw = G::TJ;
+  // Fixed-point tile rows (the first mad rows) whose 64-bit adds go to the
+  // multiply-add pipe instead of the integer ALU.
+  const int mad = FX ? int(std::min<int64_t>(g_cfg_heat_mad_rows, G::TJ)) : 0;
   const dim3 block{unsigned(kThreads)};
   cudaError_t e = cudaSuccess;
   for (int32_t t = 1; t < tsteps && e == cudaSuccess; ++t) {
     e = launch_chained(heat3d_tma<T, FX, R, CVT, NS>, grid, block, smem, st, map_a, a, b, n0, n1, n2,
-                       chunk, hw, 1u);
+                       chunk, hw, mad, 1u);
     if (e == cudaSuccess)
       e = launch_chained(heat3d_tma<T, FX, R, CVT, NS>, grid, block, smem, st, map_b, b, a, n0, n1,
-                         n2, chunk, hw, 1u);
+                         n2, chunk, hw, mad, 1u);
   }
   return cuda_status(e, "heat3d_tma");
 }

@@ -194,21 +194,24 @@ int bands_warps(int64_t nx) {
 
 }  // namespace
 
-// Runs the whole time loop of Jacobi-2D in one cooperative launch when the
-// bands fit in shared memory (about 1.4 M binary64 cells or 2.8 M binary32
-// cells on 152 SMs); NPBGB_ERR_STATE otherwise (the caller then uses the
-// chained kernels).  Automatic for binary64 runs of 16 half-sweeps or more:
-// with the warps above it measured 3-20% faster than the chained launches
-// (1000^2: 2.02 against 2.09 ms; 150^2 TSTEPS=50: 0.315 against 0.394 ms).
-// Binary32 stays on the chained launches, which measured faster at every
-// size tried (1000^2: 0.71 against 1.03 ms), because the binary32 half-sweep
-// is short enough that the band hand-off costs more than a launch boundary.
+// Runs the whole time loop of Jacobi-2D in one cooperative launch when asked
+// (NPBGB_CFG_JACOBI_BANDS = 2) and the bands fit in shared memory (about 1.4 M
+// binary64 cells or 2.8 M binary32 cells on 152 SMs); NPBGB_ERR_STATE
+// otherwise (the caller then uses the chained kernels).  It is not the
+// automatic choice.  Measured on GB300 against the chained launches: binary64
+// 1000^2 TSTEPS=100 2.01 against 2.08 ms and 150^2 TSTEPS=50 0.32 against 0.39
+// ms, but over 120 grids of the batched configuration (64 to 2048 per side,
+// binary64) 337 against 330 ms in all: one CTA per SM leaves tall, narrow
+// grids latency-bound, and grids wider than 1026 columns give some warps two
+// strips.  On the served stream it also cost 3-5% of throughput, because the
+// cooperative launch holds every SM while other streams' kernels wait.
+// Binary32 measured slower at every size (1000^2: 1.02 against 0.71 ms).  The
+// autotuner takes it per shape class where it measures faster.
 template <typename T>
 int32_t jacobi2d_bands_run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st) {
-  if (g_cfg_jacobi_bands == 1) return NPBGB_ERR_STATE;
+  if (g_cfg_jacobi_bands != 2) return NPBGB_ERR_STATE;
   if (tsteps <= 1 || ny < 3 || nx < 3) return NPBGB_ERR_STATE;
   const int32_t hs = 2 * (tsteps - 1);
-  if (g_cfg_jacobi_bands == 0 && (sizeof(T) != 8 || hs < 16)) return NPBGB_ERR_STATE;
   int dev = 0, sms = 0, smem_max = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

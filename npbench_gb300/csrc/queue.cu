@@ -23,9 +23,15 @@
 // order, so a claimed tile never waits on anything and the kernel needs no
 // co-residency (plain launch, not cooperative).  A claim takes several tiles
 // of a large segment at once (ntiles / (4 * CTAs), at least one).  Grids of
-// different sizes,
-// kinds and precisions interleave tile by tile, and a grid's next half-sweep
-// starts as soon as its own previous one is done.
+// different sizes, kinds and precisions interleave tile by tile, and a grid's
+// next half-sweep starts as soon as its own previous one is done.
+//
+// Small grids (NPBGB_CFG_QUEUE_WHOLE_CELLS) run whole: their segments are one
+// claimable unit, the claiming CTA sweeps every tile of the half-sweep and
+// then runs on to the grid's next half-sweeps itself (a CTA barrier between
+// them), up to kLocalRun, before it returns the grid to the ring.  A stream of
+// many small grids then costs one claim per kLocalRun half-sweeps instead of
+// one per tile, and its parallelism comes from the grids, one per CTA.
 //
 // New grids arrive through an inbox that the host may append to while the
 // kernel runs: a descriptor table, a ring of slot indices and a published
@@ -59,6 +65,8 @@
 #include "tma.cuh"
 
 namespace npbgb {
+
+extern int64_t g_cfg_queue_whole_cells;
 
 extern int64_t g_cfg_f64_emulation;
 
@@ -168,8 +176,8 @@ __device__ bool activate(const QArgs& q) {
       volatile uint32_t* vdone = q.done + slot;
       *vdone = 0u;
       atomicAdd(&q.st->active, 1u);
-      const int32_t ntiles = ld_rlx_gpu(&q.slots[slot].ntiles);
-      produce(q, slot, 0, ntiles);
+      const int32_t units = ld_rlx_gpu(&q.slots[slot].whole) ? 1 : ld_rlx_gpu(&q.slots[slot].ntiles);
+      produce(q, slot, 0, units);
       did = true;
     }
     st_rel_gpu(&q.st->inbox_head, ih);
@@ -299,14 +307,16 @@ __device__ void next_tiles(const QArgs& q, Claim* out, Waiting& w) {
   }
 }
 
-// Thread 0, after the CTA's barrier: counts the tiles and hands on the grid.
+// Thread 0, after the CTA's barrier: counts the units (tiles, or whole
+// segments) up to segment s and hands on the grid.
 __device__ void complete_tiles(const QArgs& q, int32_t slot, int32_t s, int32_t count,
                                const QSlot& G) {
   // bar.sync ordered the CTA's stores before this release, which is cumulative.
+  const uint32_t units = uint32_t(seg_units(G));
   const uint32_t old = atom_add_acq_rel(&q.done[slot], uint32_t(count));
-  if (old + uint32_t(count) == uint32_t(s + 1) * uint32_t(G.ntiles)) {
+  if (old + uint32_t(count) == uint32_t(s + 1) * units) {
     if (s + 1 < G.steps) {
-      produce(q, slot, s + 1, G.ntiles);
+      produce(q, slot, s + 1, int32_t(units));
     } else {
       if (q.finished) st_rel_sys(&q.finished[slot], G.gen);
       atomicSub(&q.st->active, 1u);
@@ -420,9 +430,23 @@ __global__ void __launch_bounds__(kQThreads, MINB) queue_worker(const QArgs q) {
     if (slot < 0) return;
     const int32_t s = s_cmd[1], t0 = s_cmd[2], t1 = s_cmd[3];
     const QSlot G = s_slot;
-    for (int32_t tile = t0; tile < t1; ++tile) sweep_tile(q, G, s, tile, plane);
+    if (!G.whole) {
+      for (int32_t tile = t0; tile < t1; ++tile) sweep_tile(q, G, s, tile, plane);
+      __syncthreads();
+      if (tid == 0) complete_tiles(q, slot, s, t1 - t0, G);
+      continue;
+    }
+    // Whole-grid slot: this CTA owns the segment (its one unit), so it runs
+    // the grid's next segments itself, a CTA barrier between consecutive
+    // half-sweeps ordering them, and returns the grid to the ring after
+    // kLocalRun segments or at its end.
+    const int32_t end = min(G.steps, s + kLocalRun);
+    for (int32_t s2 = s; s2 < end; ++s2) {
+      if (s2 > s) __syncthreads();  // the previous half-sweep's stores before these loads
+      for (int32_t tile = 0; tile < G.ntiles; ++tile) sweep_tile(q, G, s2, tile, plane);
+    }
     __syncthreads();
-    if (tid == 0) complete_tiles(q, slot, s, t1 - t0, G);
+    if (tid == 0) complete_tiles(q, slot, end - 1, end - s, G);
   }
 }
 
@@ -513,6 +537,10 @@ int32_t describe(const npbgb_grid& G, int64_t g, int32_t tile_rows, int32_t tile
   if (ntiles * (todo + 2) >= (int64_t(1) << 32))
     return set_error(NPBGB_ERR_ARG, "queue: grid %lld: more than 2^32 tiles in one run", (long long)g);
   out->ntiles = int32_t(ntiles);
+  // Small grids run whole: one CTA per half-sweep, several half-sweeps in a
+  // row, with no ring traffic in between (their tiles would each carry a
+  // claim and a hand-off for very little arithmetic).
+  out->whole = (g_cfg_queue_whole_cells > 0 && out->cells <= g_cfg_queue_whole_cells) ? 1 : 0;
   *updates = todo * (G.n0 - 2) * (G.n1 - 2) * (heat ? (n2 - 2) : 1);
   return NPBGB_OK;
 }
@@ -869,7 +897,7 @@ int32_t plan_static(const npbgb_grid* grids, int64_t count, int32_t tile_rows, i
   std::vector<unsigned long long> claim(s->ring_size, 0ull);
   for (size_t i = 0; i < ring.size(); ++i) ring[i] = qdev::QSeg{-1, -1, -1, qdev::kSeqEmpty};
   for (size_t i = 0; i < slots.size(); ++i) {
-    ring[i] = qdev::QSeg{int32_t(i), 0, slots[i].ntiles, uint32_t(i)};
+    ring[i] = qdev::QSeg{int32_t(i), 0, qdev::seg_units(slots[i]), uint32_t(i)};
     claim[i] = uint64_t(i) << 32;
   }
   qdev::QState st0{};

@@ -30,7 +30,8 @@ struct QSlot {
   uint32_t gen;       // residency number, written to the completion word
   int32_t steps;      // segments: total, plus 2 with conv
   int32_t conv;
-  int32_t pad0;
+  int32_t whole;      // 1: one CTA sweeps all tiles of a segment and runs on
+                      // to the next ones (the ring holds one unit per segment)
   int64_t cells;      // elements per array
   int64_t pad1[4];
 };
@@ -43,6 +44,13 @@ struct QSeg {
   int32_t ntiles;
   uint32_t seq;
 };
+
+// Claimable units per segment: every tile, or one for a whole-grid slot.
+__host__ __device__ inline int32_t seg_units(const QSlot& G) { return G.whole ? 1 : G.ntiles; }
+
+// Segments a CTA runs in a row on a whole-grid slot before it hands the grid
+// back to the ring (bounds how long one grid holds a CTA).
+constexpr int32_t kLocalRun = 256;
 
 struct QState {
   uint32_t head;        // ring position tiles are claimed from

@@ -19,8 +19,8 @@ without ever waiting for the GPU:
   sizes, kinds and precisions, and its next half-sweep starts as soon as its
   own previous one is done.  A larger grid fills the GPU by itself and goes to
   a big-grid lane (its own stream) that runs it with the tuned single-grid
-  kernels (TMA pipelines, two half-sweeps per launch in binary32 Heat-3D),
-  shortest job first; the queue's CTAs share the SMs with those launches;
+  kernels (TMA pipelines, the binary64 Jacobi-2D loop in one launch), in
+  the tuned lane order; the queue's CTAs share the SMs with those launches;
 * **completion**: the worker writes a completion word to host memory when a
   grid's last half-sweep is done, and a lane records an event; the serving
   thread polls both;

@@ -27,6 +27,13 @@ heat_f32_tb Heat-3D 416^3 float32, TSTEPS=6: 4 two-step   heat3d_tb2, -s 1
            launches, then one single-step pair
 heat_f32_384 Heat-3D 384^3 float32, TSTEPS=3, one step    heat3d_tma, -s 2
            per launch
+heat_f32_512 Heat-3D 512^3 float32, TSTEPS=3 (automatic   heat3d_tma, -s 2
+           5-plane chunks)
+heat_f32_chunks  timing sweep (CUDA events, no ncu) of    -
+           the binary32 Heat-3D plane chunks and forms,
+           256^3 to 640^3, TSTEPS=21; one JSON line per size
+jacobi_bands_1000  Jacobi-2D 1000^2 float64, TSTEPS=10,   jacobi2d_bands, -c 1
+           one launch with the bands in shared memory
 batch1024  the first 1024 grids of the 4096-grid batch,   batch_step, -s 100
            stepped form, TSTEPS as drawn (about 4 GB)
 queue_mix  240 small mixed grids through the tile queue   queue_worker, -c 1
@@ -41,6 +48,55 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
+
+
+def _heat_f32_chunks(dev, sizes=(256, 384, 416, 512, 640), T=21):
+    """Median CUDA-event time of kernel(T, A, B) per binary32 Heat-3D setting and its
+    fraction of the measured copy bandwidth at 8 bytes per update."""
+    import json
+
+    import torch
+
+    from npbench_gb300 import _lib, autotune, stencils, workloads
+    autotune.disable()
+    peak = 6687.5
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        pass
+    keys = {k: getattr(_lib, "NPBGB_CFG_" + k) for k in ("HEAT_TB", "HEAT_TB_CHUNK", "HEAT_CHUNK")}
+    settings = ([("auto", {})] + [(f"chunk {c}", {"HEAT_TB": 1, "HEAT_CHUNK": c})
+                                  for c in (4, 5, 6, 8, 16, 32, 64, 128)] +
+                [(f"two-step chunk {c}", {"HEAT_TB": 2, "HEAT_TB_CHUNK": c}) for c in (8, 16, 32)])
+    st = torch.cuda.current_stream(dev)
+    for n in sizes:
+        A0, _ = workloads.uniform_heat((n,) * 3, np.float32, seed=1)
+        pa = torch.from_numpy(A0).to(dev)
+        del A0
+        a, b = torch.empty_like(pa), torch.empty_like(pa)
+        row = {}
+        for name, cfg in settings:
+            old = {k: _lib.set_config(keys[k], v) for k, v in cfg.items()}
+            ts = []
+            for rep in range(5):
+                a.copy_(pa)
+                b.copy_(pa)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                stencils.heat_3d_kernel(T, a, b)
+                e1.record(st)
+                e1.synchronize()
+                if rep >= 2:
+                    ts.append(e0.elapsed_time(e1))
+            for k, v in old.items():
+                _lib.set_config(keys[k], v)
+            ms = float(np.median(ts))
+            frac = 2 * (T - 1) * (n - 2) ** 3 * 8 / (ms * 1e-3) / 1e9 / peak
+            row[name] = [round(ms, 3), round(frac, 3)]
+        print(json.dumps({"n": n, "TSTEPS": T, "peak_gbs": peak, "ms_and_frac": row}), flush=True)
+        del pa, a, b
+        torch.cuda.empty_cache()
 
 
 def run(case):
@@ -115,6 +171,16 @@ def run(case):
         A, B = workloads.uniform_heat((n,) * 3, np.float32, seed=0)
         a, b = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
         stencils.heat_3d_kernel(T, a, b)
+    elif case == "heat_f32_512":
+        A, B = workloads.uniform_heat((512,) * 3, np.float32, seed=0)
+        a, b = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+        stencils.heat_3d_kernel(3, a, b)
+    elif case == "heat_f32_chunks":
+        _heat_f32_chunks(dev)
+    elif case == "jacobi_bands_1000":
+        A, B = workloads.uniform_pair((1000, 1000), np.float64, seed=0)
+        a, b = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+        stencils.jacobi_2d_kernel(10, a, b)
     elif case == "batch1024":
         from npbench_gb300.batch import Batch
         specs = workloads.batch_jacobi_specs(4096, seed=0)[:1024]

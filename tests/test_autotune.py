@@ -41,9 +41,9 @@ def test_keys_name_benchmark_dtype_and_shape_class():
 
 def test_search_spaces():
     sp = autotune._space("jacobi_2d", np.float64)
-    assert {"JACOBI_HW_WARPS": 4, "JACOBI_CHUNK": 3, "JACOBI_BANDS": 1} in sp and len(sp) == 56
+    assert {"JACOBI_HW_WARPS": 4, "JACOBI_CHUNK": 3, "JACOBI_BANDS": 0} in sp and len(sp) == 56
     # binary64: the chained launches or the whole loop in one launch (bands)
-    assert {"JACOBI_HW_WARPS": 4, "JACOBI_CHUNK": 0, "JACOBI_BANDS": 0} in sp
+    assert {"JACOBI_HW_WARPS": 4, "JACOBI_CHUNK": 0, "JACOBI_BANDS": 2} in sp
     f32j = autotune._space("jacobi_2d", np.float32)
     assert all(c["JACOBI_HW_WARPS"] == -1 and "JACOBI_BANDS" not in c for c in f32j)
     heat = autotune._space("heat_3d", np.float64)

@@ -88,7 +88,8 @@ def test_argument_errors_are_status_codes_not_crashes():
         assert lib.npbgb_set_config(key, bad) == _lib.NPBGB_ERR_ARG
     for key, bad in ((_lib.NPBGB_CFG_HEAT_STAGES, 5), (_lib.NPBGB_CFG_HEAT_STAGES, 2),
                      (_lib.NPBGB_CFG_JACOBI_BANDS_WARPS, 12), (_lib.NPBGB_CFG_JACOBI_BANDS, 3),
-                     (_lib.NPBGB_CFG_LAUNCHES, 7)):
+                     (_lib.NPBGB_CFG_LAUNCHES, 7), (_lib.NPBGB_CFG_HEAT_MAD_ROWS, 65),
+                     (_lib.NPBGB_CFG_HEAT_MAD_ROWS, -1)):
         assert lib.npbgb_set_config(key, bad) == _lib.NPBGB_ERR_ARG
     assert _lib.get_config(_lib.NPBGB_CFG_HEAT_STAGES) == 0
     assert _lib.get_config(_lib.NPBGB_CFG_JACOBI_BANDS_WARPS) == 0

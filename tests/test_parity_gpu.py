@@ -703,13 +703,16 @@ def test_bounded_device_wait_reports_timeout_and_context_survives():
     assert bits_equal(_host(dA), A)
 
 
-@pytest.mark.parametrize("rows,cvt,hw", [(1, 0, 0), (2, 0, 0), (2, 1, 0), (4, 1, 3), (2, 0, 4),
-                                         (4, 0, 32)])
-def test_heat_kernel_variants_bit_exact(rows, cvt, hw):
-    """Every heat3d variant (rows per thread, conversion path, hardware rows) gives the oracle's bits."""
+@pytest.mark.parametrize("rows,cvt,hw,mad", [(1, 0, 0, 0), (2, 0, 0, 0), (2, 1, 0, 5), (4, 1, 3, 0),
+                                             (2, 0, 4, 0), (4, 0, 32, 0), (2, 0, 7, 4),
+                                             (2, 0, 7, 9), (1, 0, 3, 8), (4, 1, 8, 24)])
+def test_heat_kernel_variants_bit_exact(rows, cvt, hw, mad):
+    """Every heat3d variant (rows per thread, conversion path, hardware rows, fixed-point
+    rows with their adds on the multiply-add pipe) gives the oracle's bits."""
     from npbench_gb300 import _lib
-    keys = (_lib.NPBGB_CFG_HEAT_ROWS, _lib.NPBGB_CFG_F64_CVT, _lib.NPBGB_CFG_HEAT_HW_ROWS)
-    old = [_lib.set_config(k, v) for k, v in zip(keys, (rows, cvt, hw))]
+    keys = (_lib.NPBGB_CFG_HEAT_ROWS, _lib.NPBGB_CFG_F64_CVT, _lib.NPBGB_CFG_HEAT_HW_ROWS,
+            _lib.NPBGB_CFG_HEAT_MAD_ROWS)
+    old = [_lib.set_config(k, v) for k, v in zip(keys, (rows, cvt, hw, mad))]
     try:
         for dtype in (np.float64, np.float32):
             for field in ("uniform", "mixed"):
@@ -721,7 +724,7 @@ def test_heat_kernel_variants_bit_exact(rows, cvt, hw):
                 dA, dB = _dev(A), _dev(A)
                 stencils.heat_3d_kernel(5, dA, dB)
                 _lib.device_status()
-                assert bits_equal(_host(dA), ra), (rows, cvt, hw, dtype, field,
+                assert bits_equal(_host(dA), ra), (rows, cvt, hw, mad, dtype, field,
                                                    first_diff(_host(dA), ra))
                 assert bits_equal(_host(dB), rb)
     finally:
@@ -853,9 +856,9 @@ def test_heat_f32_plane_ring_depths(stages, chunk):
 @pytest.mark.parametrize("tsteps", [2, 3, 9, 60])
 def test_jacobi_bands_in_shared_memory(shape, tsteps):
     """The whole Jacobi-2D time loop in one launch, bands of rows resident in shared
-    memory (forced on, with the warps per CTA by width and forced to 8 and 32; and
-    automatic), against the oracle and against the chained launches (forced off), in
-    both precisions; A and B start with different faces."""
+    memory (on, with the warps per CTA by width and forced to 8 and 32), against the
+    oracle, as the chained launches (the default) are, in both precisions; A and B
+    start with different faces."""
     from npbench_gb300 import _lib
     old = (_lib.get_config(_lib.NPBGB_CFG_JACOBI_BANDS),
            _lib.get_config(_lib.NPBGB_CFG_JACOBI_BANDS_WARPS))
@@ -864,7 +867,7 @@ def test_jacobi_bands_in_shared_memory(shape, tsteps):
             A, B = workloads.uniform_pair(shape, dtype, seed=sum(shape) + tsteps)
             ra, rb = A.copy(), B.copy()
             cref.jacobi_2d_kernel(tsteps, ra, rb)
-            for mode, warps in ((2, 0), (2, 8), (2, 32), (0, 0), (1, 0)):
+            for mode, warps in ((2, 0), (2, 8), (2, 32), (0, 0)):
                 _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS, mode)
                 _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS_WARPS, warps)
                 dA, dB = _dev(A), _dev(B)
@@ -878,20 +881,28 @@ def test_jacobi_bands_in_shared_memory(shape, tsteps):
 
 
 def test_launch_counter_matches_the_paths_taken():
-    """The library's launch counter: binary64 Jacobi-2D 1000^2 at TSTEPS=100 is one
-    launch (bands in shared memory), binary32 198 chained launches, and a batch graph
-    counts its kernels at each replay."""
+    """The library's launch counter: Jacobi-2D 1000^2 at TSTEPS=100 is 198 chained
+    launches, or one with the bands in shared memory; a batch graph counts its kernels
+    at each replay."""
     import torch
-    from npbench_gb300 import _lib
+    from npbench_gb300 import _lib, autotune
     from npbench_gb300.batch import Batch
-    for dt, want in ((np.float64, 1), (np.float32, 198)):
-        A, B = workloads.uniform_pair((1000, 1000), dt, seed=5)
-        dA, dB = _dev(A), _dev(B)
-        torch.cuda.synchronize()
-        n0 = _lib.launches()
-        stencils.jacobi_2d_kernel(100, dA, dB)
-        torch.cuda.synchronize()
-        assert _lib.launches() - n0 == want, dt
+    was = autotune.enabled()
+    autotune.disable()
+    try:
+        for dt, bands, want in ((np.float64, 0, 198), (np.float64, 2, 1), (np.float32, 0, 198)):
+            old = _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS, bands)
+            A, B = workloads.uniform_pair((1000, 1000), dt, seed=5)
+            dA, dB = _dev(A), _dev(B)
+            torch.cuda.synchronize()
+            n0 = _lib.launches()
+            stencils.jacobi_2d_kernel(100, dA, dB)
+            torch.cuda.synchronize()
+            _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS, old)
+            assert _lib.launches() - n0 == want, (dt, bands)
+    finally:
+        if was:
+            autotune.enable()
     grids = [_dev(x) for x in workloads.uniform_pair((100, 90), np.float64, seed=6)]
     with Batch([(grids[0], grids[1], 5)], mode="stepped") as b:
         b.launch(graph=True)

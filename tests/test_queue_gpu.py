@@ -1,7 +1,8 @@
 """The device-side tile work queue with grids added while its worker runs.
 
 Grids of both kinds and precisions, ragged shapes and step counts are
-submitted one at a time, some while the worker kernel is already running;
+submitted one at a time, some while the worker kernel is already running,
+cut into tiles or run whole;
 each must end bit for bit as the oracle (the C restatement of the
 reference's NumPy kernels) leaves it, which is also what the grid gives when
 run alone.  The worker ends by itself once idle and is launched again for
@@ -24,6 +25,16 @@ from npbench_gb300.queue import TileQueue  # noqa: E402
 from oracle import cref  # noqa: E402
 
 DEV = torch.device("cuda", 0)
+
+
+@pytest.fixture(autouse=True, params=[0, 65536, 1 << 40], ids=["tiles", "small-whole", "all-whole"])
+def whole_cells(request):
+    """Every test with no grid run whole, with the default (grids up to 65536 cells
+    run whole: one CTA per half-sweep, running on to the next ones), and with every
+    grid run whole."""
+    old = _lib.set_config(_lib.NPBGB_CFG_QUEUE_WHOLE_CELLS, request.param)
+    yield request.param
+    _lib.set_config(_lib.NPBGB_CFG_QUEUE_WHOLE_CELLS, old)
 
 
 def _grids(n, seed, max2d=260, max3d=36, max_t=25):
@@ -112,6 +123,26 @@ def test_resumed_pieces_through_the_queue_equal_one_run():
     for (A, B, T), (a, b, _) in zip(grids, dev):
         ra, rb = _oracle(A, B, T)
         assert bits_equal(a.cpu().numpy(), ra) and bits_equal(b.cpu().numpy(), rb)
+
+
+def test_long_runs_pass_through_the_ring_many_times():
+    """Grids of 598 half-sweeps: a whole grid goes back to the ring every 256 of them
+    (and a tiled one every half-sweep); each still ends as the oracle leaves it."""
+    rng = np.random.default_rng(12)
+    grids = []
+    for shape, dt in (((40, 41), np.float64), ((33, 70), np.float32), ((10, 12, 9), np.float64),
+                      ((7, 34, 40), np.float32)):
+        A = rng.random(shape).astype(dt)
+        B = rng.random(shape).astype(dt) if len(shape) == 2 else A.copy()
+        grids.append((A, B, 300))
+    dev = [(torch.from_numpy(A).to(DEV), torch.from_numpy(B).to(DEV), T) for A, B, T in grids]
+    with TileQueue(max_slots=8) as q:
+        pending = {q.submit(a, b, T) for a, b, T in dev} - {-1}
+        _drain(q, pending)
+        _lib.device_status()
+    for (A, B, T), (a, b, _) in zip(grids, dev):
+        ra, rb = _oracle(A, B, T)
+        assert bits_equal(a.cpu().numpy(), ra) and bits_equal(b.cpu().numpy(), rb), A.shape
 
 
 def test_worker_ends_when_idle_and_is_launched_again():
