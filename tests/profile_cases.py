@@ -34,6 +34,9 @@ heat_f32_chunks  timing sweep (CUDA events, no ncu) of    -
            256^3 to 640^3, TSTEPS=21; one JSON line per size
 jacobi_bands_1000  Jacobi-2D 1000^2 float64, TSTEPS=10,   jacobi2d_bands, -c 1
            one launch with the bands in shared memory
+jacobi_f64_fx  Jacobi-2D 4096^2 float64, TSTEPS=3, every  jacobi2d_strip, -s 2
+           warp in fixed point
+jacobi_f64_hw  the same, every warp on hardware binary64  jacobi2d_strip, -s 2
 batch1024  the first 1024 grids of the 4096-grid batch,   batch_step, -s 100
            stepped form, TSTEPS as drawn (about 4 GB)
 queue_mix  240 small mixed grids through the tile queue   queue_worker, -c 1
@@ -51,8 +54,9 @@ if ROOT not in sys.path:
 
 
 def _heat_f32_chunks(dev, sizes=(256, 384, 416, 512, 640), T=21):
-    """Median CUDA-event time of kernel(T, A, B) per binary32 Heat-3D setting and its
-    fraction of the measured copy bandwidth at 8 bytes per update."""
+    """Median CUDA-event time of kernel(T, A, B) per binary32 Heat-3D setting, its
+    fraction of the measured copy bandwidth at 8 bytes per update, and the library's
+    kernel launches for one call."""
     import json
 
     import torch
@@ -83,17 +87,19 @@ def _heat_f32_chunks(dev, sizes=(256, 384, 416, 512, 640), T=21):
                 a.copy_(pa)
                 b.copy_(pa)
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                n_launch = _lib.launches()
                 e0.record(st)
                 stencils.heat_3d_kernel(T, a, b)
                 e1.record(st)
                 e1.synchronize()
+                n_launch = _lib.launches() - n_launch
                 if rep >= 2:
                     ts.append(e0.elapsed_time(e1))
             for k, v in old.items():
                 _lib.set_config(keys[k], v)
             ms = float(np.median(ts))
             frac = 2 * (T - 1) * (n - 2) ** 3 * 8 / (ms * 1e-3) / 1e9 / peak
-            row[name] = [round(ms, 3), round(frac, 3)]
+            row[name] = [round(ms, 3), round(frac, 3), n_launch]
         print(json.dumps({"n": n, "TSTEPS": T, "peak_gbs": peak, "ms_and_frac": row}), flush=True)
         del pa, a, b
         torch.cuda.empty_cache()
@@ -177,7 +183,17 @@ def run(case):
         stencils.heat_3d_kernel(3, a, b)
     elif case == "heat_f32_chunks":
         _heat_f32_chunks(dev)
+    elif case in ("jacobi_f64_fx", "jacobi_f64_hw"):
+        from npbench_gb300 import autotune
+        autotune.disable()
+        _lib.set_config(_lib.NPBGB_CFG_JACOBI_HW_WARPS, 0 if case.endswith("fx") else 8)
+        A, B = workloads.uniform_pair((4096, 4096), np.float64, seed=0)
+        a, b = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+        stencils.jacobi_2d_kernel(3, a, b)
     elif case == "jacobi_bands_1000":
+        from npbench_gb300 import autotune
+        autotune.disable()
+        _lib.set_config(_lib.NPBGB_CFG_JACOBI_BANDS, 2)
         A, B = workloads.uniform_pair((1000, 1000), np.float64, seed=0)
         a, b = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
         stencils.jacobi_2d_kernel(10, a, b)
