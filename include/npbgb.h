@@ -125,6 +125,10 @@ extern "C" {
                                           tile of a half-sweep and runs on to the next
                                           ones, up to 256, before returning the grid
                                           to the ring); 0 = never; default 65536 */
+#define NPBGB_CFG_JACOBI_FX_MUL 24    /* jacobi2d single-grid kernel, binary64: 1
+                                         (default) the fixed-point points' product by
+                                         0.2 on the integer pipes, 0 a hardware
+                                         binary64 multiply.  Results are identical. */
 
 /* Batch forms. */
 #define NPBGB_BATCH_PERSISTENT 1

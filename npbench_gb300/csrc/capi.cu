@@ -33,6 +33,7 @@ int64_t g_cfg_jacobi_bands_warps = 0;  // 0: by the grid's width
 int64_t g_cfg_heat_stages = 0;         // 0: automatic (8)
 int64_t g_cfg_heat_mad_rows = 0;
 int64_t g_cfg_queue_whole_cells = 65536;
+int64_t g_cfg_jacobi_fx_mul = 1;
 
 namespace {
 std::atomic<int64_t> g_launches{0};
@@ -187,6 +188,10 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "jacobi bands: 0, 1 or 2");
       g_cfg_jacobi_bands = value;
       return NPBGB_OK;
+    case NPBGB_CFG_JACOBI_FX_MUL:
+      if (value != 0 && value != 1) return set_error(NPBGB_ERR_ARG, "jacobi fx mul: 0 or 1");
+      g_cfg_jacobi_fx_mul = value;
+      return NPBGB_OK;
     case NPBGB_CFG_QUEUE_WHOLE_CELLS:
       if (value < 0 || value > (int64_t(1) << 40))
         return set_error(NPBGB_ERR_ARG, "queue whole cells: 0 .. 2^40");
@@ -243,6 +248,7 @@ int32_t npbgb_get_config(int32_t key, int64_t* value) {
     case NPBGB_CFG_JACOBI_BANDS: *value = g_cfg_jacobi_bands; return NPBGB_OK;
     case NPBGB_CFG_JACOBI_BANDS_WARPS: *value = g_cfg_jacobi_bands_warps; return NPBGB_OK;
     case NPBGB_CFG_HEAT_STAGES: *value = g_cfg_heat_stages; return NPBGB_OK;
+    case NPBGB_CFG_JACOBI_FX_MUL: *value = g_cfg_jacobi_fx_mul; return NPBGB_OK;
     case NPBGB_CFG_QUEUE_WHOLE_CELLS: *value = g_cfg_queue_whole_cells; return NPBGB_OK;
     case NPBGB_CFG_HEAT_MAD_ROWS: *value = g_cfg_heat_mad_rows; return NPBGB_OK;
     case NPBGB_CFG_LAUNCHES: *value = g_launches.load(std::memory_order_relaxed); return NPBGB_OK;

@@ -203,5 +203,38 @@ NPBGB_FX_FN double to_f64(int64_t w) {
   return m == 0 ? 0.0 : double_of(bits | sign);
 }
 
+// RN(0.2 * w * 2^-F), the IEEE binary64 product of 0.2 and the frame-F value
+// w, on the integer pipes.  Precondition: w == 0, or 2^12 <= w < 2^62 with at
+// most 53 significant bits (a round53 result) and a normal double result.
+//
+// The double nearest 0.2 is M * 2^-55 with M = 0x1999999999999A (53 bits), so
+// the exact product is the integer P = w * M (65 to 115 bits) times
+// 2^-(F + 55).  Its top 53 bits, rounded to nearest with ties to even on the
+// bits below them, are the significand of the IEEE product; a carry out of the
+// rounding lands in the exponent field by itself.  This is the textbook
+// multiplication of two binary floating-point numbers (exact integer product
+// of the significands, then one rounding), specialised to one constant factor.
+template <int F>
+NPBGB_FX_FN double mul02(int64_t w) {
+  constexpr uint64_t M = 0x1999999999999Aull;
+  const uint64_t a = static_cast<uint64_t>(w);
+#if defined(__CUDA_ARCH__)
+  const uint64_t lo = a * M;
+  const uint64_t hi = __umul64hi(a, M);
+#else
+  const unsigned __int128 p = static_cast<unsigned __int128>(a) * M;
+  const uint64_t lo = static_cast<uint64_t>(p);
+  const uint64_t hi = static_cast<uint64_t>(p >> 64);
+#endif
+  const int sh = (128 - clz64(hi)) - 53;          // bits below the top 53: 12 .. 62
+  uint64_t sig = (hi << ((64 - sh) & 63)) | (lo >> sh);
+  const uint64_t below = lo & ((uint64_t(1) << (sh - 1)) - 1);
+  const uint64_t half = (lo >> (sh - 1)) & 1;     // the first discarded bit
+  sig += half & static_cast<uint64_t>((below != 0) | (sig & 1));
+  // value = sig * 2^(sh - F - 55) = (sig / 2^52) * 2^(sh - F - 3)
+  const uint64_t bits = (static_cast<uint64_t>(sh - F - 3 + 1023) << 52) + (sig - (uint64_t(1) << 52));
+  return w == 0 ? 0.0 : double_of(bits);
+}
+
 }  // namespace fx
 }  // namespace npbgb

@@ -12,8 +12,11 @@
 // binary32 uses IEEE float operations.  binary64 runs its four additions
 // exactly in fixed point on the integer pipe (fx64.cuh) for every point whose
 // five inputs lie in [2^-7, 1) or are +0 (refused values carry a poison bit),
-// and uses hardware binary64 for any other point; the final product by 0.2 is
-// a hardware binary64 multiply.  Both paths give the IEEE result bit for bit.
+// and uses hardware binary64 for any other point.  The fixed-point points also
+// take the final product by 0.2 on the integer pipes (fx::mul02: the exact
+// integer product of the significands, rounded once to nearest even), so they
+// leave the binary64 pipe to the hardware warps.  Both paths give the IEEE
+// result bit for bit.
 #include "jacobi_core.cuh"
 
 namespace npbgb {
@@ -21,6 +24,7 @@ namespace npbgb {
 extern int64_t g_cfg_f64_emulation;
 extern int64_t g_cfg_jacobi_chunk;
 extern int64_t g_cfg_jacobi_hw_warps;
+extern int64_t g_cfg_jacobi_fx_mul;
 
 template <typename T>
 int32_t jacobi2d_bands_run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st);
@@ -33,7 +37,7 @@ constexpr int kUnroll = 4;
 // Grid: x over groups of kWarps column strips, y over chunks of rows.  With
 // FX, warps below hw_warps take the hardware binary64 path so that the
 // binary64 pipe works next to the integer pipe (same results either way).
-template <typename T, bool FX, bool MAD>
+template <typename T, bool FX, bool MAD, bool IMUL>
 __global__ void __launch_bounds__(32 * kWarps)
 jacobi2d_strip(const T* __restrict__ src, T* __restrict__ dst, int64_t ny, int64_t nx, int chunk,
                int hw_warps, uint32_t one) {
@@ -48,7 +52,7 @@ jacobi2d_strip(const T* __restrict__ src, T* __restrict__ dst, int64_t ny, int64
   if (FX && warp < hw_warps)
     jcore::strip_rows<T, false, false, 1>(src, dst, nx, k0, ib, ie, one);
   else
-    jcore::strip_rows<T, FX, false, FX ? 1 : kUnroll, MAD>(src, dst, nx, k0, ib, ie, one);
+    jcore::strip_rows<T, FX, false, FX ? 1 : kUnroll, MAD, IMUL>(src, dst, nx, k0, ib, ie, one);
 }
 
 int pick_chunk(int64_t ny, int64_t col_blocks) {
@@ -78,9 +82,12 @@ int32_t run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st)
   const dim3 grid{unsigned(gx), unsigned(gy)};
   const int hw = jacobi_hw_warps();
   const dim3 block{32u * kWarps};
-  // Fixed-point additions as multiply-adds below 2^21 cells (see Strip).
-  auto kern = (FX && ny * nx < (int64_t(1) << 21)) ? jacobi2d_strip<T, FX, true>
-                                                   : jacobi2d_strip<T, FX, false>;
+  // Fixed-point additions as multiply-adds below 2^21 cells (see Strip);
+  // the product by 0.2 on the integer pipes unless NPBGB_CFG_JACOBI_FX_MUL = 0.
+  const bool mad = FX && ny * nx < (int64_t(1) << 21);
+  const bool imul = g_cfg_jacobi_fx_mul != 0;
+  auto kern = mad ? (imul ? jacobi2d_strip<T, FX, true, true> : jacobi2d_strip<T, FX, true, false>)
+                  : (imul ? jacobi2d_strip<T, FX, false, true> : jacobi2d_strip<T, FX, false, false>);
   cudaError_t e = cudaSuccess;
   for (int32_t t = 1; t < tsteps && e == cudaSuccess; ++t) {
     e = launch_chained(kern, grid, block, 0, st, a, b, ny, nx, chunk, hw, 1u);

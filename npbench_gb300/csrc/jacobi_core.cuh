@@ -44,7 +44,10 @@ __device__ __forceinline__ void st(T* p, T v) {
 // fx::round53m) on the FMA pipe, else as plain integer additions.  Measured on
 // GB300: multiply-adds 0.5% faster for a 1000^2 grid, plain additions 3.5%
 // faster at 4096^2 and 2.2% for the 4096-grid batch.
-template <typename T, bool FX, bool CG, bool MAD = false>
+// IMUL: the fixed-point points' product by 0.2 on the integer pipes
+// (fx::mul02, exact product and one rounding), else a hardware binary64
+// multiply; the binary64 pipe is the scarcer one on GB300.
+template <typename T, bool FX, bool CG, bool MAD = false, bool IMUL = true>
 struct Strip {
   using S = typename std::conditional<FX, int64_t, T>::type;
   const T* src;
@@ -95,7 +98,8 @@ struct Strip {
         acc = radd(acc, e);
         acc = radd(acc, xn);
         acc = radd(acc, xp);
-        out = mul_rn(k02, fx::to_f64<59>(acc));
+        if constexpr (IMUL) out = fx::mul02<59>(acc);
+        else out = mul_rn(k02, fx::to_f64<59>(acc));
       } else {
         out = T(0);
         if (active) {
@@ -122,8 +126,8 @@ struct Strip {
 // the column (x0..x3) and the halo values of rows i and i+1 (h1, h2).  The
 // five operators run as packed f32x2 instructions (two IEEE round-to-nearest
 // operations each), so both results are bit-identical to Strip::point.
-template <bool CG, bool MAD>
-__device__ __forceinline__ void points2_f32(const Strip<float, false, CG, MAD>& sp, int64_t i, float x0,
+template <bool CG, bool MAD, bool IMUL>
+__device__ __forceinline__ void points2_f32(const Strip<float, false, CG, MAD, IMUL>& sp, int64_t i, float x0,
                                             float x1, float x2, float x3, float h1, float h2) {
   const int lane = threadIdx.x & 31;
   float w1 = __shfl_up_sync(0xffffffffu, x1, 1), e1 = __shfl_down_sync(0xffffffffu, x1, 1);
@@ -142,10 +146,10 @@ __device__ __forceinline__ void points2_f32(const Strip<float, false, CG, MAD>& 
 }
 
 // One strip (columns k0 .. k0+31) over rows [r0, r1).  Warp-collective.
-template <typename T, bool FX, bool CG, int U, bool MAD = false>
+template <typename T, bool FX, bool CG, int U, bool MAD = false, bool IMUL = true>
 __device__ __forceinline__ void strip_rows(const T* src, T* dst, int64_t nx, int64_t k0, int64_t r0,
                                            int64_t r1, uint32_t one) {
-  using St = Strip<T, FX, CG, MAD>;
+  using St = Strip<T, FX, CG, MAD, IMUL>;
   using S = typename St::S;
   const St s(src, dst, nx, k0, one);
   S x[U + 2], h[U + 2];
@@ -160,7 +164,7 @@ __device__ __forceinline__ void strip_rows(const T* src, T* dst, int64_t nx, int
     if constexpr (!FX && std::is_same<T, float>::value && U % 2 == 0) {
 #pragma unroll
       for (int u = 0; u < U; u += 2)
-        points2_f32<CG, MAD>(s, i + u, x[u], x[u + 1], x[u + 2], x[u + 3], h[u + 1], h[u + 2]);
+        points2_f32<CG, MAD, IMUL>(s, i + u, x[u], x[u + 1], x[u + 2], x[u + 3], h[u + 1], h[u + 2]);
     } else {
 #pragma unroll
       for (int u = 0; u < U; ++u) s.point(i + u, x[u], x[u + 1], x[u + 2], h[u + 1]);

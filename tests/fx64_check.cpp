@@ -86,7 +86,7 @@ int main(int argc, char** argv) {
     if (bits(to_f64_cvt<62>(W)) != bits(want)) return fail("heat cvt", v[0], v[1], want, to_f64_cvt<62>(W));
     ++checks;
   }
-  // Jacobi-2D sum (the 0.2 product stays a hardware multiply).
+  // Jacobi-2D update: the fixed-point sum and its product by 0.2 on integers.
   for (long it = 0; it < n / 2; ++it) {
     double v[5];
     int64_t X[5];
@@ -99,8 +99,37 @@ int main(int argc, char** argv) {
     const int64_t S = round53(round53(round53(round53(X[0] + X[1]) + X[2]) + X[3]) + X[4]);
     const double got = to_f64<59>(S);
     if (bits(got) != bits(want)) return fail("jacobi", v[0], v[1], want, got);
+    volatile double want02 = 0.2 * want;
+    if (bits(mul02<59>(S)) != bits(want02)) return fail("jacobi 0.2", v[0], v[1], want02, mul02<59>(S));
+    checks += 2;
+  }
+  // The product by 0.2 on frame-59 integers m * 2^k (m odd, 1 to 53 bits) over the
+  // whole range a sum of five inputs in [2^-7, 1) can take, [2^52, 5 * 2^59):
+  // small m give the exact ties (m * 0x1999999999999A with 54 significant bits).
+  for (long it = 0; it < n; ++it) {
+    const int bitsm = 1 + static_cast<int>(rng() % 53);
+    uint64_t m = (rng() >> (64 - bitsm)) | 1u | (uint64_t(1) << (bitsm - 1));
+    const int lo_k = 52 - (bitsm - 1) > 0 ? 52 - (bitsm - 1) : 0;
+    const int hi_k = 61 - (bitsm - 1);
+    if (hi_k < lo_k) continue;
+    const int k = lo_k + static_cast<int>(rng() % static_cast<uint64_t>(hi_k - lo_k + 1));
+    const int64_t W = static_cast<int64_t>(m << k);
+    if (W < (int64_t(1) << 52) || W >= 5 * (int64_t(1) << 59)) continue;
+    volatile double x = to_f64<59>(W);
+    volatile double want02 = 0.2 * x;
+    if (bits(mul02<59>(W)) != bits(want02)) return fail("0.2 product", x, 0.2, want02, mul02<59>(W));
     ++checks;
   }
+  if (bits(mul02<59>(0)) != bits(0.0)) return fail("0.2 product of +0", 0.0, 0.2, 0.0, mul02<59>(0));
+  for (int e = 52; e < 62; ++e)  // ties: 3 * 2^k
+    for (uint64_t m : {1ull, 3ull, 5ull, 7ull, 9ull, 15ull, 17ull, 255ull, 257ull}) {
+      if ((m << e) >= 5 * (uint64_t(1) << 59) || (m << e) < (uint64_t(1) << 52)) continue;
+      const int64_t W = static_cast<int64_t>(m << e);
+      volatile double x = to_f64<59>(W);
+      volatile double want02 = 0.2 * x;
+      if (bits(mul02<59>(W)) != bits(want02)) return fail("0.2 tie", x, 0.2, want02, mul02<59>(W));
+      ++checks;
+    }
   // Values the fast path must refuse.
   const double refuse[] = {-0.0, -0.5, 1.0, 1.5, 0x1p-8, 0x1p-1030, 1e300, __builtin_inf(),
                            __builtin_nan("")};
