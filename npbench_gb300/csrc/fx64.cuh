@@ -91,6 +91,18 @@ NPBGB_FX_FN int64_t round53(int64_t x) {
   return static_cast<int64_t>((static_cast<uint64_t>(x) + add) & ~static_cast<uint64_t>(mask));
 }
 
+// round53 for 0 <= x < 2^63: the leading bit comes from hi | 2^20 directly
+// (a non-negative value needs no sign fold, and the OR keeps the shift >= 0
+// for x < 2^53, which is exact already).
+NPBGB_FX_FN int64_t round53p(int64_t x) {
+  const uint32_t hi = static_cast<uint32_t>(static_cast<uint64_t>(x) >> 32);
+  const int sh = 11 - clz32(hi | 0x100000u);  // (31 - clz) - 20, 0..11
+  const uint32_t mask = (1u << sh) - 1u;
+  const uint32_t lo = static_cast<uint32_t>(x);
+  const uint32_t add = ((mask >> 1) + ((lo >> sh) & 1u)) & mask;
+  return static_cast<int64_t>((static_cast<uint64_t>(x) + add) & ~static_cast<uint64_t>(mask));
+}
+
 // x -> frame-59 integer for x == +0.0 or x in [2^-7, 1).  Sets ok = false for
 // anything else (negative, -0.0, >= 1, < 2^-7, subnormal, inf, nan); the
 // returned value is then meaningless.

@@ -99,6 +99,8 @@ int main(int argc, char** argv) {
     const int64_t S = round53(round53(round53(round53(X[0] + X[1]) + X[2]) + X[3]) + X[4]);
     const double got = to_f64<59>(S);
     if (bits(got) != bits(want)) return fail("jacobi", v[0], v[1], want, got);
+    const int64_t Sp = round53p(round53p(round53p(round53p(X[0] + X[1]) + X[2]) + X[3]) + X[4]);
+    if (Sp != S) return fail("jacobi round53p", v[0], v[1], want, to_f64<59>(Sp));
     volatile double want02 = 0.2 * want;
     if (bits(mul02<59>(S)) != bits(want02)) return fail("jacobi 0.2", v[0], v[1], want02, mul02<59>(S));
     checks += 2;
@@ -118,6 +120,14 @@ int main(int argc, char** argv) {
     volatile double x = to_f64<59>(W);
     volatile double want02 = 0.2 * x;
     if (bits(mul02<59>(W)) != bits(want02)) return fail("0.2 product", x, 0.2, want02, mul02<59>(W));
+    ++checks;
+  }
+  // round53p against round53 on non-negative integers of every length.
+  for (long it = 0; it < n; ++it) {
+    const int len = static_cast<int>(rng() % 63);
+    const int64_t x = static_cast<int64_t>(rng() >> (63 - len)) & ((int64_t(1) << 62) | ((int64_t(1) << 62) - 1));
+    if (x < 0) continue;
+    if (round53p(x) != round53(x)) return fail("round53p", 0, 0, 0, 0);
     ++checks;
   }
   if (bits(mul02<59>(0)) != bits(0.0)) return fail("0.2 product of +0", 0.0, 0.2, 0.0, mul02<59>(0));
