@@ -125,10 +125,12 @@ extern "C" {
                                           tile of a half-sweep and runs on to the next
                                           ones, up to 256, before returning the grid
                                           to the ring); 0 = never; default 65536 */
-#define NPBGB_CFG_JACOBI_FX_MUL 24    /* jacobi2d single-grid kernel, binary64: 1
-                                         (default) the fixed-point points' product by
-                                         0.2 on the integer pipes, 0 a hardware
-                                         binary64 multiply.  Results are identical. */
+#define NPBGB_CFG_JACOBI_FX_MUL 24    /* jacobi2d single-grid kernel, binary64: the
+                                         product by 0.2 on the integer pipes for the
+                                         fixed-point points (1, default), for those and
+                                         the hardware warps' points (2), or a hardware
+                                         binary64 multiply everywhere (0).  Results are
+                                         identical. */
 
 /* Batch forms. */
 #define NPBGB_BATCH_PERSISTENT 1

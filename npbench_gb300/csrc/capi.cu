@@ -189,7 +189,7 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       g_cfg_jacobi_bands = value;
       return NPBGB_OK;
     case NPBGB_CFG_JACOBI_FX_MUL:
-      if (value != 0 && value != 1) return set_error(NPBGB_ERR_ARG, "jacobi fx mul: 0 or 1");
+      if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "jacobi fx mul: 0, 1 or 2");
       g_cfg_jacobi_fx_mul = value;
       return NPBGB_OK;
     case NPBGB_CFG_QUEUE_WHOLE_CELLS:

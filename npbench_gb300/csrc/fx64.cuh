@@ -248,5 +248,35 @@ NPBGB_FX_FN double mul02(int64_t w) {
   return w == 0 ? 0.0 : double_of(bits);
 }
 
+// RN(0.2 * x) for a binary64 x, on the integer pipes when x is normal with a
+// biased exponent in [24, 2000] (then the product is normal too): the 53-bit
+// significand times M (106 bits) rounded once to nearest even, as mul02 does;
+// any other x (zeros, subnormals, huge, infinite, NaN) takes the hardware
+// multiply.
+NPBGB_FX_FN double mul02_any(double x) {
+  constexpr uint64_t M = 0x1999999999999Aull;
+  const uint64_t b = bits_of(x);
+  const uint32_t e = static_cast<uint32_t>(b >> 52) & 0x7ffu;
+  if (e - 24u > 2000u - 24u) return 0.2 * x;
+  const uint64_t sig = (b & 0xfffffffffffffull) | 0x10000000000000ull;
+#if defined(__CUDA_ARCH__)
+  const uint64_t lo = sig * M;
+  const uint64_t hi = __umul64hi(sig, M);
+#else
+  const unsigned __int128 p = static_cast<unsigned __int128>(sig) * M;
+  const uint64_t lo = static_cast<uint64_t>(p);
+  const uint64_t hi = static_cast<uint64_t>(p >> 64);
+#endif
+  const int sh = (128 - clz64(hi)) - 53;          // 52 or 53
+  uint64_t s = (hi << (64 - sh)) | (lo >> sh);
+  const uint64_t below = lo & ((uint64_t(1) << (sh - 1)) - 1);
+  const uint64_t half = (lo >> (sh - 1)) & 1;
+  s += half & static_cast<uint64_t>((below != 0) | (s & 1));
+  // x = sig * 2^(e - 1075), 0.2 = M * 2^-55: the product is s * 2^(sh + e - 1130)
+  const uint64_t mag = (static_cast<uint64_t>(sh + static_cast<int>(e) - 55) << 52) +
+                       (s - (uint64_t(1) << 52));
+  return double_of(mag | (b & 0x8000000000000000ull));
+}
+
 }  // namespace fx
 }  // namespace npbgb

@@ -46,8 +46,10 @@ __device__ __forceinline__ void st(T* p, T v) {
 // faster at 4096^2 and 2.2% for the 4096-grid batch.
 // IMUL: the fixed-point points' product by 0.2 on the integer pipes
 // (fx::mul02, exact product and one rounding), else a hardware binary64
-// multiply; the binary64 pipe is the scarcer one on GB300.
-template <typename T, bool FX, bool CG, bool MAD = false, bool IMUL = true>
+// multiply; the binary64 pipe is the scarcer one on GB300.  HWIMUL: the same
+// for the hardware binary64 path (fx::mul02_any), used by the hardware warps
+// that work next to fixed-point warps.
+template <typename T, bool FX, bool CG, bool MAD = false, bool IMUL = true, bool HWIMUL = false>
 struct Strip {
   using S = typename std::conditional<FX, int64_t, T>::type;
   const T* src;
@@ -116,7 +118,8 @@ struct Strip {
       acc = add_rn(acc, e);
       acc = add_rn(acc, xn);
       acc = add_rn(acc, xp);
-      out = mul_rn(k02, acc);
+      if constexpr (HWIMUL && std::is_same<T, double>::value) out = fx::mul02_any(acc);
+      else out = mul_rn(k02, acc);
     }
     if (active) st<CG>(dst + i * nx + j, out);
   }
@@ -126,8 +129,8 @@ struct Strip {
 // the column (x0..x3) and the halo values of rows i and i+1 (h1, h2).  The
 // five operators run as packed f32x2 instructions (two IEEE round-to-nearest
 // operations each), so both results are bit-identical to Strip::point.
-template <bool CG, bool MAD, bool IMUL>
-__device__ __forceinline__ void points2_f32(const Strip<float, false, CG, MAD, IMUL>& sp, int64_t i, float x0,
+template <bool CG, bool MAD, bool IMUL, bool HWIMUL>
+__device__ __forceinline__ void points2_f32(const Strip<float, false, CG, MAD, IMUL, HWIMUL>& sp, int64_t i, float x0,
                                             float x1, float x2, float x3, float h1, float h2) {
   const int lane = threadIdx.x & 31;
   float w1 = __shfl_up_sync(0xffffffffu, x1, 1), e1 = __shfl_down_sync(0xffffffffu, x1, 1);
@@ -146,10 +149,10 @@ __device__ __forceinline__ void points2_f32(const Strip<float, false, CG, MAD, I
 }
 
 // One strip (columns k0 .. k0+31) over rows [r0, r1).  Warp-collective.
-template <typename T, bool FX, bool CG, int U, bool MAD = false, bool IMUL = true>
+template <typename T, bool FX, bool CG, int U, bool MAD = false, bool IMUL = true, bool HWIMUL = false>
 __device__ __forceinline__ void strip_rows(const T* src, T* dst, int64_t nx, int64_t k0, int64_t r0,
                                            int64_t r1, uint32_t one) {
-  using St = Strip<T, FX, CG, MAD, IMUL>;
+  using St = Strip<T, FX, CG, MAD, IMUL, HWIMUL>;
   using S = typename St::S;
   const St s(src, dst, nx, k0, one);
   S x[U + 2], h[U + 2];
@@ -164,7 +167,7 @@ __device__ __forceinline__ void strip_rows(const T* src, T* dst, int64_t nx, int
     if constexpr (!FX && std::is_same<T, float>::value && U % 2 == 0) {
 #pragma unroll
       for (int u = 0; u < U; u += 2)
-        points2_f32<CG, MAD, IMUL>(s, i + u, x[u], x[u + 1], x[u + 2], x[u + 3], h[u + 1], h[u + 2]);
+        points2_f32<CG, MAD, IMUL, HWIMUL>(s, i + u, x[u], x[u + 1], x[u + 2], x[u + 3], h[u + 1], h[u + 2]);
     } else {
 #pragma unroll
       for (int u = 0; u < U; ++u) s.point(i + u, x[u], x[u + 1], x[u + 2], h[u + 1]);

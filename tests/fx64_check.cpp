@@ -130,6 +130,32 @@ int main(int argc, char** argv) {
     if (round53p(x) != round53(x)) return fail("round53p", 0, 0, 0, 0);
     ++checks;
   }
+  // mul02_any against the CPU's 0.2 * x over every exponent, both signs, and
+  // the special values.
+  for (long it = 0; it < n; ++it) {
+    const uint64_t b = rng();
+    volatile double x = double_of(b);
+    volatile double want = 0.2 * x;
+    const double got = mul02_any(x);
+    if (!(want != want && got != got) && bits(got) != bits(want)) return fail("mul02_any", x, 0.2, want, got);
+    ++checks;
+  }
+  for (long it = 0; it < n; ++it) {  // significands with few bits: the ties
+    const int bitsm = 1 + static_cast<int>(rng() % 8);
+    const uint64_t m = (rng() >> (64 - bitsm)) | 1u | (uint64_t(1) << (bitsm - 1));
+    const uint64_t e = 1 + rng() % 2046;
+    const uint64_t frac = (m << (53 - bitsm)) & 0xfffffffffffffull;
+    volatile double x = double_of((e << 52) | frac | ((rng() & 1) << 63));
+    volatile double want = 0.2 * x;
+    if (bits(mul02_any(x)) != bits(want)) return fail("mul02_any tie", x, 0.2, want, mul02_any(x));
+    ++checks;
+  }
+  for (double x : {0.0, -0.0, 0x1p-1074, -0x1p-1074, 0x1p-1022, 0x1.fffffffffffffp+1023,
+                   __builtin_inf(), -__builtin_inf(), 1.0, 0.375, 5.0, 4.999999999999999}) {
+    volatile double want = 0.2 * x;
+    if (bits(mul02_any(x)) != bits(want)) return fail("mul02_any special", x, 0.2, want, mul02_any(x));
+    ++checks;
+  }
   if (bits(mul02<59>(0)) != bits(0.0)) return fail("0.2 product of +0", 0.0, 0.2, 0.0, mul02<59>(0));
   for (int e = 52; e < 62; ++e)  // ties: 3 * 2^k
     for (uint64_t m : {1ull, 3ull, 5ull, 7ull, 9ull, 15ull, 17ull, 255ull, 257ull}) {
