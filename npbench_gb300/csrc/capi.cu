@@ -34,6 +34,7 @@ int64_t g_cfg_heat_stages = 0;         // 0: automatic (8)
 int64_t g_cfg_heat_mad_rows = 0;
 int64_t g_cfg_queue_whole_cells = 65536;
 int64_t g_cfg_jacobi_fx_mul = 1;
+int64_t g_cfg_jacobi_fx_adds = 0;
 
 namespace {
 std::atomic<int64_t> g_launches{0};
@@ -188,6 +189,10 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "jacobi bands: 0, 1 or 2");
       g_cfg_jacobi_bands = value;
       return NPBGB_OK;
+    case NPBGB_CFG_JACOBI_FX_ADDS:
+      if (value < 0 || value > 3) return set_error(NPBGB_ERR_ARG, "jacobi fx adds: 0 .. 3");
+      g_cfg_jacobi_fx_adds = value;
+      return NPBGB_OK;
     case NPBGB_CFG_JACOBI_FX_MUL:
       if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "jacobi fx mul: 0, 1 or 2");
       g_cfg_jacobi_fx_mul = value;
@@ -248,6 +253,7 @@ int32_t npbgb_get_config(int32_t key, int64_t* value) {
     case NPBGB_CFG_JACOBI_BANDS: *value = g_cfg_jacobi_bands; return NPBGB_OK;
     case NPBGB_CFG_JACOBI_BANDS_WARPS: *value = g_cfg_jacobi_bands_warps; return NPBGB_OK;
     case NPBGB_CFG_HEAT_STAGES: *value = g_cfg_heat_stages; return NPBGB_OK;
+    case NPBGB_CFG_JACOBI_FX_ADDS: *value = g_cfg_jacobi_fx_adds; return NPBGB_OK;
     case NPBGB_CFG_JACOBI_FX_MUL: *value = g_cfg_jacobi_fx_mul; return NPBGB_OK;
     case NPBGB_CFG_QUEUE_WHOLE_CELLS: *value = g_cfg_queue_whole_cells; return NPBGB_OK;
     case NPBGB_CFG_HEAT_MAD_ROWS: *value = g_cfg_heat_mad_rows; return NPBGB_OK;

@@ -172,6 +172,34 @@ NPBGB_FX_FN int64_t round53m(int64_t x, uint32_t one) {
   return static_cast<int64_t>(r & ~static_cast<uint64_t>(mask));
 }
 
+// round53p with its additions issued as multiply-adds (the multiplier `one`
+// == 1 at run time), so that four of its twelve instructions run on the
+// multiply-add pipe instead of the integer ALU: 11 - clz, pow - 1, the sum of
+// the rounding increment, and the 64-bit add of it (one wide multiply-add).
+// For 0 <= x < 2^63.
+NPBGB_FX_FN int64_t round53q(int64_t x, uint32_t one) {
+  const uint32_t hi = static_cast<uint32_t>(static_cast<uint64_t>(x) >> 32);
+  const uint32_t lo = static_cast<uint32_t>(x);
+  const uint32_t c = static_cast<uint32_t>(clz32(hi | 0x100000u));  // 9..11 -> sh 0..11
+#if defined(__CUDA_ARCH__)
+  uint32_t sh, mask, add;
+  uint64_t r;
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(sh) : "r"(c), "r"(0u - one), "r"(11u));
+  const uint32_t pow = 1u << sh;
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(mask) : "r"(pow), "r"(one), "r"(0xffffffffu));
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(add) : "r"((lo >> sh) & 1u), "r"(one), "r"(mask >> 1));
+  add &= mask;
+  asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(r) : "r"(add), "r"(one), "l"(x));
+#else
+  (void)one;
+  const uint32_t sh = 11u - c;
+  const uint32_t mask = (1u << sh) - 1u;
+  const uint32_t add = ((mask >> 1) + ((lo >> sh) & 1u)) & mask;
+  const uint64_t r = static_cast<uint64_t>(x) + add;
+#endif
+  return static_cast<int64_t>(r & ~static_cast<uint64_t>(mask));
+}
+
 // x -> frame-59 integer using the binary64 conversion path instead of integer
 // bit manipulation: x * 2^59 (an exponent change, exact for accepted x) is
 // converted with round-toward-zero, which is exact because the scaled value is

@@ -25,6 +25,7 @@ extern int64_t g_cfg_f64_emulation;
 extern int64_t g_cfg_jacobi_chunk;
 extern int64_t g_cfg_jacobi_hw_warps;
 extern int64_t g_cfg_jacobi_fx_mul;
+extern int64_t g_cfg_jacobi_fx_adds;
 
 template <typename T>
 int32_t jacobi2d_bands_run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st);
@@ -37,7 +38,7 @@ constexpr int kUnroll = 4;
 // Grid: x over groups of kWarps column strips, y over chunks of rows.  With
 // FX, warps below hw_warps take the hardware binary64 path so that the
 // binary64 pipe works next to the integer pipe (same results either way).
-template <typename T, bool FX, bool MAD, bool IMUL, bool HWIMUL>
+template <typename T, bool FX, int MAD, bool IMUL, bool HWIMUL>
 __global__ void __launch_bounds__(32 * kWarps)
 jacobi2d_strip(const T* __restrict__ src, T* __restrict__ dst, int64_t ny, int64_t nx, int chunk,
                int hw_warps, uint32_t one) {
@@ -50,7 +51,7 @@ jacobi2d_strip(const T* __restrict__ src, T* __restrict__ dst, int64_t ny, int64
   // Rows loaded ahead: 4 for binary32; 1 for binary64, whose chunks are short
   // (2 ahead measured 5-10% slower at 500^2 to 4096^2 with 4 hardware warps).
   if (FX && warp < hw_warps)
-    jcore::strip_rows<T, false, false, 1, false, true, HWIMUL>(src, dst, nx, k0, ib, ie, one);
+    jcore::strip_rows<T, false, false, 1, 0, true, HWIMUL>(src, dst, nx, k0, ib, ie, one);
   else
     jcore::strip_rows<T, FX, false, FX ? 1 : kUnroll, MAD, IMUL>(src, dst, nx, k0, ib, ie, one);
 }
@@ -82,16 +83,24 @@ int32_t run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st)
   const dim3 grid{unsigned(gx), unsigned(gy)};
   const int hw = jacobi_hw_warps();
   const dim3 block{32u * kWarps};
-  // Fixed-point additions as multiply-adds below 2^21 cells (see Strip);
-  // the product by 0.2 on the integer pipes unless NPBGB_CFG_JACOBI_FX_MUL = 0.
-  const bool mad = FX && ny * nx < (int64_t(1) << 21);
+  // Fixed-point additions as multiply-adds below 2^21 cells (see Strip) unless
+  // NPBGB_CFG_JACOBI_FX_ADDS says otherwise; the product by 0.2 on the integer
+  // pipes unless NPBGB_CFG_JACOBI_FX_MUL = 0.
+  const int mad = !FX ? 0
+                  : g_cfg_jacobi_fx_adds > 0 ? int(g_cfg_jacobi_fx_adds) - 1
+                  : (ny * nx < (int64_t(1) << 21) ? 1 : 0);
   const int64_t im = g_cfg_jacobi_fx_mul;
-  auto kern = mad ? (im == 0 ? jacobi2d_strip<T, FX, true, false, false>
-                             : im == 1 ? jacobi2d_strip<T, FX, true, true, false>
-                                       : jacobi2d_strip<T, FX, true, true, true>)
-                  : (im == 0 ? jacobi2d_strip<T, FX, false, false, false>
-                             : im == 1 ? jacobi2d_strip<T, FX, false, true, false>
-                                       : jacobi2d_strip<T, FX, false, true, true>);
+  using Kern = void (*)(const T*, T*, int64_t, int64_t, int, int, uint32_t);
+  Kern kern;
+  if (mad == 2)
+    kern = im == 0 ? jacobi2d_strip<T, FX, 2, false, false>
+         : im == 1 ? jacobi2d_strip<T, FX, 2, true, false> : jacobi2d_strip<T, FX, 2, true, true>;
+  else if (mad == 1)
+    kern = im == 0 ? jacobi2d_strip<T, FX, 1, false, false>
+         : im == 1 ? jacobi2d_strip<T, FX, 1, true, false> : jacobi2d_strip<T, FX, 1, true, true>;
+  else
+    kern = im == 0 ? jacobi2d_strip<T, FX, 0, false, false>
+         : im == 1 ? jacobi2d_strip<T, FX, 0, true, false> : jacobi2d_strip<T, FX, 0, true, true>;
   cudaError_t e = cudaSuccess;
   for (int32_t t = 1; t < tsteps && e == cudaSuccess; ++t) {
     e = launch_chained(kern, grid, block, 0, st, a, b, ny, nx, chunk, hw, 1u);

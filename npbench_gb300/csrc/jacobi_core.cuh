@@ -40,16 +40,17 @@ __device__ __forceinline__ void st(T* p, T v) {
   if constexpr (CG) __stcg(p, v); else *p = v;
 }
 
-// MAD: the fixed-point additions are issued as multiply-adds (fx::add64,
-// fx::round53m) on the FMA pipe, else as plain integer additions.  Measured on
-// GB300: multiply-adds 0.5% faster for a 1000^2 grid, plain additions 3.5%
-// faster at 4096^2 and 2.2% for the 4096-grid batch.
+// MAD: 1, the fixed-point additions are issued as multiply-adds (fx::add64,
+// fx::round53m) on the FMA pipe; 2, the same with more of the rounding on it
+// (fx::round53q); 0, plain integer additions.  Measured on GB300: multiply-adds
+// 0.5% faster for a 1000^2 grid, plain additions 3.5% faster at 4096^2 and
+// 2.2% for the 4096-grid batch.
 // IMUL: the fixed-point points' product by 0.2 on the integer pipes
 // (fx::mul02, exact product and one rounding), else a hardware binary64
 // multiply; the binary64 pipe is the scarcer one on GB300.  HWIMUL: the same
 // for the hardware binary64 path (fx::mul02_any), used by the hardware warps
 // that work next to fixed-point warps.
-template <typename T, bool FX, bool CG, bool MAD = false, bool IMUL = true, bool HWIMUL = false>
+template <typename T, bool FX, bool CG, int MAD = 0, bool IMUL = true, bool HWIMUL = false>
 struct Strip {
   using S = typename std::conditional<FX, int64_t, T>::type;
   const T* src;
@@ -93,7 +94,8 @@ struct Strip {
       const uint32_t tag = hi32(xc) | hi32(w) | hi32(e) | hi32(xn) | hi32(xp);
       if (!(tag & fx::kPoisonHi)) {
         auto radd = [this](int64_t x, int64_t y) -> int64_t {
-          if constexpr (MAD) return fx::round53m(fx::add64(x, y, one), one);
+          if constexpr (MAD == 2) return fx::round53q(fx::add64(x, y, one), one);
+          else if constexpr (MAD == 1) return fx::round53m(fx::add64(x, y, one), one);
           else return fx::round53p(int64_t(uint64_t(x) + uint64_t(y)));  // sums are >= 0
         };
         int64_t acc = radd(xc, w);
@@ -129,7 +131,7 @@ struct Strip {
 // the column (x0..x3) and the halo values of rows i and i+1 (h1, h2).  The
 // five operators run as packed f32x2 instructions (two IEEE round-to-nearest
 // operations each), so both results are bit-identical to Strip::point.
-template <bool CG, bool MAD, bool IMUL, bool HWIMUL>
+template <bool CG, int MAD, bool IMUL, bool HWIMUL>
 __device__ __forceinline__ void points2_f32(const Strip<float, false, CG, MAD, IMUL, HWIMUL>& sp, int64_t i, float x0,
                                             float x1, float x2, float x3, float h1, float h2) {
   const int lane = threadIdx.x & 31;
@@ -149,7 +151,7 @@ __device__ __forceinline__ void points2_f32(const Strip<float, false, CG, MAD, I
 }
 
 // One strip (columns k0 .. k0+31) over rows [r0, r1).  Warp-collective.
-template <typename T, bool FX, bool CG, int U, bool MAD = false, bool IMUL = true, bool HWIMUL = false>
+template <typename T, bool FX, bool CG, int U, int MAD = 0, bool IMUL = true, bool HWIMUL = false>
 __device__ __forceinline__ void strip_rows(const T* src, T* dst, int64_t nx, int64_t k0, int64_t r0,
                                            int64_t r1, uint32_t one) {
   using St = Strip<T, FX, CG, MAD, IMUL, HWIMUL>;

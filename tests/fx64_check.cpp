@@ -128,6 +128,7 @@ int main(int argc, char** argv) {
     const int64_t x = static_cast<int64_t>(rng() >> (63 - len)) & ((int64_t(1) << 62) | ((int64_t(1) << 62) - 1));
     if (x < 0) continue;
     if (round53p(x) != round53(x)) return fail("round53p", 0, 0, 0, 0);
+    if (round53q(x, 1u) != round53(x)) return fail("round53q", 0, 0, 0, 0);
     ++checks;
   }
   // mul02_any against the CPU's 0.2 * x over every exponent, both signs, and

@@ -750,6 +750,37 @@ def test_jacobi_hw_warp_mix_bit_exact(hw_warps):
         _lib.set_config(_lib.NPBGB_CFG_JACOBI_HW_WARPS, old)
 
 
+@pytest.mark.parametrize("adds,mul", [(1, 0), (2, 1), (3, 1), (3, 2), (1, 2), (0, 2), (2, 0)])
+@pytest.mark.parametrize("hw_warps", [0, 3, 8])
+def test_jacobi_f64_add_and_product_forms_bit_exact(adds, mul, hw_warps):
+    """Binary64 Jacobi-2D with each form of the fixed-point additions (integer adds,
+    multiply-add 64-bit adds, rounding on the multiply-add pipe) and of the product by
+    0.2 (hardware, integer for the fixed-point points, integer for every point), on
+    uniform fields and on fields with negatives, -0.0, tiny, subnormal and >= 1 values."""
+    from npbench_gb300 import _lib, autotune
+    keys = (_lib.NPBGB_CFG_JACOBI_FX_ADDS, _lib.NPBGB_CFG_JACOBI_FX_MUL,
+            _lib.NPBGB_CFG_JACOBI_HW_WARPS)
+    old = [_lib.set_config(k, v) for k, v in zip(keys, (adds, mul, hw_warps))]
+    was = autotune.enabled()
+    autotune.disable()
+    try:
+        for field in ("uniform", "mixed"):
+            for shape in ((200, 1100), (37, 45)):
+                A, B = (workloads.uniform_pair(shape, np.float64, seed=adds + mul)
+                        if field == "uniform"
+                        else (_mixed_range_field(shape, 70 + adds), _mixed_range_field(shape, 80 + mul)))
+                ra, rb = A.copy(), B.copy()
+                cref.jacobi_2d_kernel(6, ra, rb)
+                dA, dB = _dev(A), _dev(B)
+                stencils.jacobi_2d_kernel(6, dA, dB)
+                assert bits_equal(_host(dA), ra) and bits_equal(_host(dB), rb), (field, shape)
+    finally:
+        for k, v in zip(keys, old):
+            _lib.set_config(k, v)
+        if was:
+            autotune.enable()
+
+
 @pytest.mark.parametrize("bench,shape,tsteps", [("jacobi_2d", (1000, 1000), 10),
                                                 ("jacobi_2d", (1000, 1000), 100),
                                                 ("heat_3d", (256, 256, 256), 10),
