@@ -132,9 +132,9 @@ extern "C" {
                                          binary64 multiply everywhere (0).  Results are
                                          identical. */
 #define NPBGB_CFG_JACOBI_FX_ADDS 25   /* jacobi2d single-grid kernel, binary64 fixed-
-                                         point additions: 0 (default) automatic, 1
-                                         integer adds, 2 multiply-add 64-bit adds, 3
-                                         most of the rounding on the multiply-add pipe.
+                                         point additions: 0 (default) or 1 integer
+                                         adds, 2 multiply-add 64-bit adds, 3 most of
+                                         the rounding on the multiply-add pipe.
                                          Results are identical. */
 
 /* Batch forms. */

@@ -83,12 +83,12 @@ int32_t run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st)
   const dim3 grid{unsigned(gx), unsigned(gy)};
   const int hw = jacobi_hw_warps();
   const dim3 block{32u * kWarps};
-  // Fixed-point additions as multiply-adds below 2^21 cells (see Strip) unless
-  // NPBGB_CFG_JACOBI_FX_ADDS says otherwise; the product by 0.2 on the integer
-  // pipes unless NPBGB_CFG_JACOBI_FX_MUL = 0.
-  const int mad = !FX ? 0
-                  : g_cfg_jacobi_fx_adds > 0 ? int(g_cfg_jacobi_fx_adds) - 1
-                  : (ny * nx < (int64_t(1) << 21) ? 1 : 0);
+  // Fixed-point additions as plain integer adds (with the integer product by
+  // 0.2 they measured fastest at every size: 1000^2 TSTEPS=100 1.83 ms against
+  // 1.94 with multiply-add adds and 2.10 with the rounding on the multiply-add
+  // pipe) unless NPBGB_CFG_JACOBI_FX_ADDS says otherwise; the product by 0.2 on
+  // the integer pipes unless NPBGB_CFG_JACOBI_FX_MUL = 0.
+  const int mad = (FX && g_cfg_jacobi_fx_adds > 0) ? int(g_cfg_jacobi_fx_adds) - 1 : 0;
   const int64_t im = g_cfg_jacobi_fx_mul;
   using Kern = void (*)(const T*, T*, int64_t, int64_t, int, int, uint32_t);
   Kern kern;

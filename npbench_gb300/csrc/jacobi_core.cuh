@@ -42,9 +42,9 @@ __device__ __forceinline__ void st(T* p, T v) {
 
 // MAD: 1, the fixed-point additions are issued as multiply-adds (fx::add64,
 // fx::round53m) on the FMA pipe; 2, the same with more of the rounding on it
-// (fx::round53q); 0, plain integer additions.  Measured on GB300: multiply-adds
-// 0.5% faster for a 1000^2 grid, plain additions 3.5% faster at 4096^2 and
-// 2.2% for the 4096-grid batch.
+// (fx::round53q); 0, plain integer additions, which measured fastest on GB300
+// at every size once the product by 0.2 left the binary64 pipe (1000^2: 1.83
+// ms against 1.94 and 2.10 for 198 half-sweeps; 4096^2 4.33 against 4.66).
 // IMUL: the fixed-point points' product by 0.2 on the integer pipes
 // (fx::mul02, exact product and one rounding), else a hardware binary64
 // multiply; the binary64 pipe is the scarcer one on GB300.  HWIMUL: the same
