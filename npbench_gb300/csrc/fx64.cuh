@@ -75,18 +75,63 @@ NPBGB_FX_FN double double_of(uint64_t b) {
 #endif
 }
 
+// Position of the most significant bit of v that differs from its sign bit
+// (the leading 1 of v >= 0, the leading 0 of v < 0); -1 for v == 0 and v == -1.
+// One instruction on the GPU (PTX bfind.s32).
+NPBGB_FX_FN int msb_nonsign32(uint32_t v) {
+#if defined(__CUDA_ARCH__)
+  int p;
+  asm("bfind.s32 %0, %1;" : "=r"(p) : "r"(v));
+  return p;
+#else
+  const uint32_t h = v ^ static_cast<uint32_t>(static_cast<int32_t>(v) >> 31);
+  return 31 - clz32(h);
+#endif
+}
+
+// v >> s for a shift amount s read as unsigned, with amounts of 32 and more
+// giving 0 (PTX shr.b32 clamps the amount to the register width).
+NPBGB_FX_FN uint32_t shr_clamp32(uint32_t v, uint32_t s) {
+#if defined(__CUDA_ARCH__)
+  uint32_t r;
+  asm("shr.b32 %0, %1, %2;" : "=r"(r) : "r"(v), "r"(s));
+  return r;
+#else
+  return s >= 32u ? 0u : v >> s;
+#endif
+}
+
 // Rounds the exact integer x (|x| < 2^63 - 2^11) to 53 significant bits,
 // ties to even.  Works on two's complement directly: for negative x the
 // leading bit of ~x = |x| - 1 is that of |x| unless |x| is a power of two, and
 // then x has no bits below the rounding point anyway.
+//
+// With p the leading non-sign bit of the high word, sh = p - 20 bits (0..11)
+// lie below the 53-bit window.  mask = 2^sh - 1 comes from one clamped shift
+// (0 whenever p <= 20, i.e. |x| < 2^53, which is exact already), and
+// floor((x + mask/2 + lsb) / 2^sh) * 2^sh, lsb = bit sh of x, is
+// round-half-even on two's complement.  The lsb is taken as
+// (lo >> sh) & mask & 1, so that it is 0 when nothing is rounded (mask = 0).
 NPBGB_FX_FN int64_t round53(int64_t x) {
+  const uint32_t hi = static_cast<uint32_t>(static_cast<uint64_t>(x) >> 32);
+  const uint32_t lo = static_cast<uint32_t>(x);
+  const int p = msb_nonsign32(hi);
+  const uint32_t mask = shr_clamp32(0xffffffffu, static_cast<uint32_t>(52 - p));
+  const uint32_t lsb = shr_clamp32(lo, static_cast<uint32_t>(p - 20)) & mask & 1u;
+  const uint64_t r = static_cast<uint64_t>(x) + ((mask >> 1) + lsb);
+  return static_cast<int64_t>(r & ~static_cast<uint64_t>(mask));
+}
+
+// The former form of round53: sign fold, count of leading zeros, shift
+// clamped at zero, increment masked.  Kept as a second statement of the same
+// rounding for the host check.
+NPBGB_FX_FN int64_t round53_fold(int64_t x) {
   const int32_t hi = static_cast<int32_t>(x >> 32);
   const uint32_t h = static_cast<uint32_t>(hi ^ (hi >> 31));
   int sh = (31 - clz32(h)) - 20;  // bits below the 53-bit window
   sh = sh < 0 ? 0 : sh;           // 0..11, all within the low word
   const uint32_t mask = (1u << sh) - 1u;
   const uint32_t lo = static_cast<uint32_t>(x);
-  // floor((x + half - 1 + lsb) / 2^sh) * 2^sh is round-half-even on two's complement
   const uint32_t add = ((mask >> 1) + ((lo >> sh) & 1u)) & mask;
   return static_cast<int64_t>((static_cast<uint64_t>(x) + add) & ~static_cast<uint64_t>(mask));
 }
@@ -243,6 +288,42 @@ NPBGB_FX_FN double to_f64(int64_t w) {
   return m == 0 ? 0.0 : double_of(bits | sign);
 }
 
+// to_f64<F>(round53(x)) in one step, for an exact integer x with
+// |x| < 2^63 - 2^11: the IEEE double nearest x * 2^-F (ties to even).
+//
+// For 2^52 <= x < 2^63 (the common case of a non-negative sum) the rounding
+// and the conversion share their work: with p the leading bit of the high word
+// (20..30), sh = p - 20 bits lie below the 53-bit window, and
+// sig = (x + 2^(sh-1) - 1 + lsb) >> sh is the rounded significand, 2^52 <= sig
+// <= 2^53.  value = sig * 2^(sh - F), so its bits are sig plus the biased
+// exponent minus one, (sh + 1074 - F), shifted to bit 52; a carry out of the
+// rounding (sig == 2^53) moves into the exponent field by itself.  Other x
+// (smaller, negative) take round53 and to_f64.
+template <int F>
+NPBGB_FX_FN double round_to_f64(int64_t x) {
+  const uint32_t hi = static_cast<uint32_t>(static_cast<uint64_t>(x) >> 32);
+  if (hi - 0x100000u >= 0x7ff00000u) return to_f64<F>(round53(x));  // x < 2^52 or x < 0
+  const uint32_t lo = static_cast<uint32_t>(x);
+  const int p = msb_nonsign32(hi);                    // 20 .. 30
+  const uint32_t sh = static_cast<uint32_t>(p - 20);  // 0 .. 10
+  const uint32_t mask = shr_clamp32(0xffffffffu, static_cast<uint32_t>(52 - p));
+  const uint32_t lsb = (lo >> sh) & mask & 1u;
+  const uint64_t sig = (static_cast<uint64_t>(x) + ((mask >> 1) + lsb)) >> sh;
+  return double_of(sig + (static_cast<uint64_t>(sh + 1074u - F) << 52));
+}
+
+template <int F>
+NPBGB_FX_FN double mul02_wide(int64_t w);
+
+// The high word of (hi:lo) << k, for k < 32 (one funnel shift on the GPU).
+NPBGB_FX_FN uint32_t funnel_left_hi(uint32_t lo, uint32_t hi, uint32_t k) {
+#if defined(__CUDA_ARCH__)
+  return __funnelshift_l(lo, hi, k);
+#else
+  return static_cast<uint32_t>(((static_cast<uint64_t>(hi) << 32 | lo) << k) >> 32);
+#endif
+}
+
 // RN(0.2 * w * 2^-F), the IEEE binary64 product of 0.2 and the frame-F value
 // w, on the integer pipes.  Precondition: w == 0, or 2^12 <= w < 2^62 with at
 // most 53 significant bits (a round53 result) and a normal double result.
@@ -254,8 +335,46 @@ NPBGB_FX_FN double to_f64(int64_t w) {
 // rounding lands in the exponent field by itself.  This is the textbook
 // multiplication of two binary floating-point numbers (exact integer product
 // of the significands, then one rounding), specialised to one constant factor.
+//
+// The product's top 64 bits hi decide the shift.  When 2^32 <= hi < 2^51
+// (every sum of five inputs of [2^-7, 1) that is not 0 is at least 2^52, and
+// then hi >= 2^40) the top 53 bits start in hi's high word, at bit p <= 18 of it, and the
+// work is 32-bit: with k = 20 - p, the significand is hi:lo_hi shifted left by
+// k (two funnel shifts), the discarded bits of lo_hi shifted left by k are the
+// top of the remainder, and the low word of lo only decides whether the
+// remainder is exactly a half.  Rounding up happens exactly when
+// remainder + 2^63 - 1 + lsb carries out of 64 bits; the low word's
+// contribution to that is its being non-zero, folded into the remainder's
+// bit 0, which the shift by k >= 2 leaves free.  mul02_wide is the general
+// form, for small w.
 template <int F>
 NPBGB_FX_FN double mul02(int64_t w) {
+  constexpr uint64_t M = 0x1999999999999Aull;
+  const uint64_t a = static_cast<uint64_t>(w);
+#if defined(__CUDA_ARCH__)
+  const uint64_t lo = a * M;
+  const uint64_t hi = __umul64hi(a, M);
+#else
+  const unsigned __int128 pr = static_cast<unsigned __int128>(a) * M;
+  const uint64_t lo = static_cast<uint64_t>(pr);
+  const uint64_t hi = static_cast<uint64_t>(pr >> 64);
+#endif
+  const uint32_t hh = static_cast<uint32_t>(hi >> 32), hl = static_cast<uint32_t>(hi);
+  const uint32_t lh = static_cast<uint32_t>(lo >> 32), ll = static_cast<uint32_t>(lo);
+  if (hh - 1u >= (1u << 19) - 1u) return mul02_wide<F>(w);   // hi < 2^32, or w too large
+  const int p = msb_nonsign32(hh);                    // 0 .. 18
+  const uint32_t k = static_cast<uint32_t>(20 - p);   // 2 .. 20: sh = 64 - k bits dropped
+  const uint32_t sig_hi = funnel_left_hi(hl, hh, k);
+  const uint32_t sig_lo = funnel_left_hi(lh, hl, k);
+  const uint32_t rem = (lh << k) | (ll != 0u ? 1u : 0u);
+  const uint32_t inc = static_cast<uint32_t>((static_cast<uint64_t>(rem) + 0x7fffffffu + (sig_lo & 1u)) >> 32);
+  // value = sig * 2^(sh - F - 55), sh = p + 44: biased exponent minus one is p + 1063 - F
+  const uint64_t sig = (static_cast<uint64_t>(sig_hi) << 32 | sig_lo) + inc;
+  return double_of(sig + (static_cast<uint64_t>(p + 1063 - F) << 52));
+}
+
+template <int F>
+NPBGB_FX_FN double mul02_wide(int64_t w) {
   constexpr uint64_t M = 0x1999999999999Aull;
   const uint64_t a = static_cast<uint64_t>(w);
 #if defined(__CUDA_ARCH__)

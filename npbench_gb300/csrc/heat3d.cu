@@ -79,6 +79,7 @@ __device__ __forceinline__ double heat_point_fxm(int64_t c, int64_t ip, int64_t 
   const int64_t s2 = rnd(add(rnd(add(kp, nc2)), km));
   const int64_t u = rnd(add(s0, s1));
   const int64_t v = rnd(add(u, s2));
+  if constexpr (!CVT && !MAD) return fx::round_to_f64<62>(add(v, c * 8));
   const int64_t w = rnd(add(v, c * 8));
   if constexpr (CVT) return fx::to_f64_cvt<62>(w);
   return fx::to_f64<62>(w);
@@ -332,12 +333,12 @@ int32_t launch_tma(T* a, T* b, int64_t n0, int64_t n1, int64_t n2, int32_t tstep
   if (gy > 65535 || gz > 65535 || gx > 0x7fffffff)
     return set_error(NPBGB_ERR_ARG, "heat3d: extent too large");
   const dim3 grid{unsigned(gx), unsigned(gy), unsigned(gz)};
-  // Tile rows on the hardware binary64 pipe, measured best at 256^3: 7 of 16
-  // with 2 rows per warp once the hardware rows' exact products by 2 and
-  // 0.125 moved to the integer pipe (30.7 ms per 198 half-sweeps against 31.4
-  // with 6 or 8, and 31.4 for 5 rows with binary64 products); 3 of 8 with 1
-  // row per warp, 8 of 32 with 4.
-  const int hw_default = R == 2 ? 7 : (R == 1 ? 3 : G::TJ / 4);
+  // Tile rows on the hardware binary64 pipe, measured best at 256^3 (40
+  // half-sweeps): 5 of 16 with 2 rows per warp (5.18 ms; 4 rows 5.22, 6 rows
+  // 5.30, 7 rows 5.76) since the fixed-point rounding takes one leading-bit
+  // instruction and clamped shifts; 3 of 8 with 1 row per warp (5.24 ms), 6 of
+  // 32 with 4 (6.15 ms).
+  const int hw_default = R == 2 ? 5 : (R == 1 ? 3 : 6);
   int hw = g_cfg_heat_hw_rows >= 0 ? int(g_cfg_heat_hw_rows) : (FX ? hw_default : 0);
   if (hw > G::TJ) hw = G::TJ;
   // Fixed-point tile rows (the first mad rows) whose 64-bit adds go to the

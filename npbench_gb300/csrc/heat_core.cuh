@@ -79,8 +79,7 @@ __device__ __forceinline__ double heat_point_fx(int64_t c, int64_t ip, int64_t i
   const int64_t s0 = round53(round53(ip - c2) + im);  // 8 * t0 in frame 59 == t0 in frame 62
   const int64_t s1 = round53(round53(jp - c2) + jm);
   const int64_t s2 = round53(round53(kp - c2) + km);
-  const int64_t w = round53(round53(round53(s0 + s1) + s2) + c * 8);
-  return fx::to_f64<62>(w);
+  return fx::round_to_f64<62>(round53(round53(s0 + s1) + s2) + c * 8);
 }
 
 // Evaluates one point from staged values (T for the plain path, frame-59

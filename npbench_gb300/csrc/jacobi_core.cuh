@@ -96,7 +96,7 @@ struct Strip {
         auto radd = [this](int64_t x, int64_t y) -> int64_t {
           if constexpr (MAD == 2) return fx::round53q(fx::add64(x, y, one), one);
           else if constexpr (MAD == 1) return fx::round53m(fx::add64(x, y, one), one);
-          else return fx::round53p(int64_t(uint64_t(x) + uint64_t(y)));  // sums are >= 0
+          else return fx::round53(int64_t(uint64_t(x) + uint64_t(y)));
         };
         int64_t acc = radd(xc, w);
         acc = radd(acc, e);

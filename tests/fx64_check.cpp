@@ -84,6 +84,8 @@ int main(int argc, char** argv) {
     const double got = to_f64<62>(W);
     if (bits(got) != bits(want)) return fail("heat", v[0], v[1], want, got);
     if (bits(to_f64_cvt<62>(W)) != bits(want)) return fail("heat cvt", v[0], v[1], want, to_f64_cvt<62>(W));
+    const double fused = round_to_f64<62>(round53(round53(S0 + S1) + S2) + X[0] * 8);
+    if (bits(fused) != bits(want)) return fail("heat fused rounding", v[0], v[1], want, fused);
     ++checks;
   }
   // Jacobi-2D update: the fixed-point sum and its product by 0.2 on integers.
@@ -122,6 +124,22 @@ int main(int argc, char** argv) {
     if (bits(mul02<59>(W)) != bits(want02)) return fail("0.2 product", x, 0.2, want02, mul02<59>(W));
     ++checks;
   }
+  // The product by 0.2 over the whole domain of mul02, [2^12, 2^62) with at
+  // most 53 significant bits: its 32-bit path (the top 64 product bits at
+  // least 2^32) and its general path against each other and against the CPU.
+  for (long it = 0; it < n; ++it) {
+    const int bitsm = 1 + static_cast<int>(rng() % 53);
+    const uint64_t m = (rng() >> (64 - bitsm)) | (uint64_t(1) << (bitsm - 1));
+    const int lead = 12 + static_cast<int>(rng() % 50);  // leading bit 12 .. 61
+    if (lead < bitsm - 1) continue;
+    const int64_t W = static_cast<int64_t>(m << (lead - (bitsm - 1)));
+    if (mul02<59>(W) != mul02_wide<59>(W) || bits(mul02<59>(W)) != bits(mul02_wide<59>(W)))
+      return fail("0.2 product paths", to_f64<59>(W), 0.2, mul02_wide<59>(W), mul02<59>(W));
+    volatile double x = to_f64<59>(W);
+    volatile double want02 = 0.2 * x;
+    if (bits(mul02<59>(W)) != bits(want02)) return fail("0.2 product, any length", x, 0.2, want02, mul02<59>(W));
+    ++checks;
+  }
   // round53p against round53 on non-negative integers of every length.
   for (long it = 0; it < n; ++it) {
     const int len = static_cast<int>(rng() % 63);
@@ -131,6 +149,39 @@ int main(int argc, char** argv) {
     if (round53q(x, 1u) != round53(x)) return fail("round53q", 0, 0, 0, 0);
     ++checks;
   }
+  // round53 (leading non-sign bit, clamped shifts) against the sign-fold form
+  // on integers of every length and both signs, and at the edges of its range
+  // and of the 53-bit window.
+  for (long it = 0; it < n; ++it) {
+    const int len = 1 + static_cast<int>(rng() % 63);
+    int64_t x = static_cast<int64_t>(rng() >> (64 - len));  // 0 .. 2^63 - 1
+    if (rng() & 1) x = -x;
+    const int64_t lim = (int64_t(1) << 62) + ((int64_t(1) << 62) - 2048);  // 2^63 - 2^11
+    if (x >= lim || x <= -lim) continue;
+    if (round53(x) != round53_fold(x)) return fail("round53 signed", 0, 0, 0, 0);
+    if (bits(round_to_f64<62>(x)) != bits(to_f64<62>(round53_fold(x))))
+      return fail("round_to_f64", 0, 0, to_f64<62>(round53_fold(x)), round_to_f64<62>(x));
+    if (bits(round_to_f64<59>(x)) != bits(to_f64<59>(round53_fold(x))))
+      return fail("round_to_f64<59>", 0, 0, to_f64<59>(round53_fold(x)), round_to_f64<59>(x));
+    ++checks;
+  }
+  for (int e = 0; e < 63; ++e)
+    for (int64_t d = -3; d <= 3; ++d)
+      for (int s : {1, -1}) {
+        const int64_t x = s * ((int64_t(1) << e) + d);
+        if (x > (int64_t(1) << 62) || x < -(int64_t(1) << 62)) continue;
+        if (round53(x) != round53_fold(x)) return fail("round53 edge", 0, 0, 0, 0);
+        if (bits(round_to_f64<62>(x)) != bits(to_f64<62>(round53_fold(x))))
+          return fail("round_to_f64 edge", 0, 0, to_f64<62>(round53_fold(x)), round_to_f64<62>(x));
+        // ties: 53 significant bits followed by exactly one half
+        if (e >= 54 && e <= 61) {
+          const int64_t t = s * ((int64_t(1) << e) + (int64_t(1) << (e - 53)) * (d & 3) + (int64_t(1) << (e - 54)));
+          if (round53(t) != round53_fold(t)) return fail("round53 tie", 0, 0, 0, 0);
+          if (bits(round_to_f64<62>(t)) != bits(to_f64<62>(round53_fold(t))))
+            return fail("round_to_f64 tie", 0, 0, to_f64<62>(round53_fold(t)), round_to_f64<62>(t));
+        }
+        ++checks;
+      }
   // mul02_any against the CPU's 0.2 * x over every exponent, both signs, and
   // the special values.
   for (long it = 0; it < n; ++it) {
