@@ -172,10 +172,42 @@ NPBGB_FX_FN int64_t from_f64_f59(double x, bool& ok) {
 // input in one step.
 constexpr uint32_t kPoisonHi = 0x40000000u;
 
+// v << s for a shift amount s read as unsigned, with amounts of 32 and more
+// giving 0 (PTX shl.b32 clamps the amount to the register width).
+NPBGB_FX_FN uint32_t shl_clamp32(uint32_t v, uint32_t s) {
+#if defined(__CUDA_ARCH__)
+  uint32_t r;
+  asm("shl.b32 %0, %1, %2;" : "=r"(r) : "r"(v), "r"(s));
+  return r;
+#else
+  return s >= 32u ? 0u : v << s;
+#endif
+}
+
+// from_f64_f59 with refused values marked by the poison bit in the high word
+// (the low word of a poisoned value is unspecified).
+//
+// For x in [2^-7, 1) the exponent field e is 1016 .. 1022, so sh = e - 1016 =
+// 0 .. 6 and X = significand << sh: a funnel shift for the high word and a
+// shift for the low word.  The implicit leading bit is the exponent field's
+// bit 9 (set for every e in 1016 .. 1022, clear for +0.0) moved to bit 20, so
+// +0.0 gives X = 0 with no select.  Every other x has sh > 6 as an unsigned
+// number (a sign bit or a smaller exponent wraps it around) and is poisoned,
+// except +0.0.
 NPBGB_FX_FN int64_t from_f64_f59_or_poison(double x) {
-  bool ok;
-  const int64_t v = from_f64_f59(x, ok);
-  return ok ? v : static_cast<int64_t>(static_cast<uint64_t>(kPoisonHi) << 32);
+  const uint64_t b = bits_of(x);
+  const uint32_t hi = static_cast<uint32_t>(b >> 32);
+  const uint32_t lo = static_cast<uint32_t>(b);
+  const uint32_t sh = (hi >> 20) - 1016u;
+  const uint32_t mh = (hi & 0xfffffu) | ((hi >> 9) & 0x100000u);
+  const bool ok = sh <= 6u || b == 0;
+#if defined(__CUDA_ARCH__)
+  const uint32_t xh = __funnelshift_l(lo, mh, sh);  // the amount is taken mod 32
+#else
+  const uint32_t xh = static_cast<uint32_t>(((static_cast<uint64_t>(mh) << 32 | lo) << (sh & 31u)) >> 32);
+#endif
+  const uint32_t xl = shl_clamp32(lo, sh);
+  return static_cast<int64_t>((static_cast<uint64_t>(ok ? xh : kPoisonHi) << 32) | xl);
 }
 
 NPBGB_FX_FN uint32_t hi32(int64_t x) { return static_cast<uint32_t>(static_cast<uint64_t>(x) >> 32); }

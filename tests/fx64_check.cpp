@@ -218,6 +218,21 @@ int main(int argc, char** argv) {
       if (bits(mul02<59>(W)) != bits(want02)) return fail("0.2 tie", x, 0.2, want02, mul02<59>(W));
       ++checks;
     }
+  // The poison-marking conversion against from_f64_f59 on every kind of bit
+  // pattern: equal where accepted, poisoned where refused.
+  for (long it = 0; it < 4 * n; ++it) {
+    uint64_t b = rng();
+    const int kind = static_cast<int>(rng() % 4);
+    if (kind == 0) b = (b & 0x800fffffffffffffull) | ((1016ull + rng() % 7) << 52);  // in range, either sign
+    if (kind == 1) b = (b & 0x800fffffffffffffull) | ((1008ull + rng() % 24) << 52);  // around the range
+    if (kind == 2 && (rng() & 1)) b = (rng() & 3) == 0 ? 0 : (rng() & 1 ? 0x8000000000000000ull : b & 0xfffffffffffffull);
+    bool ok;
+    const int64_t want = from_f64_f59(double_of(b), ok);
+    const int64_t got = from_f64_f59_or_poison(double_of(b));
+    if (ok && got != want) return fail("poison conversion value", double_of(b), 0, 0, 0);
+    if (!ok && !(hi32(got) & kPoisonHi)) return fail("poison conversion mark", double_of(b), 0, 0, 0);
+    ++checks;
+  }
   // Values the fast path must refuse.
   const double refuse[] = {-0.0, -0.5, 1.0, 1.5, 0x1p-8, 0x1p-1030, 1e300, __builtin_inf(),
                            __builtin_nan("")};
