@@ -136,6 +136,12 @@ extern "C" {
                                          adds, 2 multiply-add 64-bit adds, 3 most of
                                          the rounding on the multiply-add pipe.
                                          Results are identical. */
+#define NPBGB_CFG_JACOBI_TMA 26       /* jacobi2d single-grid kernel: each warp
+                                         streams its rows through its own ring of
+                                         TMA copies (rows a multiple of 16 bytes)
+                                         for binary64 arrays of 64 MiB and more (1,
+                                         default), for every aligned grid (2), or
+                                         never (0).  Results are identical. */
 
 /* Batch forms. */
 #define NPBGB_BATCH_PERSISTENT 1

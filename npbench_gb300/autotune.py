@@ -59,6 +59,7 @@ _KNOBS = {
     "HEAT_CHUNK": _lib.NPBGB_CFG_HEAT_CHUNK,
     "HEAT_TB": _lib.NPBGB_CFG_HEAT_TB,
     "JACOBI_BANDS": _lib.NPBGB_CFG_JACOBI_BANDS,
+    "JACOBI_TMA": _lib.NPBGB_CFG_JACOBI_TMA,
 }
 
 
@@ -75,6 +76,11 @@ def _space(bench, dtype):
                 out.append(cfg)
             if f64:  # the whole loop in one launch where the bands fit
                 out.append({"JACOBI_HW_WARPS": hw, "JACOBI_CHUNK": 0, "JACOBI_BANDS": 2})
+        if f64:  # each warp's TMA ring on grids below the size where it is automatic
+            for hw in (2, 3, 4):
+                for ch in (8, 16, 32):
+                    out.append({"JACOBI_HW_WARPS": hw, "JACOBI_CHUNK": ch, "JACOBI_BANDS": 0,
+                                "JACOBI_TMA": 2})
     elif bench == "heat_3d":
         for rows in (1, 2, 4):
             tj = 8 * rows

@@ -35,6 +35,7 @@ int64_t g_cfg_heat_mad_rows = 0;
 int64_t g_cfg_queue_whole_cells = 65536;
 int64_t g_cfg_jacobi_fx_mul = 1;
 int64_t g_cfg_jacobi_fx_adds = 0;
+int64_t g_cfg_jacobi_tma = 1;
 
 namespace {
 std::atomic<int64_t> g_launches{0};
@@ -50,6 +51,7 @@ uint32_t take_cfd_device_error();
 uint32_t take_queue_device_error();
 uint32_t take_heat_tb_device_error();
 uint32_t take_jacobi_bands_device_error();
+uint32_t take_jacobi_tma_device_error();
 int32_t launch_wait_timeout_selftest(uint64_t limit_ns, cudaStream_t st);
 
 int32_t set_error(int32_t code, const char* fmt, ...) {
@@ -193,6 +195,10 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       if (value < 0 || value > 3) return set_error(NPBGB_ERR_ARG, "jacobi fx adds: 0 .. 3");
       g_cfg_jacobi_fx_adds = value;
       return NPBGB_OK;
+    case NPBGB_CFG_JACOBI_TMA:
+      if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "jacobi tma: 0, 1 or 2");
+      g_cfg_jacobi_tma = value;
+      return NPBGB_OK;
     case NPBGB_CFG_JACOBI_FX_MUL:
       if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "jacobi fx mul: 0, 1 or 2");
       g_cfg_jacobi_fx_mul = value;
@@ -254,6 +260,7 @@ int32_t npbgb_get_config(int32_t key, int64_t* value) {
     case NPBGB_CFG_JACOBI_BANDS_WARPS: *value = g_cfg_jacobi_bands_warps; return NPBGB_OK;
     case NPBGB_CFG_HEAT_STAGES: *value = g_cfg_heat_stages; return NPBGB_OK;
     case NPBGB_CFG_JACOBI_FX_ADDS: *value = g_cfg_jacobi_fx_adds; return NPBGB_OK;
+    case NPBGB_CFG_JACOBI_TMA: *value = g_cfg_jacobi_tma; return NPBGB_OK;
     case NPBGB_CFG_JACOBI_FX_MUL: *value = g_cfg_jacobi_fx_mul; return NPBGB_OK;
     case NPBGB_CFG_QUEUE_WHOLE_CELLS: *value = g_cfg_queue_whole_cells; return NPBGB_OK;
     case NPBGB_CFG_HEAT_MAD_ROWS: *value = g_cfg_heat_mad_rows; return NPBGB_OK;
@@ -269,10 +276,12 @@ int32_t npbgb_device_status(void* stream) {
   const uint32_t h = take_heat_device_error() | take_heat_tb_device_error();
   const uint32_t bt = take_batch_device_error();
   const uint32_t cf = take_cfd_device_error() | take_jacobi_bands_device_error();
+  const uint32_t jt = take_jacobi_tma_device_error();
   const uint32_t qu = take_queue_device_error();
-  if (h == 0xffffffffu || bt == 0xffffffffu || cf == 0xffffffffu || qu == 0xffffffffu)
+  if (h == 0xffffffffu || bt == 0xffffffffu || cf == 0xffffffffu || qu == 0xffffffffu || jt == 0xffffffffu)
     return set_error(NPBGB_ERR_CUDA, "reading the device error words");
   if (h) return set_error(NPBGB_ERR_TIMEOUT, "a bounded device wait gave up (heat3d)");
+  if (jt) return set_error(NPBGB_ERR_TIMEOUT, "a bounded device wait gave up (jacobi2d)");
   if (bt) return set_error(NPBGB_ERR_TIMEOUT, "a batch CTA made no progress within its limit");
   if (cf) return set_error(NPBGB_ERR_TIMEOUT, "a band waited on its neighbours past its limit");
   if (qu & 1u) return set_error(NPBGB_ERR_TIMEOUT, "a queue worker saw no tile complete within its limit");

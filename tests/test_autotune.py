@@ -41,9 +41,12 @@ def test_keys_name_benchmark_dtype_and_shape_class():
 
 def test_search_spaces():
     sp = autotune._space("jacobi_2d", np.float64)
-    assert {"JACOBI_HW_WARPS": 4, "JACOBI_CHUNK": 3, "JACOBI_BANDS": 0} in sp and len(sp) == 56
-    # binary64: the chained launches or the whole loop in one launch (bands)
+    assert {"JACOBI_HW_WARPS": 4, "JACOBI_CHUNK": 3, "JACOBI_BANDS": 0} in sp and len(sp) == 65
+    # binary64: the chained launches, the whole loop in one launch (bands), or the
+    # chained launches with each warp's TMA ring forced on
     assert {"JACOBI_HW_WARPS": 4, "JACOBI_CHUNK": 0, "JACOBI_BANDS": 2} in sp
+    assert {"JACOBI_HW_WARPS": 3, "JACOBI_CHUNK": 16, "JACOBI_BANDS": 0, "JACOBI_TMA": 2} in sp
+    assert all("JACOBI_TMA" not in c for c in autotune._space("jacobi_2d", np.float32))
     f32j = autotune._space("jacobi_2d", np.float32)
     assert all(c["JACOBI_HW_WARPS"] == -1 and "JACOBI_BANDS" not in c for c in f32j)
     heat = autotune._space("heat_3d", np.float64)

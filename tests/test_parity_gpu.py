@@ -668,6 +668,48 @@ def test_jacobi_f64_integer_and_hardware_paths_agree(field):
             _lib.set_config(_lib.NPBGB_CFG_F64_EMULATION, old)
 
 
+@pytest.mark.parametrize("tma", [2, 0])
+@pytest.mark.parametrize("shape", [(300, 518), (37, 46), (5, 8), (130, 4), (1000, 1000)])
+def test_jacobi_tma_ring_and_plain_loads(tma, shape):
+    """Each warp's TMA ring (forced on every grid whose rows are 16-byte multiples)
+    and the plain-load strips give the oracle's bits: binary64 in fixed point and on
+    hardware, with uniform and mixed-range fields, and binary32; odd widths fall back
+    to the plain loads, chunks of 1 and 7 rows leave partial boxes."""
+    from npbench_gb300 import autotune
+    keys = (_lib.NPBGB_CFG_JACOBI_TMA, _lib.NPBGB_CFG_JACOBI_CHUNK)
+    was = autotune.enabled()
+    autotune.disable()
+    try:
+        for chunk in (0, 1, 7):
+            old = [_lib.set_config(k, v) for k, v in zip(keys, (tma, chunk))]
+            try:
+                cases = [(np.float64, "uniform", 1), (np.float64, "mixed", 1),
+                         (np.float64, "uniform", 0), (np.float32, "uniform", 1)]
+                for dt, field, emul in cases:
+                    A, B = (workloads.uniform_pair(shape, dt, seed=shape[0] + chunk)
+                            if field == "uniform"
+                            else (_mixed_range_field(shape, 90), _mixed_range_field(shape, 91)))
+                    T = 4 if shape[0] == 1000 else 7
+                    ra, rb = A.copy(), B.copy()
+                    cref.jacobi_2d_kernel(T, ra, rb)
+                    old_e = _lib.set_config(_lib.NPBGB_CFG_F64_EMULATION, emul)
+                    try:
+                        dA, dB = _dev(A), _dev(B)
+                        stencils.jacobi_2d_kernel(T, dA, dB)
+                        _lib.device_status()
+                    finally:
+                        _lib.set_config(_lib.NPBGB_CFG_F64_EMULATION, old_e)
+                    assert bits_equal(_host(dA), ra), (tma, shape, chunk, dt, field, emul,
+                                                       first_diff(_host(dA), ra))
+                    assert bits_equal(_host(dB), rb), (tma, shape, chunk, dt, field, emul)
+            finally:
+                for k, v in zip(keys, old):
+                    _lib.set_config(k, v)
+    finally:
+        if was:
+            autotune.enable()
+
+
 @pytest.mark.parametrize("chunk", [1, 5, 64, 4000])
 def test_jacobi_chunking_does_not_change_bits(chunk):
     from npbench_gb300 import _lib
