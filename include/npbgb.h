@@ -136,6 +136,14 @@ extern "C" {
                                          adds, 2 multiply-add 64-bit adds, 3 most of
                                          the rounding on the multiply-add pipe.
                                          Results are identical. */
+#define NPBGB_CFG_BATCH_TMA 27        /* stepped batches, read when planned: binary64
+                                         Jacobi-2D grids whose rows are 16-byte
+                                         multiples stream each warp's rows through a
+                                         ring of TMA copies (1) or use plain loads
+                                         (0, default: the rings measured 1-1.5%
+                                         slower on the 4096-grid batch, whose
+                                         32-64-row tiles are short).  Results are
+                                         identical. */
 #define NPBGB_CFG_JACOBI_TMA 26       /* jacobi2d single-grid kernel: each warp
                                          streams its rows through its own ring of
                                          TMA copies (rows a multiple of 16 bytes)

@@ -44,6 +44,7 @@ NPBGB_CFG_QUEUE_WHOLE_CELLS = 23
 NPBGB_CFG_JACOBI_FX_MUL = 24
 NPBGB_CFG_JACOBI_FX_ADDS = 25
 NPBGB_CFG_JACOBI_TMA = 26
+NPBGB_CFG_BATCH_TMA = 27
 NPBGB_BATCH_PERSISTENT = 1
 NPBGB_BATCH_STEPPED = 2
 NPBGB_BATCH_QUEUE = 3

@@ -313,7 +313,7 @@ def batch_applied(settings):
         yield settings
 
 
-def tune_batch(n_grids=512, seed=0, rows=(32, 64, 128, 256), hw_warps=(-1, 2, 6), repeats=2,
+def tune_batch(n_grids=512, seed=0, rows=(32, 64, 128, 256), hw_warps=(-1, 2, 3, 6), repeats=2,
                store=True, path=None, guard=True, full_grids=4096):
     """Tunes the stepped batch's tile rows and binary64 hardware warps on the first
     n_grids of the batched configuration (its distribution: sides log-uniform in

@@ -48,6 +48,7 @@ extern int64_t g_cfg_f64_emulation;
 extern int64_t g_cfg_jacobi_hw_warps;
 extern int64_t g_cfg_batch_ctas_per_sm;
 extern int64_t g_cfg_batch_mode;
+extern int64_t g_cfg_batch_tma;
 
 namespace {
 
@@ -79,6 +80,7 @@ struct StepGrid {
   int32_t chunk;       // rows (Jacobi-2D) or planes (Heat-3D) per tile
   int32_t tx, ty;      // tiles along the contiguous axis and the next one
   int16_t dtype, kind;
+  int32_t map;         // binary64 Jacobi-2D: index of the grid's tensor-map pair, or -1
 };
 
 // A share of one grid's arrays for the binary32 <-> binary64 conversions of a
@@ -92,7 +94,7 @@ struct ConvChunk {
 };
 constexpr int64_t kConvChunk = 1 << 16;  // elements per conversion CTA
 
-__device__ unsigned int g_batch_error;  // bit 0: a CTA made no progress for the limit
+__device__ unsigned int g_batch_error;  // bit 0: a CTA made no progress for the limit; bit 1: a TMA wait gave up
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
   uint32_t v;
@@ -223,8 +225,9 @@ batch_persistent(const BandDesc* __restrict__ bands, uint32_t* done, const int32
 // per SM, as the single-grid fixed-point strip kernel runs.
 __global__ void __launch_bounds__(kBThreads, 4)
 batch_step(const StepGrid* __restrict__ grids, const int32_t* __restrict__ tile_grid, int32_t s,
-           int f64_emulation, int hw_warps, uint32_t one) {
+           int f64_emulation, int hw_warps, uint32_t one, const CUtensorMap* __restrict__ maps) {
   pdl_begin();
+  extern __shared__ __align__(128) unsigned char ring_smem[];  // the TMA rings (binary64 Jacobi-2D)
   const int64_t t = blockIdx.x;
   const StepGrid G = grids[tile_grid[t]];
   const int64_t r = t - G.first_tile;
@@ -257,7 +260,28 @@ batch_step(const StepGrid* __restrict__ grids, const int32_t* __restrict__ tile_
   const int64_t k0 = 1 + (bx * kBWarps + warp) * 32;
   if (k0 >= G.n1 - 1) return;  // warp-uniform; the strip path has no CTA barrier
   const int64_t ib = 1 + rest * G.chunk, ie = min(ib + G.chunk, int64_t(G.n0) - 1);
-  if (G.dtype == NPBGB_F64) {
+  if (G.dtype == NPBGB_F64 && G.map >= 0) {
+    // Each warp's ring of TMA copies (jcore::tma_strip_rows), from the source's map.
+    using TS = jcore::TmaStrip<double, kBWarps>;
+    const double* sp = static_cast<const double*>(src);
+    double* dp = static_cast<double*>(dst);
+    const CUtensorMap* map = &maps[2 * G.map + (odd ? 1 : 0)];
+    // The rings start at the first 128-byte boundary of the dynamic shared
+    // memory (TMA destinations are 128-byte aligned; the launch adds 128 bytes).
+    unsigned char* rings = ring_smem + ((128u - (tma::smem_u32(ring_smem) & 127u)) & 127u);
+    unsigned char* ring = rings + warp * TS::kWarpBytes;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(rings + kBWarps * TS::kWarpBytes) + warp * jcore::kTmaRing;
+    if ((threadIdx.x & 31) == 0) {
+      tma::fence_tensormap_acquire(map);
+      for (int q = 0; q < jcore::kTmaRing; ++q) tma::mbar_init(&bars[q], 1);
+      tma::fence_mbar_init();
+    }
+    __syncwarp();
+    const bool ok = (!f64_emulation || warp < hw_warps)
+                        ? jcore::tma_strip_rows<double, false, 0, true>(map, sp, dp, G.n1, k0, ib, ie, ring, bars, one)
+                        : jcore::tma_strip_rows<double, true, 0, true>(map, sp, dp, G.n1, k0, ib, ie, ring, bars, one);
+    if (!ok && (threadIdx.x & 31) == 0) atomicOr(&g_batch_error, 2u);
+  } else if (G.dtype == NPBGB_F64) {
     const double* sp = static_cast<const double*>(src);
     double* dp = static_cast<double*>(dst);
     // Two rows loaded ahead (tiles are 128 rows tall; measured 12% faster than one).
@@ -331,6 +355,9 @@ struct npbgb_batch {
   std::vector<int32_t> launch_tiles;  // CTAs of launch s = tiles of the grids active at s
   npbgb::ConvChunk* d_conv = nullptr;  // stepped form: conversion chunks of promoted grids
   int64_t cap_conv = 0, nconv = 0;
+  CUtensorMap* d_maps = nullptr;  // stepped form: tensor maps (a, b) of the TMA grids
+  int64_t cap_maps = 0;
+  size_t step_smem = 0;           // dynamic shared memory of each stepped launch
   // Queue form (mode NPBGB_BATCH_QUEUE).
   npbgb::qhost::StaticQueue* sq = nullptr;
 };
@@ -409,6 +436,7 @@ void free_batch(npbgb_batch* b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   npbgb::qhost::free_static(b->sq);
   cudaFree(b->d_conv);
+  cudaFree(b->d_maps);
   cudaFree(b->d_step);
   cudaFree(b->d_tiles);
   cudaFree(b->d_bands);
@@ -427,8 +455,9 @@ int32_t launch_stepped(npbgb_batch* b, cudaStream_t st) {
     e = launch_chained(batch_convert, dim3{unsigned(b->nconv)}, dim3{256u}, 0, st,
                        static_cast<const ConvChunk*>(b->d_conv), 1);
   for (size_t s = 0; s < b->launch_tiles.size() && e == cudaSuccess; ++s)
-    e = launch_chained(batch_step, dim3{unsigned(b->launch_tiles[s])}, dim3{unsigned(kBThreads)}, 0,
-                       st, b->d_step, b->d_tiles, int32_t(s), f64_emul, hw_warps, 1u);
+    e = launch_chained(batch_step, dim3{unsigned(b->launch_tiles[s])}, dim3{unsigned(kBThreads)},
+                       b->step_smem, st, b->d_step, b->d_tiles, int32_t(s), f64_emul, hw_warps, 1u,
+                       static_cast<const CUtensorMap*>(b->d_maps));
   if (b->nconv > 0 && e == cudaSuccess)
     e = launch_chained(batch_convert, dim3{unsigned(b->nconv)}, dim3{256u}, 0, st,
                        static_cast<const ConvChunk*>(b->d_conv), 0);
@@ -472,6 +501,7 @@ int32_t plan_stepped(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int
                      int64_t updates) {
   using namespace npbgb;
   std::vector<StepGrid> sg;
+  std::vector<CUtensorMap> maps;
   for (int64_t g = 0; g < count; ++g) {
     const npbgb_grid& G = grids[g];
     const bool heat = G.kind == NPBGB_KIND_HEAT3D;
@@ -489,6 +519,23 @@ int32_t plan_stepped(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int
     d.count = int32_t(todo);
     d.dtype = int16_t(G.dtype);
     d.kind = int16_t(G.kind);
+    d.map = -1;
+    // On request (NPBGB_CFG_BATCH_TMA), binary64 Jacobi-2D grids whose rows are
+    // 16-byte multiples stream through each warp's ring of TMA copies (box: 34
+    // columns x kTmaRows rows).  Off by default: on the 4096-grid batch the
+    // rings measured 1-1.5% slower than two rows loaded ahead (3.67 against
+    // 3.63 s per pass with 64-row tiles, 3.73 against 3.68 with 32).
+    if (!heat && G.dtype == NPBGB_F64 && g_cfg_batch_tma && (G.n1 * 8) % 16 == 0) {
+      CUtensorMap ma, mb;
+      const uint64_t dims[3] = {uint64_t(G.n1), uint64_t(G.n0), 1u};
+      const uint32_t box[3] = {uint32_t(jcore::TmaStrip<double, kBWarps>::BX), uint32_t(jcore::kTmaRows), 1u};
+      if (tma::encode_3d(&ma, 8, G.a, dims, box) == cudaSuccess &&
+          tma::encode_3d(&mb, 8, G.b, dims, box) == cudaSuccess) {
+        d.map = int32_t(maps.size() / 2);
+        maps.push_back(ma);
+        maps.push_back(mb);
+      }
+    }
     const int32_t rows = G.band_rows > 0 ? G.band_rows : (band_rows > 0 ? band_rows : (heat ? 16 : 32));
     d.chunk = rows;
     if (heat) {
@@ -572,6 +619,18 @@ int32_t plan_stepped(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int
       (e = cudaMemcpy(b->d_conv, conv.data(), sizeof(ConvChunk) * conv.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
     return cuda_status(e, "batch: upload");
   b->nconv = int64_t(conv.size());
+  if (int64_t(maps.size()) > b->cap_maps) {
+    cudaFree(b->d_maps);
+    b->d_maps = nullptr;
+    b->cap_maps = 0;
+    if ((e = cudaMalloc(&b->d_maps, sizeof(CUtensorMap) * maps.size())) != cudaSuccess)
+      return cuda_status(e, "batch: alloc");
+    b->cap_maps = int64_t(maps.size());
+  }
+  if (!maps.empty() &&
+      (e = cudaMemcpy(b->d_maps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_status(e, "batch: upload");
+  b->step_smem = maps.empty() ? 0 : jcore::TmaStrip<double, kBWarps>::smem() + 128;
   b->mode = NPBGB_BATCH_STEPPED;
   b->ntiles = int64_t(tiles.size());
   b->launch_tiles = std::move(launch_tiles);

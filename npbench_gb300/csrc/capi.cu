@@ -36,6 +36,7 @@ int64_t g_cfg_queue_whole_cells = 65536;
 int64_t g_cfg_jacobi_fx_mul = 1;
 int64_t g_cfg_jacobi_fx_adds = 0;
 int64_t g_cfg_jacobi_tma = 1;
+int64_t g_cfg_batch_tma = 0;
 
 namespace {
 std::atomic<int64_t> g_launches{0};
@@ -199,6 +200,10 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "jacobi tma: 0, 1 or 2");
       g_cfg_jacobi_tma = value;
       return NPBGB_OK;
+    case NPBGB_CFG_BATCH_TMA:
+      if (value != 0 && value != 1) return set_error(NPBGB_ERR_ARG, "batch tma: 0 or 1");
+      g_cfg_batch_tma = value;
+      return NPBGB_OK;
     case NPBGB_CFG_JACOBI_FX_MUL:
       if (value < 0 || value > 2) return set_error(NPBGB_ERR_ARG, "jacobi fx mul: 0, 1 or 2");
       g_cfg_jacobi_fx_mul = value;
@@ -261,6 +266,7 @@ int32_t npbgb_get_config(int32_t key, int64_t* value) {
     case NPBGB_CFG_HEAT_STAGES: *value = g_cfg_heat_stages; return NPBGB_OK;
     case NPBGB_CFG_JACOBI_FX_ADDS: *value = g_cfg_jacobi_fx_adds; return NPBGB_OK;
     case NPBGB_CFG_JACOBI_TMA: *value = g_cfg_jacobi_tma; return NPBGB_OK;
+    case NPBGB_CFG_BATCH_TMA: *value = g_cfg_batch_tma; return NPBGB_OK;
     case NPBGB_CFG_JACOBI_FX_MUL: *value = g_cfg_jacobi_fx_mul; return NPBGB_OK;
     case NPBGB_CFG_QUEUE_WHOLE_CELLS: *value = g_cfg_queue_whole_cells; return NPBGB_OK;
     case NPBGB_CFG_HEAT_MAD_ROWS: *value = g_cfg_heat_mad_rows; return NPBGB_OK;
@@ -282,7 +288,7 @@ int32_t npbgb_device_status(void* stream) {
     return set_error(NPBGB_ERR_CUDA, "reading the device error words");
   if (h) return set_error(NPBGB_ERR_TIMEOUT, "a bounded device wait gave up (heat3d)");
   if (jt) return set_error(NPBGB_ERR_TIMEOUT, "a bounded device wait gave up (jacobi2d)");
-  if (bt) return set_error(NPBGB_ERR_TIMEOUT, "a batch CTA made no progress within its limit");
+  if (bt) return set_error(NPBGB_ERR_TIMEOUT, "a batch CTA made no progress, or a batch TMA wait gave up, within its limit");
   if (cf) return set_error(NPBGB_ERR_TIMEOUT, "a band waited on its neighbours past its limit");
   if (qu & 1u) return set_error(NPBGB_ERR_TIMEOUT, "a queue worker saw no tile complete within its limit");
   if (qu) return set_error(NPBGB_ERR_STATE, "a queue worker found an invalid inbox entry");

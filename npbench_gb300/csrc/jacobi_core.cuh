@@ -16,6 +16,7 @@
 
 #include "fx64.cuh"
 #include "npbgb_common.cuh"
+#include "tma.cuh"
 
 namespace npbgb {
 
@@ -148,6 +149,103 @@ __device__ __forceinline__ void points2_f32(const Strip<float, false, CG, MAD, I
     st<CG>(sp.dst + i * sp.nx + sp.j, f2x(out));
     st<CG>(sp.dst + (i + 1) * sp.nx + sp.j, f2y(out));
   }
+}
+
+// ---------------------------------------------------------------------------
+// TMA form: each warp streams its strip's rows through its own ring
+// ---------------------------------------------------------------------------
+// The plain-load strip keeps one row per warp in flight (binary64), so at
+// 4096^2 the kernel waits on load latency with DRAM at a quarter of its
+// bandwidth.  Here every warp owns a ring of kTmaRing boxes of kTmaRows rows
+// of its strip and the two halo columns (34 columns of binary64, 36 of
+// binary32: a 16-byte multiple), each box one cp.async.bulk.tensor copy that
+// completes on the box's own mbarrier.  Lane 0 issues; every lane reads its
+// column (and lanes 0 and 31 the halo columns) from shared memory into the
+// same register queue as the plain-load strip, and a box's slot is refilled
+// as soon as its last row has been read.  The warps of a CTA never wait on
+// each other.  Rows beyond the array read as zero (the tensor map's
+// out-of-bounds fill) and are never written.
+constexpr int kTmaRows = 4;  // rows per box
+constexpr int kTmaRing = 4;  // boxes per warp: 16 rows in flight
+
+template <typename T, int kWarps>
+struct TmaStrip {
+  static constexpr int BX = sizeof(T) == 8 ? 34 : 36;  // box columns k0-1 .. k0+BX-2
+  static constexpr int kBoxBytes = BX * kTmaRows * int(sizeof(T));
+  static constexpr int kSlot = (kBoxBytes + 127) / 128 * 128;  // 128-byte aligned slots
+  static constexpr int kWarpBytes = kTmaRing * kSlot;
+  static constexpr size_t smem() { return size_t(kWarps) * (kWarpBytes + kTmaRing * sizeof(uint64_t)); }
+};
+
+// Output rows [ib, ie) of the strip at columns k0 .. k0+31 (warp-collective),
+// from the tensor map `map` of the source array (read through the tensormap
+// proxy; a map in global memory must be fenced before its first use).  FXW:
+// this warp evaluates in fixed point.  Returns false when a wait gave up
+// (after waiting, bounded, for the copies it still had in flight).
+template <typename T, bool FXW, int MAD, bool IMUL>
+__device__ __forceinline__ bool tma_strip_rows(const CUtensorMap* map, const T* src, T* dst, int64_t nx,
+                                               int64_t k0, int64_t ib, int64_t ie, unsigned char* ring,
+                                               uint64_t* bars, uint32_t one) {
+  using G = TmaStrip<T, 8>;
+  using St = Strip<T, FXW, false, MAD, IMUL, false>;
+  using S = typename St::S;
+  const St s(src, dst, nx, k0, one);
+  const int lane = threadIdx.x & 31;
+  const int nrows = int(ie - ib) + 2;  // staged rows ib-1 .. ie
+  const int nbox = (nrows + kTmaRows - 1) / kTmaRows;
+  const int x0 = int(k0 - 1), y0 = int(ib - 1);  // x0 = 32 * strip: a 16-byte multiple
+  auto issue = [&](int b) {
+    uint64_t* bar = &bars[b % kTmaRing];
+    tma::mbar_arrive_expect_tx(bar, G::kBoxBytes);
+    tma::load_3d(ring + (b % kTmaRing) * G::kSlot, map, x0, y0 + b * kTmaRows, 0, bar);
+  };
+  auto read = [&](int q, S& own, S& halo) {
+    const T* row = reinterpret_cast<const T*>(ring + ((q / kTmaRows) % kTmaRing) * G::kSlot) +
+                   (q % kTmaRows) * G::BX;
+    const T v = row[lane + 1];
+    if constexpr (FXW) own = fx::from_f64_f59_or_poison(v); else own = v;
+    if (lane == 0 || lane == 31) {
+      const T h = row[lane == 0 ? 0 : 33];
+      if constexpr (FXW) halo = fx::from_f64_f59_or_poison(h); else halo = h;
+    }
+  };
+  const int first = nbox < kTmaRing ? nbox : kTmaRing;
+  if (lane == 0)
+    for (int b = 0; b < first; ++b) issue(b);
+  int issued = first, waited = 1;
+  bool ok = tma::mbar_wait(&bars[0], 0);
+  S xp = S(0), xc = S(0), xn = S(0), hp = S(0), hc = S(0), hn = S(0);
+  if (ok) {
+    read(0, xp, hp);
+    read(1, xc, hc);
+  }
+  for (int q = 1; ok && q + 1 < nrows; ++q) {  // output row ib - 1 + q
+    const int qn = q + 1;
+    if (qn % kTmaRows == 0) {
+      const int b = qn / kTmaRows;
+      ok = tma::mbar_wait(&bars[b % kTmaRing], uint32_t((b / kTmaRing) & 1));
+      waited = b + 1;
+      if (!ok) break;
+    }
+    read(qn, xn, hn);
+    if (qn % kTmaRows == kTmaRows - 1) {  // box fully read: refill its slot
+      tma::fence_proxy_async();
+      __syncwarp();
+      const int b = qn / kTmaRows + kTmaRing;
+      if (b < nbox) {
+        if (lane == 0) issue(b);
+        issued = b + 1;
+      }
+    }
+    s.point(ib - 1 + q, xp, xc, xn, hc);
+    xp = xc;
+    xc = xn;
+    hc = hn;
+  }
+  if (!ok)  // let the copies still in flight land (bounded) before the CTA may exit
+    for (int b = waited; b < issued; ++b)
+      tma::mbar_wait_for(&bars[b % kTmaRing], uint32_t((b / kTmaRing) & 1), tma::kWaitLimitNs / 16);
+  return ok;
 }
 
 // One strip (columns k0 .. k0+31) over rows [r0, r1).  Warp-collective.

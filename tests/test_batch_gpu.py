@@ -63,6 +63,39 @@ def test_batch_matches_oracle_and_single_launches(band_rows):
         assert torch.equal(sA, dA) and torch.equal(sB, dB), n
 
 
+@pytest.mark.parametrize("tma", [1, 0])
+def test_stepped_batch_tma_rings_match_oracle(batch_mode, tma):
+    """The stepped form's binary64 Jacobi-2D tiles through each warp's TMA ring (rows
+    of a 16-byte multiple, on request) or plain loads: the oracle's bits on uniform and
+    mixed-range fields, even and odd widths, tiles of 1, 7 and 32 rows."""
+    if batch_mode != _lib.NPBGB_BATCH_STEPPED:
+        pytest.skip("the TMA rings belong to the stepped form")
+    rng = np.random.default_rng(7 + tma)
+    grids = []
+    for g, (ny, nx) in enumerate([(3, 4), (9, 30), (40, 34), (130, 258), (77, 64), (65, 65), (200, 17)]):
+        A = rng.random((ny, nx))
+        B = rng.random((ny, nx))
+        if g % 3 == 1:  # values outside the fixed-point range take the hardware path
+            flat = A.reshape(-1)
+            flat[rng.choice(flat.size, size=max(1, flat.size // 20), replace=False)] = -0.5
+        grids.append((A, B, int(rng.integers(2, 12))))
+    old = _lib.set_config(_lib.NPBGB_CFG_BATCH_TMA, tma)
+    try:
+        for rows in (1, 7, 32):
+            dev = [(torch.from_numpy(A).to(DEV), torch.from_numpy(B).to(DEV), T) for A, B, T in grids]
+            with Batch(dev, band_rows=rows) as b:
+                b.launch()
+                _lib.device_status()
+            for n, ((A, B, T), (dA, dB, _)) in enumerate(zip(grids, dev)):
+                ra, rb = A.copy(), B.copy()
+                cref.jacobi_2d_kernel(T, ra, rb)
+                assert bits_equal(dA.cpu().numpy(), ra), (tma, rows, n, A.shape, T,
+                                                          first_diff(dA.cpu().numpy(), ra))
+                assert bits_equal(dB.cpu().numpy(), rb), (tma, rows, n, A.shape, T)
+    finally:
+        _lib.set_config(_lib.NPBGB_CFG_BATCH_TMA, old)
+
+
 def test_batch_graph_replay_is_repeatable():
     grids = _mixed_batch(25, seed=99, max_side=500, max_t=30)
     init = [(torch.from_numpy(A).to(DEV), torch.from_numpy(B).to(DEV), T) for A, B, T in grids]
