@@ -15,11 +15,12 @@
 //
 // Method (the textbook one): order the operands by magnitude, give both
 // significands 9 guard bits (leading bit at bit 61), shift the smaller right
-// by the exponent difference keeping a sticky bit, add or subtract, put the
-// leading bit back at 61 (right by one with sticky after a carry, left after
-// cancellation, which is exact), and round the 9 low bits to nearest even.
-// With 9 guard bits and a sticky bit the rounding is exact in every case
-// (at most one bit of cancellation can follow a lossy alignment).
+// by the exponent difference keeping a sticky bit, add or subtract, move the
+// leading bit to 62 (no shift after a carry, left after no carry or after
+// cancellation, which is exact), and round the 10 low bits to nearest even as
+// (n + 2^9 - 1 + lsb) >> 10.  With 9 guard bits and a sticky bit the rounding
+// is exact in every case (at most one bit of cancellation can follow a lossy
+// alignment).
 //
 // Host and device: the header compiles for both, so the host build is
 // checked against the CPU's IEEE addition.
@@ -31,12 +32,6 @@
 
 namespace npbgb {
 namespace f64emu {
-
-// Leading zeros of a 64-bit value from two 32-bit counts.
-NPBGB_FX_FN int clz64_32(uint64_t v) {
-  const int hi = fx::clz32(static_cast<uint32_t>(v >> 32));
-  return hi < 32 ? hi : 32 + fx::clz32(static_cast<uint32_t>(v));
-}
 
 NPBGB_FX_FN bool dadd_ok(uint64_t a, uint64_t b) {
   const uint32_t ea = static_cast<uint32_t>(a >> 52) & 0x7ffu;
@@ -64,26 +59,17 @@ NPBGB_FX_FN uint64_t dadd_int(uint64_t a, uint64_t b) {
   const uint64_t my = ((y & kMant) | (1ull << 52)) << 9;
   uint32_t d = ex - ey;
   d = d < 63u ? d : 63u;
-  const uint64_t lost = my & ((1ull << d) - 1);
-  const uint64_t ya = (my >> d) | (lost != 0 ? 1ull : 0ull);
+  const uint64_t yt = my >> d;
+  const uint64_t ya = yt | ((yt << d) != my ? 1ull : 0ull);  // sticky: a bit was shifted out
   const bool sub = ((x ^ y) >> 63) != 0;
   const uint64_t s = sub ? mx - ya : mx + ya;
   if (s == 0) return 0;  // x + (-x) = +0 in round to nearest
-  const int lz = clz64_32(s);  // 1 (carry), 2 (aligned) or more (cancellation)
-  uint64_t n;
-  int e = int(ex);
-  if (lz == 1) {
-    n = (s >> 1) | (s & 1ull);
-    e += 1;
-  } else {
-    n = s << (lz - 2);
-    e -= lz - 2;
-  }
-  // n: leading bit 61, mantissa bits 61..9, round bit 8, sticky bits 7..0.
-  const uint64_t rest = n & 0x1ffull, lsb = (n >> 9) & 1ull;
-  const uint64_t up = (rest > 0x100ull || (rest == 0x100ull && lsb)) ? 1ull : 0ull;
-  const uint64_t m = (n >> 9) + up;  // in [2^52, 2^53]; 2^53 carries into the exponent
-  return (x & 0x8000000000000000ull) + ((static_cast<uint64_t>(e - 1) << 52) + m);
+  const int lz = fx::clz64(s);  // 1 (carry), 2 (aligned) or more (cancellation)
+  // n: leading bit 62, mantissa bits 62..10, round bit 9, sticky bits 8..0.
+  const uint64_t n = s << (lz - 1);
+  const uint64_t m = (n + 0x1ffull + ((n >> 10) & 1ull)) >> 10;  // [2^52, 2^53]; 2^53 carries on
+  // exponent of the sum: ex + 2 - lz; the field is that minus one plus m's leading bit
+  return (x & 0x8000000000000000ull) + ((static_cast<uint64_t>(int(ex) + 1 - lz) << 52) + m);
 }
 
 }  // namespace f64emu
