@@ -1106,9 +1106,11 @@ def serve_measure(rates=(200.0, 1000.0, 5000.0), n_requests=100, compare=True, f
         torch.cuda.synchronize()
         n_launch0 = _library_launches()
         srv = StencilServer(hbm_budget_bytes=150e9).start()
-        t0 = time.perf_counter()
         futs = []
         with ClockSampler(0) as clk:
+            # The arrival clock starts once the sampler runs (its start-up wait
+            # would otherwise turn the first arrivals into one burst).
+            t0 = time.perf_counter()
             for r, at in zip(reqs, arrivals):
                 now = time.perf_counter() - t0
                 if at > now:
