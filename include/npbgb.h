@@ -147,7 +147,7 @@ extern "C" {
 #define NPBGB_CFG_JACOBI_TMA 26       /* jacobi2d single-grid kernel: each warp
                                          streams its rows through its own ring of
                                          TMA copies (rows a multiple of 16 bytes)
-                                         for binary64 arrays of 64 MiB and more (1,
+                                         for binary64 arrays of 48 MiB and more (1,
                                          default), for every aligned grid (2), or
                                          never (0).  Results are identical. */
 

@@ -221,9 +221,11 @@ batch_persistent(const BandDesc* __restrict__ bands, uint32_t* done, const int32
 
 // Half-sweep s of every tile in [0, gridDim.x): CTA t finds its grid in the
 // tile table and processes one tile (Jacobi-2D: 8 warps x 32 columns x chunk
-// rows; Heat-3D: a 32 x 8 column tile streamed over chunk planes).  Four CTAs
-// per SM, as the single-grid fixed-point strip kernel runs.
-__global__ void __launch_bounds__(kBThreads, 4)
+// rows; Heat-3D: a 32 x 8 column tile streamed over chunk planes).  Five CTAs
+// per SM (48 registers, a few spilled): on the 4096-grid batch 3.13 s per pass
+// against 3.36 s with four (64 registers) and 3.47 s with six (40 registers,
+// more spills).
+__global__ void __launch_bounds__(kBThreads, 5)
 batch_step(const StepGrid* __restrict__ grids, const int32_t* __restrict__ tile_grid, int32_t s,
            int f64_emulation, int hw_warps, uint32_t one, const CUtensorMap* __restrict__ maps) {
   pdl_begin();

@@ -151,14 +151,15 @@ int32_t run(T* a, T* b, int64_t ny, int64_t nx, int32_t tsteps, cudaStream_t st)
   // the integer pipes unless NPBGB_CFG_JACOBI_FX_MUL = 0.
   const int mad = (FX && g_cfg_jacobi_fx_adds > 0) ? int(g_cfg_jacobi_fx_adds) - 1 : 0;
   const int64_t im = g_cfg_jacobi_fx_mul;
-  // The TMA ring where it pays: binary64 arrays of 64 MiB and more (beyond
-  // the L2), automatically; any aligned grid when forced (NPBGB_CFG_JACOBI_TMA
-  // = 2).  Measured on GB300 (TSTEPS=21 at 4096^2, 41 at 2048^2, 100 at 1000^2
-  // and 500^2; best settings of each form, ms): 4096^2 binary64 3.44 against
-  // 4.04 with plain loads; L2-resident grids lose (2048^2 2.11 / 1.92, 1000^2
-  // 1.91 / 1.64, 500^2 1.45 / 0.89), and binary32 loses at every size (4096^2
-  // 1.68 / 1.16): its plain strips already load four rows ahead.
-  const bool big = nx * ny * int64_t(sizeof(T)) >= (int64_t(64) << 20);
+  // The TMA ring where it pays: binary64 arrays of 48 MiB and more (the pair
+  // beyond most of the L2), automatically; any aligned grid when forced
+  // (NPBGB_CFG_JACOBI_TMA = 2).  Measured on GB300 (TSTEPS=21 at 4096^2 and
+  // 2800^2, 41 at 2048^2, 100 at 1000^2 and 500^2; best settings of each
+  // form, ms): 4096^2 binary64 3.44 against 4.04 with plain loads, 2800^2
+  // 1.88 / 1.99; grids the L2 holds lose (2048^2, 32 MiB arrays: 2.11 / 1.92,
+  // 1000^2 1.91 / 1.64, 500^2 1.45 / 0.89), and binary32 loses at every size
+  // (4096^2 1.68 / 1.16): its plain strips already load four rows ahead.
+  const bool big = nx * ny * int64_t(sizeof(T)) >= (int64_t(48) << 20);
   if (g_cfg_jacobi_tma == 2 || (g_cfg_jacobi_tma == 1 && FX && big)) {
     // 16-row chunks and 3 of 8 warps on hardware binary64 measured best with the
     // ring at 4096^2 (3.44 ms; the plain form's 54-row chunks 3.63, 4 warps 3.61).
