@@ -64,9 +64,12 @@ extern "C" {
 #define NPBGB_CFG_JACOBI_HW_WARPS 8 /* jacobi2d / batch binary64: warps per CTA (of 8)
                                        that use hardware binary64 next to the
                                        fixed-point warps; -1 (default) = 4 */
-#define NPBGB_CFG_BATCH_CTAS_PER_SM 9 /* persistent and queue batch kernels: 2, 3
-                                         (default) or 4 CTAs per SM (the persistent form
-                                         uses 3 for 4); read when a batch is planned */
+#define NPBGB_CFG_BATCH_CTAS_PER_SM 9 /* persistent and queue batch kernels: 2 to 5
+                                         (default 5) CTAs per SM (the persistent form
+                                         uses 3 for 3 and more); read when a batch is
+                                         planned.  The queue form of the 4096-grid
+                                         batch: 0.91e11 / 1.14e11 / 1.32e11 updates/s
+                                         with 3 / 4 / 5. */
 #define NPBGB_CFG_PDL 10              /* 1 (default): the per-half-sweep launches of the
                                          time loops use programmatic dependent launch;
                                          0: plain stream order */
@@ -395,7 +398,7 @@ NPBGB_API int32_t npbgb_batch_destroy(npbgb_batch* batch);
  * npbgb_queue_create: up to max_slots grids in flight; tile_rows / tile_planes
  *   are the Jacobi-2D rows and Heat-3D planes per tile (0 = sized per grid for
  *   about one tile per worker CTA, 8-256 rows or 4-64 planes; a grid's band_rows
- *   overrides); ctas_per_sm (1-4, 0 = 3) sizes the worker launch;
+ *   overrides); ctas_per_sm (1-5, 0 = 3) sizes the worker launch;
  *   the worker ends after idle_us microseconds with nothing to do.  Device
  *   buffers and pinned host memory are allocated here, never later.
  * npbgb_queue_submit: takes a grid (npbgb_grid, step0/nsteps honoured) and

@@ -19,7 +19,7 @@ int64_t g_cfg_heat_rows = 0;     // 0: per-dtype default
 int64_t g_cfg_heat_hw_rows = -1; // -1: per-kernel default
 int64_t g_cfg_f64_cvt = 0;
 int64_t g_cfg_jacobi_hw_warps = -1;  // -1: default
-int64_t g_cfg_batch_ctas_per_sm = 3;
+int64_t g_cfg_batch_ctas_per_sm = 5;  // the persistent form takes 3 for 3 and more
 int64_t g_cfg_jacobi_chunk = 0;
 int64_t g_cfg_pdl = 1;
 int64_t g_cfg_batch_mode = 0;
@@ -161,7 +161,7 @@ int32_t npbgb_set_config(int32_t key, int64_t value) {
       g_cfg_jacobi_hw_warps = value;
       return NPBGB_OK;
     case NPBGB_CFG_BATCH_CTAS_PER_SM:
-      if (value < 2 || value > 4) return set_error(NPBGB_ERR_ARG, "batch CTAs per SM: 2, 3 or 4");
+      if (value < 2 || value > 5) return set_error(NPBGB_ERR_ARG, "batch CTAs per SM: 2 .. 5");
       g_cfg_batch_ctas_per_sm = value;
       return NPBGB_OK;
     case NPBGB_CFG_PDL:

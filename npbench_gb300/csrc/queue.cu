@@ -453,7 +453,9 @@ __global__ void __launch_bounds__(kQThreads, MINB) queue_worker(const QArgs q) {
 using WorkerFn = void (*)(const QArgs);
 
 WorkerFn worker_fn(int ctas_per_sm) {
-  return ctas_per_sm >= 4 ? queue_worker<4> : (ctas_per_sm == 3 ? queue_worker<3> : queue_worker<2>);
+  return ctas_per_sm >= 5   ? queue_worker<5>
+         : ctas_per_sm == 4 ? queue_worker<4>
+                            : (ctas_per_sm == 3 ? queue_worker<3> : queue_worker<2>);
 }
 
 }  // namespace
@@ -656,7 +658,7 @@ int32_t npbgb_queue_create(int32_t max_slots, int32_t tile_rows, int32_t tile_pl
   *out = nullptr;
   if (max_slots < 1 || max_slots > (1 << 20)) return set_error(NPBGB_ERR_ARG, "queue: max_slots");
   if (tile_rows < 0 || tile_planes < 0) return set_error(NPBGB_ERR_ARG, "queue: tile extents");
-  if (ctas_per_sm < 0 || ctas_per_sm > 4) return set_error(NPBGB_ERR_ARG, "queue: ctas_per_sm");
+  if (ctas_per_sm < 0 || ctas_per_sm > 5) return set_error(NPBGB_ERR_ARG, "queue: ctas_per_sm");
   if (idle_us < 0 || idle_us > 10000000) return set_error(NPBGB_ERR_ARG, "queue: idle_us");
   auto* q = new (std::nothrow) npbgb_queue();
   if (!q) return set_error(NPBGB_ERR_NOMEM, "queue: host allocation");
