@@ -143,7 +143,7 @@ extern "C" {
                                          Jacobi-2D grids whose rows are 16-byte
                                          multiples stream each warp's rows through a
                                          ring of TMA copies (1) or use plain loads
-                                         (0, default: the rings measured 1-1.5%
+                                         (0, default: the rings measured 1.5-2.6%
                                          slower on the 4096-grid batch, whose
                                          32-64-row tiles are short).  Results are
                                          identical. */

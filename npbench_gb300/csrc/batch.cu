@@ -525,8 +525,9 @@ int32_t plan_stepped(npbgb_batch* b, const npbgb_grid* grids, int64_t count, int
     // On request (NPBGB_CFG_BATCH_TMA), binary64 Jacobi-2D grids whose rows are
     // 16-byte multiples stream through each warp's ring of TMA copies (box: 34
     // columns x kTmaRows rows).  Off by default: on the 4096-grid batch the
-    // rings measured 1-1.5% slower than two rows loaded ahead (3.67 against
-    // 3.63 s per pass with 64-row tiles, 3.73 against 3.68 with 32).
+    // rings measured 1.5-2.6% slower than two rows loaded ahead (3.21 against
+    // 3.13 s per pass with 64-row tiles and 5 CTAs per SM; 3.73 against 3.68
+    // with 32-row tiles and 4).
     if (!heat && G.dtype == NPBGB_F64 && g_cfg_batch_tma && (G.n1 * 8) % 16 == 0) {
       CUtensorMap ma, mb;
       const uint64_t dims[3] = {uint64_t(G.n1), uint64_t(G.n0), 1u};

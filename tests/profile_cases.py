@@ -38,7 +38,8 @@ jacobi_f64_fx  Jacobi-2D 4096^2 float64, TSTEPS=3, every  jacobi2d_strip, -s 2
            warp in fixed point
 jacobi_f64_hw  the same, every warp on hardware binary64  jacobi2d_strip, -s 2
 batch1024  the first 1024 grids of the 4096-grid batch,   batch_step, -s 100
-           stepped form, TSTEPS as drawn (about 4 GB)
+           stepped form, TSTEPS as drawn, tuned tile rows,
+           float64 guard (about 5 GB)
 queue_mix  240 small mixed grids through the tile queue   queue_worker, -c 1
 pipes      the seven pipe-rate probes                     pipe_probe, -c 7
 ========== ============================================== ===================
@@ -207,7 +208,11 @@ def run(case):
             tdt = torch.float64 if dtp == np.float64 else torch.float32
             work.append((torch.rand((ny, nx), dtype=tdt, device=dev, generator=g),
                          torch.rand((ny, nx), dtype=tdt, device=dev, generator=g), T))
-        with Batch(work, band_rows=128, mode="stepped") as bt:
+        # the batched configuration's settings: its tuned tile rows and knobs, the float64 guard
+        from npbench_gb300 import autotune
+        tuned = autotune.batch_settings([(s_, dt_) for s_, dt_, _ in workloads.batch_jacobi_specs(4096, seed=0)])
+        with autotune.batch_applied(tuned), Batch(work, band_rows=tuned.get("rows", 64), mode="stepped",
+                                                  guard=True) as bt:
             bt.launch()
     elif case == "queue_mix":
         from npbench_gb300.queue import TileQueue
