@@ -286,7 +286,9 @@ batch_step(const StepGrid* __restrict__ grids, const int32_t* __restrict__ tile_
   } else if (G.dtype == NPBGB_F64) {
     const double* sp = static_cast<const double*>(src);
     double* dp = static_cast<double*>(dst);
-    // Two rows loaded ahead (tiles are 128 rows tall; measured 12% faster than one).
+    // Two rows loaded ahead (measured 12% faster than one with 128-row tiles; with
+    // 64-row tiles and 5 CTAs per SM three and four rows ahead spill and measured
+    // 3.77 and 3.88 s per pass of the 4096 grids against 3.13 s).
     if (!f64_emulation || warp < hw_warps)
       jcore::strip_rows<double, false, false, 2>(sp, dp, G.n1, k0, ib, ie, one);
     else
