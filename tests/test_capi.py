@@ -89,8 +89,14 @@ def test_argument_errors_are_status_codes_not_crashes():
     for key, bad in ((_lib.NPBGB_CFG_HEAT_STAGES, 5), (_lib.NPBGB_CFG_HEAT_STAGES, 2),
                      (_lib.NPBGB_CFG_JACOBI_BANDS_WARPS, 12), (_lib.NPBGB_CFG_JACOBI_BANDS, 3),
                      (_lib.NPBGB_CFG_LAUNCHES, 7), (_lib.NPBGB_CFG_HEAT_MAD_ROWS, 65),
-                     (_lib.NPBGB_CFG_HEAT_MAD_ROWS, -1)):
+                     (_lib.NPBGB_CFG_HEAT_MAD_ROWS, -1), (_lib.NPBGB_CFG_JACOBI_TMA, 3),
+                     (_lib.NPBGB_CFG_JACOBI_TMA, -1), (_lib.NPBGB_CFG_BATCH_TMA, 2),
+                     (_lib.NPBGB_CFG_BATCH_CTAS_PER_SM, 6), (_lib.NPBGB_CFG_BATCH_CTAS_PER_SM, 1)):
         assert lib.npbgb_set_config(key, bad) == _lib.NPBGB_ERR_ARG
+    # the rings: automatic for large binary64 Jacobi-2D grids, off for batches by default
+    assert _lib.get_config(_lib.NPBGB_CFG_JACOBI_TMA) == 1
+    assert _lib.get_config(_lib.NPBGB_CFG_BATCH_TMA) == 0
+    assert _lib.get_config(_lib.NPBGB_CFG_BATCH_CTAS_PER_SM) == 5
     assert _lib.get_config(_lib.NPBGB_CFG_HEAT_STAGES) == 0
     assert _lib.get_config(_lib.NPBGB_CFG_JACOBI_BANDS_WARPS) == 0
 
