@@ -212,8 +212,9 @@ __device__ __forceinline__ bool tma_strip_rows(const CUtensorMap* map, const T* 
   const int first = nbox < kTmaRing ? nbox : kTmaRing;
   if (lane == 0)
     for (int b = 0; b < first; ++b) issue(b);
-  int issued = first, waited = 1;
+  int issued = first, waited = 0;  // boxes issued; boxes whose wait completed
   bool ok = tma::mbar_wait(&bars[0], 0);
+  if (ok) waited = 1;
   S xp = S(0), xc = S(0), xn = S(0), hp = S(0), hc = S(0), hn = S(0);
   if (ok) {
     read(0, xp, hp);
@@ -224,8 +225,8 @@ __device__ __forceinline__ bool tma_strip_rows(const CUtensorMap* map, const T* 
     if (qn % kTmaRows == 0) {
       const int b = qn / kTmaRows;
       ok = tma::mbar_wait(&bars[b % kTmaRing], uint32_t((b / kTmaRing) & 1));
-      waited = b + 1;
       if (!ok) break;
+      waited = b + 1;
     }
     read(qn, xn, hn);
     if (qn % kTmaRows == kTmaRows - 1) {  // box fully read: refill its slot
@@ -242,7 +243,7 @@ __device__ __forceinline__ bool tma_strip_rows(const CUtensorMap* map, const T* 
     xc = xn;
     hc = hn;
   }
-  if (!ok)  // let the copies still in flight land (bounded) before the CTA may exit
+  if (!ok)  // let the copies still in flight (the late one included) land, bounded, before exit
     for (int b = waited; b < issued; ++b)
       tma::mbar_wait_for(&bars[b % kTmaRing], uint32_t((b / kTmaRing) & 1), tma::kWaitLimitNs / 16);
   return ok;
