@@ -141,13 +141,18 @@ heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ sr
   auto stage_ptr = [&](int q) -> S* {
     return reinterpret_cast<S*>(smem + (q % kStages) * G::kStride);
   };
+  int issued = 0;     // planes issued so far (thread 0 issues them, in order)
+  int next_wait = 0;  // planes this thread has seen land
   auto issue = [&](int q) {
     uint64_t* bar = &bars[q % kStages];
     tma::mbar_arrive_expect_tx(bar, G::kBytes);
     tma::load_3d(smem + (q % kStages) * G::kStride, &src_map, x0, y0, int(ib - 1 + q), bar);
+    issued = q + 1;
   };
   auto wait = [&](int q) -> bool {
-    return tma::mbar_wait(&bars[q % kStages], uint32_t((q / kStages) & 1));
+    const bool landed = tma::mbar_wait(&bars[q % kStages], uint32_t((q / kStages) & 1));
+    if (landed) next_wait = q + 1;
+    return landed;
   };
   auto convert = [&](int q) {
     if constexpr (FX) {
@@ -188,7 +193,12 @@ heat3d_tma(const __grid_constant__ CUtensorMap src_map, const T* __restrict__ sr
     }
     tma::fence_proxy_async();  // order this thread's generic smem accesses before later bulk writes
     if (__syncthreads_or(!ok)) {
-      if (tid == 0) atomicOr(&g_heat_error, 1u);
+      if (tid == 0) {
+        atomicOr(&g_heat_error, 1u);
+        // let the copies still in flight land (bounded) before the CTA exits
+        for (int q = next_wait; q < issued; ++q)
+          tma::mbar_wait_for(&bars[q % kStages], uint32_t((q / kStages) & 1), tma::kWaitLimitNs / 16);
+      }
       return;
     }
     if (tid == 0) {

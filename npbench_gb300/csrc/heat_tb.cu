@@ -81,11 +81,13 @@ heat3d_tb2(const __grid_constant__ CUtensorMap src_map, const float* __restrict_
   auto stage = [&](int64_t q) -> const float* {
     return reinterpret_cast<const float*>(smem + int((q - qlo) % kStages) * kStageStride);
   };
+  int64_t issued = qlo;  // next plane to issue (thread 0 issues them, in order)
   auto issue = [&](int64_t q) {
     const int st = int((q - qlo) % kStages);
     uint64_t* bar = &bars[st];
     tma::mbar_arrive_expect_tx(bar, kPlaneBytes);
     tma::load_3d(smem + st * kStageStride, &src_map, x0, y0, int(q), bar);
+    issued = q + 1;
   };
   auto wait = [&](int64_t q) -> bool {
     const int r = int(q - qlo);
@@ -183,7 +185,14 @@ heat3d_tb2(const __grid_constant__ CUtensorMap src_map, const float* __restrict_
     }
     tma::fence_proxy_async();  // this thread's reads of the stage before it is refilled
     if (__syncthreads_or(!ok)) {
-      if (tid == 0) atomicOr(&g_heat_tb_error, 1u);
+      if (tid == 0) {
+        atomicOr(&g_heat_tb_error, 1u);
+        // let the copies still in flight (the late one included) land, bounded, before exit
+        for (int64_t q = ok ? waited + 1 : waited; q < issued; ++q) {
+          const int r = int(q - qlo);
+          tma::mbar_wait_for(&bars[r % kStages], uint32_t((r / kStages) & 1), tma::kWaitLimitNs / 16);
+        }
+      }
       return;
     }
     // Input plane p-1 is no longer needed: refill its buffer kStages planes on.
