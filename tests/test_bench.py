@@ -53,6 +53,23 @@ def test_reference_arm_prints_once_under_torchrun():
     assert len(lines) == 1 and lines[0]["impl"] == "reference" and lines[0]["n_gpus"] == 2
 
 
+def test_compute_roofline_from_committed_instruction_mix():
+    """The arithmetic roof of the headline kernel: the committed ncu instruction counts per
+    update against given pipe rates; the tightest pipe is the bound."""
+    import bench
+    rates = {"lop3": 2.0e13, "dadd": 5.26e11, "imad": 2.0e13, "issue_slots": 4.03e13}
+    rec = bench._ncu_record("heat3d_f64_256")["inst_per_update"]
+    r = bench.compute_roofline("heat3d_f64_256", 1.3e11, rates)
+    limits = r["per_pipe_ceiling_updates_per_s"]
+    assert limits["alu"] == pytest.approx(2.0e13 / rec["alu"])
+    assert limits["fp64"] == pytest.approx(5.26e11 / rec["fp64"])
+    assert limits["issue"] == pytest.approx(4.03e13 / rec["issue"])
+    assert r["ceiling_updates_per_s"] == min(limits.values())
+    assert r["bound"] == min(limits, key=limits.get)
+    assert r["frac"] == pytest.approx(1.3e11 / r["ceiling_updates_per_s"])
+    assert bench.compute_roofline("no_such_kernel", 1.0, rates) is None
+
+
 @pytest.mark.gpu
 def test_default_run_line():
     torch = pytest.importorskip("torch")
