@@ -125,6 +125,32 @@ def test_shipped_table_is_consulted_after_the_user_cache(cache, monkeypatch, tmp
     autotune.load_cache(refresh=True)
 
 
+def test_shipped_table_names_known_knobs_with_accepted_values():
+    """Every setting in the shipped table is a knob the library accepts (set and read back
+    through the C ABI), a batch's tile rows, or one of the serving loop's parameters."""
+    import json
+    from npbench_gb300 import _lib
+    with open(autotune.SHIPPED_PATH) as f:
+        table = json.load(f)
+    server_keys = set(autotune._SERVER_DEFAULT)
+    for key, entry in table.items():
+        cfg = entry["config"]
+        if key.startswith("serve/"):
+            assert set(cfg) <= server_keys, key
+            continue
+        for name, value in cfg.items():
+            if key.startswith("batch/") and name == "rows":
+                assert value > 0, key
+                continue
+            assert name in autotune._KNOBS, (key, name)
+            old = _lib.get_config(autotune._KNOBS[name])
+            try:
+                _lib.set_config(autotune._KNOBS[name], value)  # raises for a refused value
+                assert _lib.get_config(autotune._KNOBS[name]) == value, (key, name)
+            finally:
+                _lib.set_config(autotune._KNOBS[name], old)
+
+
 def test_store_merges_entries(cache):
     autotune._store("a/float64/1x1", {"config": {}, "ms": 1.0})
     autotune._store("b/float64/2x2", {"config": {}, "ms": 2.0})
